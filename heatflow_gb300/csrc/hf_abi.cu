@@ -1,0 +1,748 @@
+// C ABI of libheatflow_gb300 (include/heatflow_gb300.h): context set-up, state transfer and the
+// host side of the step loop.  Host arithmetic here is the reference's set-up arithmetic
+// (cell lengths, volumes, heated volume, Neumann power densities) and is compiled without FMA
+// contraction so it rounds as the reference does.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "hf_ctx.cuh"
+
+namespace hf {
+cudaError_t launch_props(Ctx& c, const double* rho, const double* hc, const double* tau,
+                         const double* em);
+}
+
+using namespace hf;
+
+struct hf_ctx {
+  Ctx c;
+};
+
+static thread_local std::string g_err;
+
+static int set_err(int code, const std::string& msg) {
+  g_err = msg;
+  return code;
+}
+
+#define CU(call)                                                                         \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return set_err(HF_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_));      \
+  } while (0)
+
+extern "C" {
+
+int hf_abi_version(void) { return HF_ABI_VERSION; }
+
+const char* hf_strerror(int code) {
+  switch (code) {
+    case HF_OK: return "ok";
+    case HF_EARG: return "invalid argument";
+    case HF_ECUDA: return "CUDA error";
+    case HF_ENOMEM: return "device allocation failed";
+    case HF_ESTATE: return "call order error";
+    case HF_EDEVICE: return "device-side check failed";
+    case HF_ENAN_B: return "fatal error: NAN in B vector";
+    case HF_ENAN_Q: return "fatal error: NAN in Q vector";
+    case HF_ENAN_QDENS: return "fatal error: NAN in Qdens vector";
+    case HF_ENAN_SCAT: return "fatal error: NAN in S_CAT vector";
+    case HF_ENAN_S: return "fatal error: NAN in S vector";
+    case HF_ENAN_X: return "fatal error: NAN in x tempurature vector";
+    default: return "unknown status";
+  }
+}
+
+const char* hf_last_error(void) { return g_err.c_str(); }
+
+void hf_default_opts(hf_solver_opts* o) {
+  if (!o) return;
+  std::memset(o, 0, sizeof(*o));
+  o->precision = HF_PREC_FP64;
+  o->criterion = HF_STOP_RECURSIVE;
+  o->tol = 1.0e-32;        // mod_evolve.f90:143
+  o->itmax = 50000;        // mod_evolve.f90:144
+  o->inner_tol = 1.0e-4;
+  o->inner_itmax = 200;
+  o->max_refine = 20;
+  o->check_every = 2;
+  o->use_graph = 0;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+namespace {
+
+template <typename T>
+int dalloc(Ctx& c, T** p, size_t count) {
+  void* q = nullptr;
+  size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+  cudaError_t e = cudaMalloc(&q, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return set_err(HF_ENOMEM, std::string("cudaMalloc ") + std::to_string(bytes) + " bytes: " +
+                                  cudaGetErrorString(e));
+  }
+  c.allocs.push_back(q);
+  *p = static_cast<T*>(q);
+  return HF_OK;
+}
+
+void free_all(Ctx& c) {
+  if (c.graph_exec) cudaGraphExecDestroy(c.graph_exec);
+  for (void* p : c.allocs) cudaFree(p);
+  c.allocs.clear();
+  if (c.h_scal) cudaFreeHost(c.h_scal);
+  c.h_scal = nullptr;
+  if (c.own_stream && c.stream) cudaStreamDestroy(c.stream);
+  c.stream = nullptr;
+}
+
+DevOpts dev_opts(const hf_solver_opts& o) {
+  DevOpts d{};
+  d.precision = o.precision;
+  d.criterion = o.criterion;
+  d.tol = o.tol;
+  d.itmax = o.itmax;
+  d.inner_tol = o.inner_tol;
+  d.inner_itmax = o.inner_itmax;
+  d.max_refine = o.max_refine;
+  return d;
+}
+
+int validate_opts(const hf_solver_opts& o) {
+  if (o.precision != HF_PREC_FP64 && o.precision != HF_PREC_MIXED)
+    return set_err(HF_EARG, "precision must be HF_PREC_FP64 or HF_PREC_MIXED");
+  if (o.criterion != HF_STOP_RECURSIVE && o.criterion != HF_STOP_TRUE)
+    return set_err(HF_EARG, "criterion must be HF_STOP_RECURSIVE or HF_STOP_TRUE");
+  if (o.criterion == HF_STOP_RECURSIVE && o.precision != HF_PREC_FP64)
+    return set_err(HF_EARG, "the reference's recursive criterion is defined for the FP64 path");
+  if (!(o.tol >= 0.0) || o.itmax < 1 || o.inner_itmax < 1 || o.max_refine < 1 || o.check_every < 1)
+    return set_err(HF_EARG, "tol >= 0, itmax, inner_itmax, max_refine, check_every >= 1");
+  return HF_OK;
+}
+
+int sync_scal(Ctx& c) {
+  CU(cudaMemcpyAsync(c.h_scal, c.A.scal, sizeof(InstScal) * c.ninst, cudaMemcpyDeviceToHost,
+                     c.stream));
+  CU(cudaStreamSynchronize(c.stream));
+  return HF_OK;
+}
+
+int push_scal(Ctx& c) {
+  CU(cudaMemcpyAsync(c.A.scal, c.h_scal, sizeof(InstScal) * c.ninst, cudaMemcpyHostToDevice,
+                     c.stream));
+  CU(cudaStreamSynchronize(c.stream));
+  return HF_OK;
+}
+
+// First NaN code of an instance's status bits, in the reference's check order.
+int status_code(int bits) {
+  for (int k = 0; k <= HF_ENAN_X - HF_ENAN_B; ++k)
+    if (bits & (1 << k)) return HF_ENAN_B + k;
+  return HF_OK;
+}
+
+// Drive one step's solve after the RHS / initial residual kernels are queued.
+int solve_loop(Ctx& c) {
+  const bool fp32 = c.opts.precision == HF_PREC_MIXED;
+  const int64_t per_solve = fp32 ? c.opts.inner_itmax : c.opts.itmax;
+  const int64_t guard = (int64_t)(c.opts.max_refine + 3) * (per_solve / c.opts.check_every + 3);
+  for (int64_t it = 0; it < guard; ++it) {
+    int rc = sync_scal(c);
+    if (rc) return rc;
+    bool any_outer = false, any_inner = false;
+    for (int64_t i = 0; i < c.ninst; ++i) {
+      any_outer |= c.h_scal[i].outer_active != 0;
+      any_inner |= c.h_scal[i].inner_active != 0;
+    }
+    if (!any_outer) return HF_OK;
+    if (any_inner) {
+      for (int k = 0; k < c.opts.check_every; ++k) CU(launch_inner_iteration(c, fp32 ? 1 : 0));
+    } else {
+      CU(launch_residual(c, 1));
+    }
+  }
+  return set_err(HF_EDEVICE, "solve loop did not terminate within its bound");
+}
+
+int run_one_step(Ctx& c, int64_t itime) {
+  CU(launch_step_begin(c, itime, 0));
+  CU(launch_rhs(c));
+  CU(launch_residual(c, 0));
+  int rc = solve_loop(c);
+  if (rc) return rc;
+  CU(launch_step_end(c));
+  return HF_OK;
+}
+
+void fill_stats(Ctx& c, hf_stats* st, int64_t steps, const std::vector<InstScal>& before) {
+  if (!st) return;
+  std::memset(st, 0, sizeof(*st));
+  st->steps = steps;
+  st->failed_step = -1;
+  st->failed_instance = -1;
+  for (int64_t i = 0; i < c.ninst; ++i) {
+    const InstScal& s = c.h_scal[i];
+    const InstScal& b = before[i];
+    st->iterations += s.tot_iters - b.tot_iters;
+    st->inner_iterations += s.tot_inner - b.tot_inner;
+    st->refinements += s.tot_refine - b.tot_refine;
+    st->unconverged += s.unconverged - b.unconverged;
+    st->last_iter = std::max<int64_t>(st->last_iter, s.last_iter);
+    st->last_err = std::max(st->last_err, s.last_err);
+    st->last_true_relres = std::max(st->last_true_relres, s.last_relres);
+    if (s.status && st->failed_instance < 0) {
+      st->failed_instance = (int32_t)i;
+      st->failed_step = s.failed_step;
+      st->status = status_code(s.status);
+    }
+  }
+}
+
+int first_error(Ctx& c) {
+  for (int64_t i = 0; i < c.ninst; ++i) {
+    if (c.h_scal[i].status) return status_code(c.h_scal[i].status);
+    if (c.h_scal[i].devcheck)
+      return set_err(HF_EDEVICE, "assembly consistency check failed on instance " +
+                                     std::to_string(i) + " (code " +
+                                     std::to_string(c.h_scal[i].devcheck) + ")");
+  }
+  return HF_OK;
+}
+
+// Copy a per-instance host array (concatenated, unpadded) to a padded device array.
+template <typename T>
+int upload_padded(Ctx& c, T* dst, const T* src) {
+  int64_t pos = 0;
+  for (int64_t i = 0; i < c.ninst; ++i) {
+    const InstDesc& d = c.h_inst[i];
+    CU(cudaMemcpyAsync(dst + d.off, src + pos, sizeof(T) * d.n, cudaMemcpyHostToDevice, c.stream));
+    pos += d.n;
+  }
+  return HF_OK;
+}
+
+template <typename T>
+int download_padded(Ctx& c, T* dst, const T* src) {
+  int64_t pos = 0;
+  for (int64_t i = 0; i < c.ninst; ++i) {
+    const InstDesc& d = c.h_inst[i];
+    CU(cudaMemcpyAsync(dst + pos, src + d.off, sizeof(T) * d.n, cudaMemcpyDeviceToHost, c.stream));
+    pos += d.n;
+  }
+  return HF_OK;
+}
+
+int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* opts, hf_ctx** out) {
+  if (!probs || count < 1 || !out) return set_err(HF_EARG, "null problem/out or count < 1");
+  *out = nullptr;
+  hf_solver_opts o;
+  if (opts) o = *opts; else hf_default_opts(&o);
+  int rc = validate_opts(o);
+  if (rc) return rc;
+  for (int64_t i = 0; i < count; ++i) {
+    const hf_problem& p = probs[i];
+    if (p.nx < 1 || p.ny < 1 || p.nz < 1) return set_err(HF_EARG, "grid dimensions must be >= 1");
+    const int64_t n = p.nx * p.ny * p.nz;
+    if (n >= (int64_t(1) << 31)) return set_err(HF_EARG, "more than 2^31-1 cells in one grid");
+    if (p.nx == 1 && n > 1)
+      return set_err(HF_EARG, "nx = 1 with more than one cell: the reference's COO assembly "
+                              "(sparse_Hmatrix) writes past its capacity for such grids");
+    if (!p.kappa || !p.rho || !p.heat_capacity) return set_err(HF_EARG, "kappa, rho, heat_capacity required");
+    if (!(p.time_step > 0.0)) return set_err(HF_EARG, "time_step must be > 0");
+    if (!(p.lx > 0.0 && p.ly > 0.0 && p.lz > 0.0)) return set_err(HF_EARG, "box lengths must be > 0");
+  }
+  hf_ctx* h = new hf_ctx();
+  Ctx& c = h->c;
+  c.opts = o;
+  if (cudaGetDevice(&c.device) != cudaSuccess) { delete h; return set_err(HF_ECUDA, "no CUDA device"); }
+  if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete h;
+    return set_err(HF_ECUDA, "cudaStreamCreate failed");
+  }
+  c.own_stream = true;
+  c.ninst = count;
+  // ---- layout: instances at multiples of kTile cells
+  int64_t off = 0, tiles = 0;
+  std::vector<int32_t> tile_inst;
+  c.h_inst.resize(count);
+  c.h_bc.resize(count);
+  for (int64_t i = 0; i < count; ++i) {
+    const hf_problem& p = probs[i];
+    InstDesc& d = c.h_inst[i];
+    std::memset(&d, 0, sizeof(d));
+    d.nx = (int32_t)p.nx; d.ny = (int32_t)p.ny; d.nz = (int32_t)p.nz;
+    d.n = (int32_t)(p.nx * p.ny * p.nz);
+    d.off = off;
+    d.tile0 = tiles;
+    d.ntiles = (int32_t)((d.n + kTile - 1) / kTile);
+    for (int t = 0; t < d.ntiles; ++t) tile_inst.push_back((int32_t)i);
+    tiles += d.ntiles;
+    off += (int64_t)d.ntiles * kTile;
+    d.px = p.periodic[0] ? 1 : 0; d.py = p.periodic[1] ? 1 : 0; d.pz = p.periodic[2] ? 1 : 0;
+    d.icattaneo = p.icattaneo; d.isteady = p.isteady;
+    d.qdens_mode = p.qdens_mode;
+    d.time_step = p.time_step;
+    d.inv_dt = 1.0 / p.time_step;                       // mod_setup.f90:45
+    d.freq = p.freq;
+    d.power_in = p.power_in;
+    d.time_pulse = (double)p.heated_steps * p.time_step; // mod_heating.f90:41
+    d.t_bath = p.t_bath;
+    // Length = L/real(n) (default-real conversion of n), volume = L1*L2*L3 (mod_inputs.f90:619-622)
+    d.len[0] = p.lx / (double)(float)p.nx;
+    d.len[1] = p.ly / (double)(float)p.ny;
+    d.len[2] = p.lz / (double)(float)p.nz;
+    d.volume = d.len[0] * d.len[1] * d.len[2];
+    double hv = 0.0;
+    bool heater = false, case5 = false, em = false;
+    for (int64_t k = 0; k < d.n; ++k) {
+      int64_t ih = p.iheater ? p.iheater[k] : 0;
+      if (ih > 0) { heater = true; hv = hv + d.volume; }   // mod_heating.f90:145-148
+      if (ih == 5) case5 = true;
+      if (p.em && p.em[k] != 0.0) em = true;
+    }
+    d.heater = heater ? 1 : 0;
+    d.has_case5 = case5 ? 1 : 0;
+    d.has_em = (heater && em) ? 1 : 0;
+    d.has_power = (heater && p.power) ? 1 : 0;
+    d.heated_volume = hv;
+    InstBC& bc = c.h_bc[i];
+    for (int f = 0; f < 6; ++f) {
+      bc.kb[f] = p.kappa_bound[f];
+      bc.tb[f] = p.t_bath_face[f];
+      bc.cg[f] = p.cg_face[f] ? 1 : 0;
+      bc.pd[f] = 0.0;
+    }
+    bc.br = p.br;
+    // Neumann power densities, mod_boundary.f90:43-66 (T_BathCG / (volume * n_a * n_b))
+    const double nxd = (double)p.nx, nyd = (double)p.ny, nzd = (double)p.nz;
+    if (bc.cg[4]) bc.pd[4] = p.t_bath_cg / (d.volume * nxd * nyd);
+    if (bc.cg[5]) bc.pd[5] = p.t_bath_cg / (d.volume * nxd * nyd);
+    if (bc.cg[2]) bc.pd[2] = p.t_bath_cg / (d.volume * nxd * nzd);
+    if (bc.cg[3]) bc.pd[3] = p.t_bath_cg / (d.volume * nxd * nzd);
+    if (bc.cg[0]) bc.pd[0] = p.t_bath_cg / (d.volume * nyd * nzd);
+    if (bc.cg[1]) bc.pd[1] = p.t_bath_cg / (d.volume * nyd * nzd);
+    c.any_heater |= heater;
+    c.any_power |= (heater && p.power);
+    c.any_em |= (heater && em);
+    c.any_case5 |= case5;
+  }
+  c.ncells = off;
+  c.ntiles = tiles;
+  const size_t N = (size_t)c.ncells;
+  // ---- device memory
+  DevArrays& A = c.A;
+  std::memset(&A, 0, sizeof(A));
+  A.ncells = c.ncells; A.ntiles = c.ntiles; A.ninst = c.ninst;
+  A.opts = dev_opts(o);
+#define ALLOC(ptr, n) do { int r_ = dalloc(c, &(ptr), (n)); if (r_) { free_all(c); delete h; return r_; } } while (0)
+  InstDesc* d_inst; InstScal* d_scal; int32_t* d_tile_inst;
+  ALLOC(d_inst, (size_t)count);
+  ALLOC(d_scal, (size_t)count);
+  ALLOC(d_tile_inst, (size_t)tiles);
+  ALLOC(A.partials, (size_t)tiles * kNR);
+  ALLOC(A.counters, (size_t)count);
+  ALLOC(c.d_bc, (size_t)count);
+  A.inst = d_inst; A.scal = d_scal; A.tile_inst = d_tile_inst;
+  ALLOC(A.diag, N); ALLOC(A.cx, N); ALLOC(A.cy, N); ALLOC(A.cz, N); ALLOC(A.sinv, N);
+  ALLOC(A.a64x, N); ALLOC(A.a64y, N); ALLOC(A.a64z, N);
+  ALLOC(A.a32x, N); ALLOC(A.a32y, N); ALLOC(A.a32z, N);
+  ALLOC(A.rhoc, N); ALLOC(A.ccat, N); ALLOC(A.bvec, N); ALLOC(A.tau_s, N);
+  ALLOC(c.asm_.kappa, N);
+  if (c.any_power) ALLOC(A.power, N);
+  if (c.any_em) ALLOC(A.emc, N);
+  if (c.any_heater) ALLOC(A.icase, N);
+  for (int k = 0; k < 4; ++k) ALLOC(A.tbuf[k], N);
+  ALLOC(A.b, N); ALLOC(A.y, N); ALLOC(A.r, N); ALLOC(A.p, N); ALLOC(A.q, N);
+  ALLOC(A.y32, N); ALLOC(A.r32, N); ALLOC(A.p32, N); ALLOC(A.q32, N);
+  double *d_rho, *d_hc, *d_tau, *d_em = nullptr;
+  ALLOC(d_rho, N); ALLOC(d_hc, N); ALLOC(d_tau, N);
+  if (c.any_em) ALLOC(d_em, N);
+#undef ALLOC
+  if (cudaMallocHost((void**)&c.h_scal, sizeof(InstScal) * count) != cudaSuccess) {
+    free_all(c); delete h; return set_err(HF_ENOMEM, "cudaMallocHost failed");
+  }
+  auto fail = [&](int r) { free_all(c); delete h; return r; };
+#define CK(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) return fail(set_err(HF_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_))); } while (0)
+  CK(cudaMemsetAsync(A.counters, 0, sizeof(unsigned) * count, c.stream));
+  CK(cudaMemsetAsync(d_scal, 0, sizeof(InstScal) * count, c.stream));
+  for (void* p : {(void*)A.diag, (void*)A.cx, (void*)A.cy, (void*)A.cz, (void*)c.asm_.kappa,
+                  (void*)d_rho, (void*)d_hc, (void*)d_tau, (void*)A.rhoc, (void*)A.ccat,
+                  (void*)A.bvec, (void*)A.tau_s, (void*)A.a64x, (void*)A.a64y, (void*)A.a64z,
+                  (void*)A.b, (void*)A.y, (void*)A.r, (void*)A.p, (void*)A.q})
+    CK(cudaMemsetAsync(p, 0, N * sizeof(double), c.stream));
+  for (void* p : {(void*)A.a32x, (void*)A.a32y, (void*)A.a32z, (void*)A.y32, (void*)A.r32,
+                  (void*)A.p32, (void*)A.q32})
+    CK(cudaMemsetAsync(p, 0, N * sizeof(float), c.stream));
+  for (int k = 0; k < 4; ++k) CK(cudaMemsetAsync(A.tbuf[k], 0, N * sizeof(double), c.stream));
+  if (d_em) CK(cudaMemsetAsync(d_em, 0, N * sizeof(double), c.stream));
+  if (A.power) CK(cudaMemsetAsync(A.power, 0, N * sizeof(double), c.stream));
+  if (A.icase) CK(cudaMemsetAsync(A.icase, 0, N, c.stream));
+  CK(cudaMemcpyAsync(d_inst, c.h_inst.data(), sizeof(InstDesc) * count, cudaMemcpyHostToDevice, c.stream));
+  CK(cudaMemcpyAsync(c.d_bc, c.h_bc.data(), sizeof(InstBC) * count, cudaMemcpyHostToDevice, c.stream));
+  CK(cudaMemcpyAsync(d_tile_inst, tile_inst.data(), sizeof(int32_t) * tiles, cudaMemcpyHostToDevice, c.stream));
+  // per-cell inputs into the padded layout
+  std::vector<int8_t> icase;
+  for (int64_t i = 0; i < count; ++i) {
+    const hf_problem& p = probs[i];
+    const InstDesc& d = c.h_inst[i];
+    CK(cudaMemcpyAsync(c.asm_.kappa + d.off, p.kappa, 8 * d.n, cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemcpyAsync(d_rho + d.off, p.rho, 8 * d.n, cudaMemcpyHostToDevice, c.stream));
+    CK(cudaMemcpyAsync(d_hc + d.off, p.heat_capacity, 8 * d.n, cudaMemcpyHostToDevice, c.stream));
+    if (p.tau) CK(cudaMemcpyAsync(d_tau + d.off, p.tau, 8 * d.n, cudaMemcpyHostToDevice, c.stream));
+    if (d_em && p.em) CK(cudaMemcpyAsync(d_em + d.off, p.em, 8 * d.n, cudaMemcpyHostToDevice, c.stream));
+    if (A.power) {
+      if (p.power) {
+        CK(cudaMemcpyAsync(A.power + d.off, p.power, 8 * d.n, cudaMemcpyHostToDevice, c.stream));
+      } else {
+        std::vector<double> pw((size_t)d.n, p.power_in);
+        CK(cudaMemcpyAsync(A.power + d.off, pw.data(), 8 * d.n, cudaMemcpyHostToDevice, c.stream));
+        CK(cudaStreamSynchronize(c.stream));
+      }
+    }
+    if (A.icase) {
+      icase.assign((size_t)d.n, 0);
+      for (int64_t k = 0; k < d.n; ++k) {
+        int64_t ih = p.iheater ? p.iheater[k] : 0;
+        icase[k] = (int8_t)(ih < 0 ? -1 : (ih > 6 ? 7 : ih));
+      }
+      CK(cudaMemcpyAsync(A.icase + d.off, icase.data(), d.n, cudaMemcpyHostToDevice, c.stream));
+      CK(cudaStreamSynchronize(c.stream));
+    }
+  }
+  CK(launch_props(c, d_rho, d_hc, d_tau, d_em));
+  CK(launch_assemble(c));
+  CK(cudaStreamSynchronize(c.stream));
+  // mean of sinv over a strided sample of each instance (scaling of FP32 right-hand sides)
+  for (int64_t i = 0; i < count; ++i) {
+    InstDesc& d = c.h_inst[i];
+    const int64_t m = std::min<int64_t>(d.n, 4096);
+    const int64_t stride = d.n / m;
+    std::vector<double> smp((size_t)m);
+    CK(cudaMemcpy2D(smp.data(), sizeof(double), A.sinv + d.off, sizeof(double) * stride,
+                    sizeof(double), (size_t)m, cudaMemcpyDeviceToHost));
+    double acc = 0.0;
+    for (double v : smp) acc += v;
+    d.mean_sinv = acc / (double)m;
+  }
+  CK(cudaMemcpyAsync(d_inst, c.h_inst.data(), sizeof(InstDesc) * count, cudaMemcpyHostToDevice, c.stream));
+  // initial scalars: roles 0..3, status from assembly
+  CK(cudaMemcpyAsync(c.h_scal, d_scal, sizeof(InstScal) * count, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  for (int64_t i = 0; i < count; ++i) {
+    InstScal& s = c.h_scal[i];
+    s.role[0] = 0; s.role[1] = 1; s.role[2] = 2; s.role[3] = 3;
+    s.sigma = 1.0; s.sigma_prev = 1.0;
+    s.failed_step = -1;
+  }
+  CK(cudaMemcpyAsync(d_scal, c.h_scal, sizeof(InstScal) * count, cudaMemcpyHostToDevice, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+#undef CK
+  // the temporary property inputs are no longer needed
+  for (void* p : {(void*)d_rho, (void*)d_hc, (void*)d_tau, (void*)d_em}) {
+    if (!p) continue;
+    cudaFree(p);
+    c.allocs.erase(std::remove(c.allocs.begin(), c.allocs.end(), p), c.allocs.end());
+  }
+  for (int64_t i = 0; i < count; ++i) {
+    if (c.h_scal[i].devcheck) {
+      int r = set_err(HF_EDEVICE, "assembly consistency check failed (code " +
+                                      std::to_string(c.h_scal[i].devcheck) + ", instance " +
+                                      std::to_string(i) + "): operator diagonal must be < 0");
+      free_all(c);
+      delete h;
+      return r;
+    }
+  }
+  *out = h;
+  return HF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int hf_create(const hf_problem* prob, const hf_solver_opts* opts, hf_ctx** out) {
+  return create_impl(prob, 1, opts, out);
+}
+
+int hf_create_batch(const hf_problem* probs, int64_t count, const hf_solver_opts* opts, hf_ctx** out) {
+  return create_impl(probs, count, opts, out);
+}
+
+int hf_destroy(hf_ctx* h) {
+  if (!h) return HF_OK;
+  cudaStreamSynchronize(h->c.stream);
+  free_all(h->c);
+  delete h;
+  return HF_OK;
+}
+
+int hf_set_opts(hf_ctx* h, const hf_solver_opts* opts) {
+  if (!h || !opts) return set_err(HF_EARG, "null argument");
+  int rc = validate_opts(*opts);
+  if (rc) return rc;
+  h->c.opts = *opts;
+  h->c.A.opts = dev_opts(*opts);
+  return HF_OK;
+}
+
+int hf_get_sizes(const hf_ctx* h, int64_t* instances, int64_t* total_cells) {
+  if (!h) return set_err(HF_EARG, "null context");
+  int64_t tot = 0;
+  for (const auto& d : h->c.h_inst) tot += d.n;
+  if (instances) *instances = h->c.ninst;
+  if (total_cells) *total_cells = tot;
+  return HF_OK;
+}
+
+int64_t hf_instance_cells(const hf_ctx* h, int64_t i) {
+  if (!h || i < 0 || i >= h->c.ninst) return -1;
+  return h->c.h_inst[i].n;
+}
+
+int hf_set_stream(hf_ctx* h, void* stream) {
+  if (!h) return set_err(HF_EARG, "null context");
+  Ctx& c = h->c;
+  CU(cudaStreamSynchronize(c.stream));
+  if (stream) {
+    if (c.own_stream) cudaStreamDestroy(c.stream);
+    c.stream = (cudaStream_t)stream;
+    c.own_stream = false;
+  } else if (!c.own_stream) {
+    CU(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+    c.own_stream = true;
+  }
+  return HF_OK;
+}
+
+int hf_set_state(hf_ctx* h, const double* tp, const double* tpp) {
+  if (!h || !tp || !tpp) return set_err(HF_EARG, "null argument");
+  Ctx& c = h->c;
+  int rc = sync_scal(c);
+  if (rc) return rc;
+  int64_t pos = 0;
+  for (int64_t i = 0; i < c.ninst; ++i) {
+    const InstDesc& d = c.h_inst[i];
+    const InstScal& s = c.h_scal[i];
+    CU(cudaMemcpyAsync(c.A.tbuf[s.role[0]] + d.off, tp + pos, 8 * d.n, cudaMemcpyHostToDevice, c.stream));
+    CU(cudaMemcpyAsync(c.A.tbuf[s.role[1]] + d.off, tpp + pos, 8 * d.n, cudaMemcpyHostToDevice, c.stream));
+    pos += d.n;
+  }
+  CU(cudaStreamSynchronize(c.stream));
+  c.state_set = true;
+  return HF_OK;
+}
+
+int hf_get_state(hf_ctx* h, double* tp, double* tpp) {
+  if (!h) return set_err(HF_EARG, "null context");
+  Ctx& c = h->c;
+  int rc = sync_scal(c);
+  if (rc) return rc;
+  int64_t pos = 0;
+  for (int64_t i = 0; i < c.ninst; ++i) {
+    const InstDesc& d = c.h_inst[i];
+    const InstScal& s = c.h_scal[i];
+    if (tp) CU(cudaMemcpyAsync(tp + pos, c.A.tbuf[s.role[0]] + d.off, 8 * d.n, cudaMemcpyDeviceToHost, c.stream));
+    if (tpp) CU(cudaMemcpyAsync(tpp + pos, c.A.tbuf[s.role[1]] + d.off, 8 * d.n, cudaMemcpyDeviceToHost, c.stream));
+    pos += d.n;
+  }
+  CU(cudaStreamSynchronize(c.stream));
+  return HF_OK;
+}
+
+int hf_state_device(hf_ctx* h, double** tp, double** tpp) {
+  if (!h) return set_err(HF_EARG, "null context");
+  Ctx& c = h->c;
+  if (c.ninst != 1) return set_err(HF_EARG, "device state pointers are for single-grid contexts");
+  int rc = sync_scal(c);
+  if (rc) return rc;
+  if (tp) *tp = c.A.tbuf[c.h_scal[0].role[0]];
+  if (tpp) *tpp = c.A.tbuf[c.h_scal[0].role[1]];
+  return HF_OK;
+}
+
+int hf_state_device_ready(hf_ctx* h) {
+  if (!h) return set_err(HF_EARG, "null context");
+  h->c.state_set = true;
+  return HF_OK;
+}
+
+int hf_step(hf_ctx* h, int64_t itime, hf_stats* stats) {
+  return hf_run(h, itime, 1, stats);
+}
+
+int hf_run(hf_ctx* h, int64_t itime0, int64_t nsteps, hf_stats* stats) {
+  if (!h || nsteps < 0) return set_err(HF_EARG, "null context or nsteps < 0");
+  Ctx& c = h->c;
+  if (!c.state_set) return set_err(HF_ESTATE, "hf_set_state must be called before stepping");
+  int rc = sync_scal(c);
+  if (rc) return rc;
+  std::vector<InstScal> before(c.h_scal, c.h_scal + c.ninst);
+  int64_t done = 0;
+  for (int64_t k = 0; k < nsteps; ++k) {
+    rc = run_one_step(c, itime0 + k);
+    if (rc) return rc;
+    ++done;
+    if (c.ninst == 1) {
+      if (c.h_scal[0].status) break;   // the reference stops at the first fatal error
+    }
+  }
+  rc = sync_scal(c);
+  if (rc) return rc;
+  fill_stats(c, stats, done, before);
+  return first_error(c);
+}
+
+int hf_get_operator(hf_ctx* h, double* diag, double* cx, double* cy, double* cz) {
+  if (!h) return set_err(HF_EARG, "null context");
+  Ctx& c = h->c;
+  int rc;
+  if (diag && (rc = download_padded(c, diag, c.A.diag))) return rc;
+  if (cx && (rc = download_padded(c, cx, c.A.cx))) return rc;
+  if (cy && (rc = download_padded(c, cy, c.A.cy))) return rc;
+  if (cz && (rc = download_padded(c, cz, c.A.cz))) return rc;
+  CU(cudaStreamSynchronize(c.stream));
+  return HF_OK;
+}
+
+int hf_apply_operator(hf_ctx* h, const double* x, double* y) {
+  if (!h || !x || !y) return set_err(HF_EARG, "null argument");
+  Ctx& c = h->c;
+  int rc;
+  if ((rc = upload_padded(c, c.A.p, x))) return rc;   // p and q are free outside a step
+  CU(launch_apply(c, c.A.p, c.A.q));
+  if ((rc = download_padded(c, y, c.A.q))) return rc;
+  CU(cudaStreamSynchronize(c.stream));
+  return HF_OK;
+}
+
+int hf_get_rhs(hf_ctx* h, int64_t itime, double* B, double* Q, double* Qd, double* sc, double* S,
+               double* x0) {
+  if (!h) return set_err(HF_EARG, "null context");
+  Ctx& c = h->c;
+  if (!c.state_set) return set_err(HF_ESTATE, "hf_set_state must be called first");
+  // scratch: the FP64 CG vectors are free outside a step
+  CU(launch_step_begin(c, itime, 0));
+  CU(launch_rhs_parts(c, c.A.y, c.A.r, c.A.p, c.A.q));
+  int rc = sync_scal(c);
+  if (rc) return rc;
+  if (B && (rc = download_padded(c, B, (const double*)c.A.y))) return rc;
+  if (Q && (rc = download_padded(c, Q, (const double*)c.A.r))) return rc;
+  if (Qd && (rc = download_padded(c, Qd, (const double*)c.A.p))) return rc;
+  if (sc && (rc = download_padded(c, sc, (const double*)c.A.q))) return rc;
+  if (S && (rc = download_padded(c, S, (const double*)c.A.b))) return rc;
+  int64_t pos = 0;
+  for (int64_t i = 0; i < c.ninst; ++i) {
+    const InstDesc& d = c.h_inst[i];
+    const InstScal& s = c.h_scal[i];
+    if (x0) CU(cudaMemcpyAsync(x0 + pos, c.A.tbuf[s.role[2]] + d.off, 8 * d.n, cudaMemcpyDeviceToHost, c.stream));
+    pos += d.n;
+  }
+  CU(cudaStreamSynchronize(c.stream));
+  if (x0) {
+    pos = 0;
+    for (int64_t i = 0; i < c.ninst; ++i) {
+      const InstDesc& d = c.h_inst[i];
+      if (c.h_scal[i].x0flag)
+        for (int64_t k = 0; k < d.n; ++k) x0[pos + k] = x0[pos + k] + kTiny;   // mod_evolve.f90:141
+      pos += d.n;
+    }
+  }
+  for (int64_t i = 0; i < c.ninst; ++i)
+    if (c.h_scal[i].status) return status_code(c.h_scal[i].status);
+  return HF_OK;
+}
+
+int hf_solve(hf_ctx* h, const double* b, double* x, hf_stats* stats) {
+  if (!h || !b || !x) return set_err(HF_EARG, "null argument");
+  Ctx& c = h->c;
+  if (c.ninst != 1) return set_err(HF_EARG, "hf_solve takes single-grid contexts");
+  int rc = sync_scal(c);
+  if (rc) return rc;
+  std::vector<InstScal> before(c.h_scal, c.h_scal + 1);
+  const InstDesc& d = c.h_inst[0];
+  InstScal& s = c.h_scal[0];
+  double bb = 0.0;
+  for (int64_t k = 0; k < d.n; ++k) bb += b[k] * b[k];
+  CU(cudaMemcpyAsync(c.A.b + d.off, b, 8 * d.n, cudaMemcpyHostToDevice, c.stream));
+  CU(cudaMemcpyAsync(c.A.tbuf[s.role[2]] + d.off, x, 8 * d.n, cudaMemcpyHostToDevice, c.stream));
+  s.bb = bb;
+  s.itime = 0;
+  s.outer_active = 1;
+  s.inner_active = 0;
+  s.refine = 0;
+  s.iter = 0;
+  s.step_iters = 0;
+  s.x0flag = 0;
+  s.status = 0;
+  double rms = std::sqrt(bb / (double)d.n) * d.mean_sinv * 1e-6;
+  s.sigma = (c.opts.precision == HF_PREC_MIXED && rms > 0.0 && std::isfinite(rms))
+                ? std::exp2(std::rint(std::log2(rms))) : 1.0;
+  if ((rc = push_scal(c))) return rc;
+  CU(launch_residual(c, 0));
+  if ((rc = solve_loop(c))) return rc;
+  if ((rc = sync_scal(c))) return rc;
+  CU(cudaMemcpyAsync(x, c.A.tbuf[c.h_scal[0].role[2]] + d.off, 8 * d.n, cudaMemcpyDeviceToHost, c.stream));
+  CU(cudaStreamSynchronize(c.stream));
+  fill_stats(c, stats, 0, before);
+  return first_error(c);
+}
+
+int hf_assemble_coo(hf_ctx* h, int64_t inst, int64_t cap, int64_t* irow, int64_t* jcol, double* val,
+                    int64_t* len, int64_t* count) {
+  if (!h) return set_err(HF_EARG, "null context");
+  Ctx& c = h->c;
+  if (inst < 0 || inst >= c.ninst) return set_err(HF_EARG, "instance out of range");
+  const InstDesc& d = c.h_inst[inst];
+  const int64_t nx = d.nx, ny = d.ny, nz = d.nz;
+  int64_t L = 7 * nx * ny * nz - 2 * (nx * ny + ny * nz + nz * nx);   // mod_setup.f90:96-99
+  if (d.px) L += 2 * ny * nz;
+  if (d.py) L += 2 * nz * nx;
+  if (d.pz) L += 2 * nx * ny;
+  if (len) *len = L;
+  if (!irow || !jcol || !val) return HF_OK;
+  if (cap < L) return set_err(HF_EARG, "capacity below the reference's COO length");
+  int64_t *d_counts = nullptr, *d_pos = nullptr, *d_irow = nullptr, *d_jcol = nullptr;
+  double* d_val = nullptr;
+  auto cleanup = [&]() { cudaFree(d_counts); cudaFree(d_pos); cudaFree(d_irow); cudaFree(d_jcol); cudaFree(d_val); };
+  if (cudaMalloc(&d_counts, 8 * d.n) != cudaSuccess || cudaMalloc(&d_pos, 8 * d.n) != cudaSuccess ||
+      cudaMalloc(&d_irow, 8 * std::max<int64_t>(L, 1)) != cudaSuccess ||
+      cudaMalloc(&d_jcol, 8 * std::max<int64_t>(L, 1)) != cudaSuccess ||
+      cudaMalloc(&d_val, 8 * std::max<int64_t>(L, 1)) != cudaSuccess) {
+    cleanup();
+    return set_err(HF_ENOMEM, "COO scratch allocation failed");
+  }
+  std::vector<int64_t> counts((size_t)d.n), pos((size_t)d.n);
+  cudaError_t e = launch_coo(c, inst, d_counts, nullptr, nullptr, nullptr, nullptr, 0);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(counts.data(), d_counts, 8 * d.n, cudaMemcpyDeviceToHost, c.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+  if (e != cudaSuccess) { cleanup(); return set_err(HF_ECUDA, cudaGetErrorString(e)); }
+  int64_t run = 0;
+  for (int64_t k = 0; k < d.n; ++k) { pos[k] = run; run += counts[k]; }
+  if (run > L) { cleanup(); return set_err(HF_EARG, "entries exceed the reference's COO capacity"); }
+  std::vector<int64_t> hi((size_t)L, -2), hj((size_t)L, -1);
+  std::vector<double> hv((size_t)L, 0.0);
+  e = cudaMemcpyAsync(d_pos, pos.data(), 8 * d.n, cudaMemcpyHostToDevice, c.stream);
+  if (e == cudaSuccess && L > 0) e = cudaMemcpyAsync(d_irow, hi.data(), 8 * L, cudaMemcpyHostToDevice, c.stream);
+  if (e == cudaSuccess && L > 0) e = cudaMemcpyAsync(d_jcol, hj.data(), 8 * L, cudaMemcpyHostToDevice, c.stream);
+  if (e == cudaSuccess && L > 0) e = cudaMemcpyAsync(d_val, hv.data(), 8 * L, cudaMemcpyHostToDevice, c.stream);
+  if (e == cudaSuccess) e = launch_coo(c, inst, nullptr, d_irow, d_jcol, d_val, d_pos, 1);
+  if (e == cudaSuccess && L > 0) e = cudaMemcpyAsync(irow, d_irow, 8 * L, cudaMemcpyDeviceToHost, c.stream);
+  if (e == cudaSuccess && L > 0) e = cudaMemcpyAsync(jcol, d_jcol, 8 * L, cudaMemcpyDeviceToHost, c.stream);
+  if (e == cudaSuccess && L > 0) e = cudaMemcpyAsync(val, d_val, 8 * L, cudaMemcpyDeviceToHost, c.stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c.stream);
+  cleanup();
+  if (e != cudaSuccess) return set_err(HF_ECUDA, cudaGetErrorString(e));
+  if (count) *count = run;
+  return HF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,42 @@
+// Host-side context of libheatflow_gb300 (one or more grids on one GPU).
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "hf_internal.cuh"
+
+namespace hf {
+
+// Assembly-only device inputs (kept for the parity probes, not read per step).
+struct AsmArrays {
+  double *kappa = nullptr, *tau_s = nullptr;
+  // per instance: boundary-condition block
+};
+
+struct InstBC {
+  double kb[6], tb[6], pd[6], br;
+  int32_t cg[6];
+};
+
+struct Ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int64_t ninst = 0, ncells = 0, ntiles = 0;
+  std::vector<InstDesc> h_inst;
+  std::vector<InstBC> h_bc;
+  std::vector<int64_t> h_tile0;
+  hf_solver_opts opts{};
+  DevArrays A{};
+  AsmArrays asm_{};
+  InstBC* d_bc = nullptr;
+  std::vector<void*> allocs;
+  InstScal* h_scal = nullptr;    // pinned mirror for polling
+  bool state_set = false;
+  bool any_heater = false, any_power = false, any_em = false, any_case5 = false;
+  // graph of one step (host loop replays it)
+  cudaGraphExec_t graph_exec = nullptr;
+};
+
+}  // namespace hf

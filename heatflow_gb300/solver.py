@@ -1,0 +1,193 @@
+"""Python host mirror of the reference's hot-path interface, over the C ABI.
+
+``HeatFlow`` owns one device context (one grid, or a batch of independent grids) and exposes
+the reference's routines under their reference names:
+
+==========================  ===========================================================
+reference                   here
+==========================  ===========================================================
+set_global_variables +      ``HeatFlow(problem)`` (mod_setup.f90:34-83, 89-152)
+sparse_Hmatrix
+initial_evolve              ``initial_evolve()`` / ``set_state`` (mod_init_evolve.f90:34-51)
+simulate(itime)             ``simulate(itime)`` (mod_evolve.f90:45-177)
+the time loop               ``run(itime0, nsteps)`` (heatflow.f90:67-90)
+linbcg                      ``linbcg(b, x)`` (mod_Sparse.f90:372-434)
+atimes / SRSax              ``atimes(x)`` (mod_Sparse.f90:436-450, 293-315)
+boundary / heater / S_catS  ``rhs(itime)`` (mod_boundary.f90:24, mod_heating.f90:27,
+                            mod_cattaneo.f90:23)
+sparse_Hmatrix COO          ``sparse_hmatrix()``
+==========================  ===========================================================
+
+Errors raise :class:`heatflow_gb300.abi.HeatFlowError` carrying the reference's message (the
+reference writes it and executes ``stop 1``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import Sequence, Union
+
+import numpy as np
+
+from . import abi
+from .problem import Problem
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int64)
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def make_opts(precision="fp64", criterion="recursive", tol=None, itmax=50000, inner_tol=1e-4,
+              inner_itmax=200, max_refine=20, check_every=2, use_graph=0) -> abi.HfSolverOpts:
+    lib = abi.load_library()
+    o = abi.HfSolverOpts()
+    lib.hf_default_opts(C.byref(o))
+    o.precision = {"fp64": abi.HF_PREC_FP64, "mixed": abi.HF_PREC_MIXED}[precision]
+    o.criterion = {"recursive": abi.HF_STOP_RECURSIVE, "true": abi.HF_STOP_TRUE}[criterion]
+    if tol is None:
+        tol = 1e-32 if criterion == "recursive" else 1e-10
+    o.tol = tol
+    o.itmax = itmax
+    o.inner_tol = inner_tol
+    o.inner_itmax = inner_itmax
+    o.max_refine = max_refine
+    o.check_every = check_every
+    o.use_graph = use_graph
+    return o
+
+
+class HeatFlow:
+    def __init__(self, problems: Union[Problem, Sequence[Problem]], **opts):
+        self.lib = abi.load_library()
+        self.problems = [problems] if isinstance(problems, Problem) else list(problems)
+        self.opts = make_opts(**opts)
+        arr = (abi.HfProblem * len(self.problems))(*[p.to_c() for p in self.problems])
+        self._arr = arr
+        h = C.c_void_p()
+        abi.check(self.lib.hf_create_batch(arr, len(self.problems), C.byref(self.opts), C.byref(h)),
+                  "hf_create")
+        self.h = h
+        self.sizes = [p.ncells for p in self.problems]
+        self.n = sum(self.sizes)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.hf_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # ---- options
+    def set_opts(self, **opts):
+        self.opts = make_opts(**opts)
+        abi.check(self.lib.hf_set_opts(self.h, C.byref(self.opts)), "hf_set_opts")
+
+    # ---- state
+    def set_state(self, tp, tpp):
+        tp = np.ascontiguousarray(tp, np.float64)
+        tpp = np.ascontiguousarray(tpp, np.float64)
+        assert tp.size == self.n and tpp.size == self.n
+        abi.check(self.lib.hf_set_state(self.h, _d(tp), _d(tpp)), "hf_set_state")
+
+    def initial_evolve(self):
+        """Temp_p = Temp_pp = T_System (mod_init_evolve.f90:47-48)."""
+        t = np.concatenate([np.full(p.ncells, p.t_system) for p in self.problems])
+        self.set_state(t, t)
+
+    def get_state(self):
+        tp = np.empty(self.n)
+        tpp = np.empty(self.n)
+        abi.check(self.lib.hf_get_state(self.h, _d(tp), _d(tpp)), "hf_get_state")
+        return tp, tpp
+
+    def split(self, a):
+        out, pos = [], 0
+        for s in self.sizes:
+            out.append(a[pos:pos + s])
+            pos += s
+        return out
+
+    # ---- stepping
+    def simulate(self, itime: int) -> dict:
+        st = abi.HfStats()
+        abi.check(self.lib.hf_step(self.h, int(itime), C.byref(st)), "simulate")
+        return st.as_dict()
+
+    def run(self, itime0: int, nsteps: int) -> dict:
+        st = abi.HfStats()
+        abi.check(self.lib.hf_run(self.h, int(itime0), int(nsteps), C.byref(st)), "run")
+        return st.as_dict()
+
+    # ---- parity probes
+    def operator(self):
+        out = [np.empty(self.n) for _ in range(4)]
+        abi.check(self.lib.hf_get_operator(self.h, *[_d(a) for a in out]), "hf_get_operator")
+        return dict(zip(("diag", "cx", "cy", "cz"), out))
+
+    def rhs(self, itime: int):
+        out = [np.empty(self.n) for _ in range(6)]
+        abi.check(self.lib.hf_get_rhs(self.h, int(itime), *[_d(a) for a in out]), "hf_get_rhs")
+        return dict(zip(("B", "Q", "Qdens", "S_cat", "S", "x0"), out))
+
+    def atimes(self, x):
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.empty(self.n)
+        abi.check(self.lib.hf_apply_operator(self.h, _d(x), _d(y)), "atimes")
+        return y
+
+    def linbcg(self, b, x):
+        b = np.ascontiguousarray(b, np.float64)
+        x = np.array(x, np.float64, copy=True)
+        st = abi.HfStats()
+        abi.check(self.lib.hf_solve(self.h, _d(b), _d(x), C.byref(st)), "linbcg")
+        return x, st.as_dict()
+
+    def sparse_hmatrix(self, instance: int = 0):
+        ln = C.c_int64()
+        abi.check(self.lib.hf_assemble_coo(self.h, instance, 0, None, None, None, C.byref(ln), None),
+                  "hf_assemble_coo")
+        cap = ln.value
+        irow = np.empty(cap, np.int64)
+        jcol = np.empty(cap, np.int64)
+        val = np.empty(cap, np.float64)
+        cnt = C.c_int64()
+        abi.check(self.lib.hf_assemble_coo(self.h, instance, cap, irow.ctypes.data_as(_ip),
+                                           jcol.ctypes.data_as(_ip), _d(val), C.byref(ln),
+                                           C.byref(cnt)), "hf_assemble_coo")
+        return irow, jcol, val, cnt.value
+
+
+def geometric_to_dense(problem: Problem, op: dict) -> np.ndarray:
+    """Expand the geometric SoA operator into a dense matrix (small grids; tests)."""
+    nx, ny, nz = problem.nx, problem.ny, problem.nz
+    N = problem.ncells
+    H = np.diag(op["diag"].copy())
+    per = problem.periodic
+    for I in range(N):
+        x, y, z = I % nx, (I // nx) % ny, I // (nx * ny)
+        for a, (c, n, stride, key) in enumerate(((x, nx, 1, "cx"), (y, ny, nx, "cy"),
+                                                 (z, nz, nx * ny, "cz"))):
+            v = op[key][I]
+            if v == 0.0 or n == 1:
+                continue
+            if c + 1 < n:
+                J = I + stride
+            elif per[a]:
+                J = I - (n - 1) * stride
+            else:
+                continue
+            H[I, J] += v
+            H[J, I] += v
+    return H

@@ -1,0 +1,183 @@
+/*
+ * heatflow_gb300 — C ABI of the GB300 (sm_103a) time-stepping hot path of HeatFlow.
+ *
+ * The reference (ExeQuantCode/HeatFlow, Fortran 2018) has no plugin API: its hot path is a
+ * set of module procedures sharing module-global state.  Each entry point below replaces one of
+ * them; the citation after each declaration is the reference interface it stands in for
+ * (paths relative to the reference project root).
+ *
+ * Conventions
+ *  - Cell index I = ix + nx*(iy + ny*iz), 0-based, x fastest.  This is the reference's
+ *    1-based lexicographic order (src/heatflow/mod_hmatrix.f90:71-74) minus one, i.e.
+ *    Fortran grid(ix,iy,iz) == C [iz][iy][ix].
+ *  - All arithmetic on the reference path is IEEE binary64; indices are int64
+ *    (src/heatflow/mod_constants.f90:8-9).
+ *  - Arrays passed in and out are caller-owned HOST buffers unless the name says _device.
+ *    Device state is owned by the context.  Calls on one context are serialised by the
+ *    caller; separate contexts are independent.
+ *  - Every call returns an int status (HF_OK or an HF_E* code).  The reference prints
+ *    "fatal error: NAN in ... vector" and executes `stop 1` (src/heatflow/mod_evolve.f90:70-73,
+ *    82-89, 102-105, 124-127, 153-158); the matching HF_ENAN_* codes let the host do the same.
+ *  - A context may hold several independent grids ("instances", hf_create_batch); state
+ *    arrays of a batch are the instances' arrays concatenated in instance order.
+ */
+#ifndef HEATFLOW_GB300_H
+#define HEATFLOW_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HF_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------------------------ */
+enum {
+  HF_OK = 0,
+  HF_EARG = 1,        /* invalid argument or a grid the reference cannot represent */
+  HF_ECUDA = 2,       /* CUDA runtime error (message via hf_last_error) */
+  HF_ENOMEM = 3,      /* device allocation failed */
+  HF_ESTATE = 4,      /* call order error (e.g. step before set_state) */
+  HF_EDEVICE = 5,     /* a device-side check failed (see hf_last_error) */
+  HF_ENAN_B = 10,     /* mod_evolve.f90:70-73   "fatal error: NAN in B vector" */
+  HF_ENAN_Q = 11,     /* mod_evolve.f90:82-85   "fatal error: NAN in Q vector" */
+  HF_ENAN_QDENS = 12, /* mod_evolve.f90:86-89   "fatal error: NAN in Qdens vector" */
+  HF_ENAN_SCAT = 13,  /* mod_evolve.f90:102-105 "fatal error: NAN in S_CAT vector" */
+  HF_ENAN_S = 14,     /* mod_evolve.f90:124-127 "fatal error: NAN in S vector" */
+  HF_ENAN_X = 15      /* mod_evolve.f90:153-158 "fatal error: NAN in x tempurature vector" */
+};
+
+/* ---- solver options ---------------------------------------------------------------------- */
+enum { HF_PREC_FP64 = 0, HF_PREC_MIXED = 1 };
+/* HF_STOP_RECURSIVE: the reference's linbcg itol=1 rule, err = ||r_k||/||b|| on the
+ * recursively updated residual, exit when err <= tol (mod_Sparse.f90:418-425).
+ * HF_STOP_TRUE: exit when the true residual ||b - H x||/||b|| <= tol (FP64). */
+enum { HF_STOP_RECURSIVE = 0, HF_STOP_TRUE = 1 };
+/* Heat density normalisation.  HF_QDENS_HEATED_VOLUME is the reference: every cell's Q is
+ * divided by the total volume of all heated cells (mod_heating.f90:164-167).
+ * HF_QDENS_CELL_VOLUME divides each cell by its own volume (per-cell source amplitudes). */
+enum { HF_QDENS_HEATED_VOLUME = 0, HF_QDENS_CELL_VOLUME = 1 };
+
+typedef struct hf_problem {
+  int64_t nx, ny, nz;            /* read_system, mod_inputs.f90:611 */
+  double lx, ly, lz;             /* box lengths; cell length = L/n, mod_inputs.f90:619-622 */
+  /* per-cell properties, length nx*ny*nz, x fastest (heatblock, mod_constructions.f90:25-31) */
+  const double* kappa;           /* W/m/K */
+  const double* rho;             /* kg/m^3 */
+  const double* heat_capacity;   /* J/kg/K */
+  const double* tau;             /* s, unscaled; the library applies tau/dt^2 (mod_setup.f90:62) */
+  const double* em;              /* emissivity; NULL means 0 everywhere */
+  const int64_t* iheater;        /* heater case per cell (mod_heating.f90:59-117); NULL = none */
+  const double* power;           /* optional per-cell POWER replacing power_in; NULL = power_in */
+  double power_in;               /* W (param.in power_in) */
+  double freq;                   /* Hz (param.in freq) */
+  double time_step;              /* s (param.in time_step) */
+  int64_t heated_steps;          /* param.in heattime (heater case 2) */
+  int32_t icattaneo;             /* 1: Cattaneo term on */
+  int32_t isteady;               /* 1: steady state (alpha = 0, S = -Qdens - B) */
+  int32_t periodic[3];           /* Periodicx/y/z */
+  int32_t cg_face[6];            /* Neumann "CG" faces: -x,+x,-y,+y,-z,+z (CG_x_m, CG_x_p, ...) */
+  double kappa_bound[6];         /* kappaBoundx1, Nx, y1, Ny, z1, Nz */
+  double t_bath_face[6];         /* T_Bathx1, x2, y1, y2, z1, z2 */
+  double t_bath;                 /* T_Bath (radiative loss reference temperature) */
+  double t_bath_cg;              /* T_BathCG */
+  double br;                     /* BR, boundary resistance factor */
+  int32_t qdens_mode;            /* HF_QDENS_* */
+  int32_t reserved;
+} hf_problem;
+
+typedef struct hf_solver_opts {
+  int32_t precision;    /* HF_PREC_FP64 or HF_PREC_MIXED */
+  int32_t criterion;    /* HF_STOP_RECURSIVE or HF_STOP_TRUE */
+  double tol;           /* relative residual target (reference: 1e-32 recursive) */
+  int64_t itmax;        /* max FP64 PCG iterations per step (reference: 50000) */
+  double inner_tol;     /* mixed: relative reduction asked of each FP32 inner solve */
+  int32_t inner_itmax;  /* mixed: max FP32 CG iterations per inner solve */
+  int32_t max_refine;   /* mixed: max FP64 refinement sweeps per step */
+  int32_t check_every;  /* iterations launched between host convergence polls */
+  int32_t use_graph;    /* 1: hf_run captures the step loop in one CUDA graph */
+} hf_solver_opts;
+
+typedef struct hf_stats {
+  int64_t steps;             /* steps completed */
+  int64_t iterations;        /* FP64 PCG iterations, summed over steps and instances */
+  int64_t inner_iterations;  /* FP32 CG iterations (mixed), summed */
+  int64_t refinements;       /* FP64 residual/refinement sweeps, summed */
+  int64_t last_iter;         /* iterations of the last step (reference `iter`), max over instances */
+  double last_err;           /* last step's exit criterion value, max over instances */
+  double last_true_relres;   /* ||b - H x||/||b|| of the last step in FP64, max over instances */
+  int64_t unconverged;       /* instance-steps that hit itmax / max_refine (the reference continues) */
+  int64_t failed_step;       /* itime of the step that raised an HF_ENAN_* code, else -1 */
+  int32_t status;
+  int32_t failed_instance;
+} hf_stats;
+
+typedef struct hf_ctx hf_ctx;
+
+/* ---- library ---------------------------------------------------------------------------- */
+int hf_abi_version(void);
+const char* hf_strerror(int code);
+/* Message of the last HF_ECUDA / HF_EDEVICE / HF_EARG raised on this thread. */
+const char* hf_last_error(void);
+/* Reference defaults: FP64, recursive criterion, tol 1e-32, itmax 50000
+ * (mod_evolve.f90:142-144). */
+void hf_default_opts(hf_solver_opts* opts);
+
+/* ---- set-up ----------------------------------------------------------------------------- */
+/* Replaces set_global_variables + sparse_Hmatrix (mod_setup.f90:34-83, 89-152): scales tau,
+ * forms rho*c, assembles the 7-point H operator on the device (hmatrixfunc,
+ * mod_hmatrix.f90:62-391) and the boundary vector (boundary, mod_boundary.f90:24-152). */
+int hf_create(const hf_problem* prob, const hf_solver_opts* opts, hf_ctx** out);
+/* Several independent grids of uneven sizes advanced together (one launch per kernel). */
+int hf_create_batch(const hf_problem* probs, int64_t count, const hf_solver_opts* opts,
+                    hf_ctx** out);
+int hf_destroy(hf_ctx* ctx);
+int hf_set_opts(hf_ctx* ctx, const hf_solver_opts* opts);
+/* Number of instances and total cells; cells of one instance. */
+int hf_get_sizes(const hf_ctx* ctx, int64_t* instances, int64_t* total_cells);
+int64_t hf_instance_cells(const hf_ctx* ctx, int64_t instance);
+/* Bind the context to a CUDA stream (cudaStream_t passed as void*; NULL = its own stream). */
+int hf_set_stream(hf_ctx* ctx, void* stream);
+
+/* ---- state (Temp_p = T^n, Temp_pp = T^(n-1); globe_data, mod_global.f90:10) ------------- */
+/* Replaces initial_evolve (mod_init_evolve.f90:34-51). */
+int hf_set_state(hf_ctx* ctx, const double* temp_p, const double* temp_pp);
+int hf_get_state(hf_ctx* ctx, double* temp_p, double* temp_pp);
+/* Device-resident state for zero-copy callers (torch): the context's own buffers. */
+int hf_state_device(hf_ctx* ctx, double** temp_p_device, double** temp_pp_device);
+/* Mark device state (written through hf_state_device) as set. */
+int hf_state_device_ready(hf_ctx* ctx);
+
+/* ---- time stepping ---------------------------------------------------------------------- */
+/* Replaces simulate(itime) (mod_evolve.f90:45-177): RHS, initial guess, linear solve, state
+ * rotation.  stats may be NULL. */
+int hf_step(hf_ctx* ctx, int64_t itime, hf_stats* stats);
+/* The time loop of heatflow.f90:67-90 without the I/O: steps itime0 .. itime0+nsteps-1. */
+int hf_run(hf_ctx* ctx, int64_t itime0, int64_t nsteps, hf_stats* stats);
+
+/* ---- parity probes (each replaces one reference routine) -------------------------------- */
+/* Geometric SoA operator: y_I = diag_I x_I + sum over axes of c_a[I] x[E_a(I)] +
+ * c_a[W_a(I)] x[W_a(I)], where E_a/W_a are the +/- neighbours with periodic wrap and
+ * c_a[I] is the face to the + neighbour (0 where the reference stores no entry). */
+int hf_get_operator(hf_ctx* ctx, double* diag, double* cx, double* cy, double* cz);
+/* RHS pieces for step itime from the current state: boundary(B) (mod_boundary.f90:24),
+ * heater(itime,Q,Qdens) (mod_heating.f90:27), S_catS (mod_cattaneo.f90:23), S and the
+ * initial guess x0 (mod_evolve.f90:112-141).  Any pointer may be NULL. */
+int hf_get_rhs(hf_ctx* ctx, int64_t itime, double* B, double* Q, double* Qdens, double* s_cat,
+               double* S, double* x0);
+/* y = H x with the device operator (atimes/SRSax, mod_Sparse.f90:293-315, 436-450). */
+int hf_apply_operator(hf_ctx* ctx, const double* x, double* y);
+/* Solve H x = b in place (x: initial guess in, solution out) with the context's options
+ * (linbcg, mod_Sparse.f90:372-434).  Single-instance contexts only. */
+int hf_solve(hf_ctx* ctx, const double* b, double* x, hf_stats* stats);
+/* COO assembly in the reference's storage order (sparse_Hmatrix, mod_setup.f90:89-152):
+ * capacity `len` slots, irow=-2/jcol=-1 in unused slots, 1-based indices.  cap must be
+ * >= the reference capacity returned in *len; *count receives the entries written. */
+int hf_assemble_coo(hf_ctx* ctx, int64_t instance, int64_t cap, int64_t* irow, int64_t* jcol,
+                    double* val, int64_t* len, int64_t* count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HEATFLOW_GB300_H */

@@ -1,0 +1,35 @@
+"""Generate the golden fixtures under tests/golden/ from the reference's own test data.
+
+Reads the reference's test/data/{param.in, mat.in, system.in, TempDis.dat} (a 25x25x1 Fourier
+run of 10 steps whose final Temp_p the reference wrote with final_print) and stores them in
+tempdis_25x25.json: the three input decks verbatim (they are the run's inputs) and the 625
+golden temperatures.  Run from the repository root:
+
+    python tests/golden/make_golden.py /root/reference
+"""
+import json
+import os
+import sys
+
+
+def main(ref_root: str):
+    data = os.path.join(ref_root, "test", "data")
+    rd = lambda n: open(os.path.join(data, n)).read()
+    vals = [float(t) for t in rd("TempDis.dat").split()]
+    out = {
+        "source": "reference test/data: param.in, mat.in, system.in, TempDis.dat",
+        "param_in": rd("param.in"),
+        "mat_in": rd("mat.in"),
+        "system_in": rd("system.in"),
+        "ntime": 10,
+        "tempdis": vals,
+        "print_precision": "ES16.8",
+    }
+    here = os.path.dirname(os.path.abspath(__file__))
+    with open(os.path.join(here, "tempdis_25x25.json"), "w") as f:
+        json.dump(out, f, indent=1)
+    print(f"wrote {len(vals)} golden values")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,244 @@
+"""Parity of the CUDA path (through the C ABI) with the oracle, on the GPU.
+
+Bit-exact: the assembled operator and COO (sparse_Hmatrix), the SpMV in SRSax order, the
+boundary vector, S_cat, S and x0 (no transcendental functions involved).  Within tolerance:
+heater terms that call sin/cos/pow (rtol 1e-14), and temperature fields after the solve
+(FP64 path: 1e-10 relative L2, the bar the reference's own output is held to; mixed path:
+1e-9 relative L2 at a true relative residual of 1e-10 per step).
+"""
+import numpy as np
+import pytest
+
+from heatflow_gb300 import abi, inputs
+from heatflow_gb300.problem import Problem, layered_slab, point_source_cube, random_instance
+from heatflow_gb300.solver import HeatFlow, geometric_to_dense
+from oracle.oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _rng_problem(nx, ny, nz, seed=1, **kw):
+    rng = np.random.default_rng(seed)
+    N = nx * ny * nz
+    base = dict(nx=nx, ny=ny, nz=nz, lx=nx * 1e-9, ly=ny * 1.3e-9, lz=nz * 0.8e-9,
+                kappa=rng.choice([149.0, 0.2, 50.0], size=N), rho=rng.uniform(1000, 3000, N),
+                heat_capacity=rng.uniform(500, 1500, N), tau=1e-12, em=0.0,
+                time_step=1e-13, icattaneo=1, kappa_bound=(149.0, 20.0, 149.0, 0.2, 60.0, 149.0),
+                t_bath_face=(300.0, 310.0, 295.0, 300.0, 305.0, 290.0), t_bath=300.0, br=0.7)
+    base.update(kw)
+    return Problem(**base)
+
+
+def _cases():
+    c = {}
+    c["cube6"] = point_source_cube(6)
+    c["layered"] = layered_slab(8, nz=10, layer=3)
+    c["br_mixed"] = _rng_problem(5, 4, 6)
+    c["periodic_xy"] = _rng_problem(5, 4, 3, periodic=(1, 1, 0))
+    c["periodic_all_n2"] = _rng_problem(2, 2, 2, periodic=(1, 1, 1))
+    c["periodic_z2"] = _rng_problem(3, 3, 2, periodic=(0, 0, 1))
+    c["flat"] = _rng_problem(7, 5, 1)
+    c["line"] = _rng_problem(6, 1, 1)
+    c["single"] = _rng_problem(1, 1, 1)
+    c["neumann"] = _rng_problem(4, 5, 3, cg_face=(1, 0, 0, 0, 0, 1), t_bath_cg=2.0)
+    c["steady"] = _rng_problem(3, 3, 3, isteady=1, iheater=np.r_[np.zeros(13), 1, np.zeros(13)].astype(np.int64),
+                               power_in=1e-6)
+    c["fourier"] = _rng_problem(4, 3, 5, icattaneo=0)
+    return c
+
+
+CASES = _cases()
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_operator_bit_exact(cuda_lib, name):
+    prob = CASES[name]
+    ref = Oracle(prob).dense()
+    with HeatFlow(prob) as hf:
+        H = geometric_to_dense(prob, hf.operator())
+    assert np.array_equal(H, ref), np.abs(H - ref).max()
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_coo_assembly_bit_exact(cuda_lib, name):
+    prob = CASES[name]
+    ri, rj, rv, rc = Oracle(prob).coo()
+    with HeatFlow(prob) as hf:
+        gi, gj, gv, gc = hf.sparse_hmatrix()
+    assert gc == rc
+    assert np.array_equal(gi, ri) and np.array_equal(gj, rj) and np.array_equal(gv, rv)
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_atimes_srsax_order(cuda_lib, name):
+    prob = CASES[name]
+    x = np.random.default_rng(3).uniform(250, 350, prob.ncells)
+    ref = Oracle(prob).atimes(x)
+    with HeatFlow(prob) as hf:
+        y = hf.atimes(x)
+    assert np.array_equal(y, ref), np.abs(y - ref).max()
+
+
+def _heater_problem(em=0.3):
+    n = 4
+    N = n ** 3
+    ih = np.arange(N, dtype=np.int64) % 9 - 1          # cases -1..7
+    return _rng_problem(n, n, n, iheater=ih, power_in=2e-6, freq=3.0e11, heated_steps=2,
+                        em=em, t_bath=280.0)
+
+
+@pytest.mark.parametrize("itime", [1, 2, 3, 7])
+@pytest.mark.parametrize("em", [0.0, 0.3])
+def test_rhs_pieces(cuda_lib, itime, em):
+    prob = _heater_problem(em)
+    rng = np.random.default_rng(itime)
+    tp = rng.uniform(290, 320, prob.ncells)
+    tpp = tp + rng.uniform(-1, 1, prob.ncells)
+    o = Oracle(prob)
+    o.set_state(tp, tpp)
+    rc, ref = o.rhs(itime)
+    assert rc == 0
+    with HeatFlow(prob) as hf:
+        hf.set_state(tp, tpp)
+        got = hf.rhs(itime)
+    assert np.array_equal(got["B"], ref["B"])
+    assert np.array_equal(got["S_cat"], ref["S_cat"])
+    assert np.array_equal(got["x0"], ref["x0"])
+    ih = prob.iheater
+    exact = np.isin(ih, [-1, 0, 1, 2, 6, 7]) if em == 0.0 else np.zeros(prob.ncells, bool)
+    for key in ("Q", "Qdens", "S"):
+        assert np.array_equal(got[key][exact], ref[key][exact]), key
+        np.testing.assert_allclose(got[key], ref[key], rtol=1e-14, atol=0, err_msg=key)
+
+
+def test_golden_tempdis_gpu(cuda_lib, golden):
+    """The reference's test deck, 10 steps, FP64 path with the reference's stopping rule."""
+    param, prob = inputs.read_all_files(golden["param_in"], golden["mat_in"], golden["system_in"])
+    with HeatFlow(prob, precision="fp64", criterion="recursive", tol=1e-32) as hf:
+        hf.initial_evolve()
+        st = hf.run(1, param["ntime"])
+        T, _ = hf.get_state()
+    gold = np.asarray(golden["tempdis"])
+    assert np.linalg.norm(T - gold) / np.linalg.norm(gold) < 1.1e-9
+    o = Oracle(prob)
+    o.set_state(*prob.initial_state())
+    o.run(param["ntime"])
+    Tref, _ = o.get_state()
+    assert np.linalg.norm(T - Tref) / np.linalg.norm(Tref) < 1e-12
+    assert st["steps"] == 10 and st["unconverged"] == 0
+
+
+def _oracle_run(prob, nsteps, mode=0, tol=1e-32):
+    o = Oracle(prob)
+    o.set_state(*prob.initial_state())
+    rc, iters = o.run(nsteps, mode=mode, tol=tol)
+    assert rc == 0
+    return o.get_state()[0], iters
+
+
+def test_config1_fp64_reference_rule(cuda_lib):
+    """20^3 Cattaneo point source, 100 steps: FP64 path with the reference's BiCG rule (tol
+    1e-32 on the recursive residual) against the oracle's BiCG, 1e-10 relative L2."""
+    prob = point_source_cube(20)
+    Tref, iters = _oracle_run(prob, 100)
+    with HeatFlow(prob, precision="fp64", criterion="recursive", tol=1e-32) as hf:
+        hf.initial_evolve()
+        st = hf.run(1, 100)
+        T, _ = hf.get_state()
+    assert np.linalg.norm(T - Tref) / np.linalg.norm(Tref) < 1e-10
+    assert st["unconverged"] == 0
+
+
+@pytest.mark.parametrize("precision,tol_err", [("fp64", 1e-10), ("mixed", 1e-9)])
+def test_config1_true_residual(cuda_lib, precision, tol_err):
+    prob = point_source_cube(20)
+    Tref, _ = _oracle_run(prob, 30)
+    with HeatFlow(prob, precision=precision, criterion="true", tol=1e-10) as hf:
+        hf.initial_evolve()
+        for k in range(1, 31):
+            st = hf.simulate(k)
+            assert st["last_true_relres"] <= 1e-10
+            assert st["unconverged"] == 0
+        T, _ = hf.get_state()
+    assert np.linalg.norm(T - Tref) / np.linalg.norm(Tref) < tol_err
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_layered_slab_vs_oracle(cuda_lib, precision):
+    prob = layered_slab(24, layer=4, sigma=3.0)
+    Tref, _ = _oracle_run(prob, 20, mode=1, tol=1e-13)
+    with HeatFlow(prob, precision=precision, criterion="true", tol=1e-10 if precision == "mixed" else 1e-13) as hf:
+        hf.initial_evolve()
+        st = hf.run(1, 20)
+        T, _ = hf.get_state()
+    err = np.linalg.norm(T - Tref) / np.linalg.norm(Tref)
+    assert err < (1e-9 if precision == "mixed" else 1e-12), err
+    assert st["last_true_relres"] <= (1e-10 if precision == "mixed" else 1e-13)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batch_equals_single(cuda_lib, precision):
+    rng = np.random.default_rng(5)
+    probs = [random_instance(rng, lo=5, hi=12) for _ in range(4)]
+    kw = dict(precision=precision, criterion="true", tol=1e-10)
+    with HeatFlow(probs, **kw) as hf:
+        hf.initial_evolve()
+        hf.run(1, 6)
+        Tb, _ = hf.get_state()
+    parts = []
+    for p in probs:
+        with HeatFlow(p, **kw) as hf:
+            hf.initial_evolve()
+            hf.run(1, 6)
+            parts.append(hf.get_state()[0])
+    assert np.array_equal(Tb, np.concatenate(parts))
+
+
+def test_nan_in_boundary_vector(cuda_lib):
+    prob = point_source_cube(4)
+    prob.kappa = prob.kappa.copy()
+    prob.kappa[0] = np.nan            # a corner cell: its boundary faces become NaN
+    with HeatFlow(prob) as hf:
+        hf.initial_evolve()
+        with pytest.raises(abi.HeatFlowError) as e:
+            hf.simulate(1)
+        assert e.value.code == abi.HF_ENAN_B
+        assert "NAN in B vector" in str(e.value)
+
+
+@pytest.mark.parametrize("icattaneo,code", [(1, abi.HF_ENAN_SCAT), (0, abi.HF_ENAN_S)])
+def test_nan_in_state(cuda_lib, icattaneo, code):
+    prob = point_source_cube(4, icattaneo=icattaneo)
+    tp, tpp = prob.initial_state()
+    tp[5] = np.nan
+    with HeatFlow(prob) as hf:
+        hf.set_state(tp, tpp)
+        with pytest.raises(abi.HeatFlowError) as e:
+            hf.simulate(1)
+        assert e.value.code == code
+        after, _ = hf.get_state()
+    assert np.isnan(after[5])          # the state was not rotated (the reference stops)
+
+
+def test_reject_nx1_grid(cuda_lib):
+    with pytest.raises(abi.HeatFlowError) as e:
+        HeatFlow(_rng_problem(1, 3, 3))
+    assert e.value.code == abi.HF_EARG
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_full_size_residual_property(cuda_lib, precision):
+    """256^3 layered slab (the measured workload), one step: the solution satisfies
+    ||S - H T|| / ||S|| <= 1e-10, checked with the independent SRSax-order SpMV."""
+    prob = layered_slab(256)
+    with HeatFlow(prob, precision=precision, criterion="true", tol=1e-10) as hf:
+        hf.initial_evolve()
+        S = hf.rhs(1)["S"]
+        st = hf.simulate(1)
+        T, Tpp = hf.get_state()
+        HT = hf.atimes(T)
+    assert np.all(Tpp == 300.0)
+    rel = np.linalg.norm(S - HT) / np.linalg.norm(S)
+    assert rel <= 1e-10, rel
+    assert st["last_true_relres"] <= 1e-10
+    assert np.isfinite(T).all() and T.max() > 300.0
