@@ -66,6 +66,7 @@ class HfStats(C.Structure):
         ("refinements", C.c_int64), ("last_iter", C.c_int64), ("last_err", C.c_double),
         ("last_true_relres", C.c_double), ("unconverged", C.c_int64),
         ("failed_step", C.c_int64), ("status", C.c_int32), ("failed_instance", C.c_int32),
+        ("kernel_launches", C.c_int64),
     ]
 
     def as_dict(self):
@@ -105,7 +106,9 @@ _SIGNATURES = {
     "hf_apply_operator": (C.c_int, [C.c_void_p, _dp, _dp]),
     "hf_solve": (C.c_int, [C.c_void_p, _dp, _dp, C.POINTER(HfStats)]),
     "hf_assemble_coo": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, _ip, _ip, _dp, _ip, _ip]),
+    "hf_time_kernel": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp]),
 }
+HF_KERNEL_RHS, HF_KERNEL_RESIDUAL, HF_KERNEL_CG_P, HF_KERNEL_CG_SPMV, HF_KERNEL_CG_UPDATE = 0, 1, 2, 3, 4
 
 _lib = None
 

@@ -165,8 +165,10 @@ int solve_loop(Ctx& c) {
     if (!any_outer) return HF_OK;
     if (any_inner) {
       for (int k = 0; k < c.opts.check_every; ++k) CU(launch_inner_iteration(c, fp32 ? 1 : 0));
+      c.launches += 3 * c.opts.check_every;
     } else {
       CU(launch_residual(c, 1));
+      c.launches += 1;
     }
   }
   return set_err(HF_EDEVICE, "solve loop did not terminate within its bound");
@@ -176,9 +178,11 @@ int run_one_step(Ctx& c, int64_t itime) {
   CU(launch_step_begin(c, itime, 0));
   CU(launch_rhs(c));
   CU(launch_residual(c, 0));
+  c.launches += 3;
   int rc = solve_loop(c);
   if (rc) return rc;
   CU(launch_step_end(c));
+  c.launches += 1;
   return HF_OK;
 }
 
@@ -586,6 +590,7 @@ int hf_run(hf_ctx* h, int64_t itime0, int64_t nsteps, hf_stats* stats) {
   int rc = sync_scal(c);
   if (rc) return rc;
   std::vector<InstScal> before(c.h_scal, c.h_scal + c.ninst);
+  const int64_t launches0 = c.launches;
   int64_t done = 0;
   for (int64_t k = 0; k < nsteps; ++k) {
     rc = run_one_step(c, itime0 + k);
@@ -598,7 +603,50 @@ int hf_run(hf_ctx* h, int64_t itime0, int64_t nsteps, hf_stats* stats) {
   rc = sync_scal(c);
   if (rc) return rc;
   fill_stats(c, stats, done, before);
+  if (stats) stats->kernel_launches = c.launches - launches0;
   return first_error(c);
+}
+
+int hf_time_kernel(hf_ctx* h, int which, int reps, double* ms) {
+  if (!h || !ms || reps < 1 || which < HF_KERNEL_RHS || which > HF_KERNEL_CG_UPDATE)
+    return set_err(HF_EARG, "bad arguments");
+  Ctx& c = h->c;
+  if (!c.state_set) return set_err(HF_ESTATE, "hf_set_state must be called first");
+  int rc = sync_scal(c);
+  if (rc) return rc;
+  std::vector<InstScal> saved(c.h_scal, c.h_scal + c.ninst);
+  std::vector<InstScal> phase = saved;
+  for (auto& s : phase) {
+    s.outer_active = 1;
+    s.inner_active = (which >= HF_KERNEL_CG_P) ? 1 : 0;
+    s.refine = 1;
+    s.iter = (which == HF_KERNEL_CG_P || which == HF_KERNEL_CG_UPDATE) ? 1 : (which == HF_KERNEL_RESIDUAL ? 1 : 0);
+    s.status = 0;
+    s.rho = 1.0; s.gg0 = 1.0; s.beta = 0.5; s.alpha = 0.5; s.eta = 0.0;
+    s.sigma = 1.0; s.sigma_prev = 1.0;
+    if (s.bb <= 0.0) s.bb = 1.0;
+  }
+  cudaEvent_t e0, e1;
+  CU(cudaEventCreate(&e0));
+  CU(cudaEventCreate(&e1));
+  double total = 0.0;
+  for (int r = 0; r < reps; ++r) {
+    std::memcpy(c.h_scal, phase.data(), sizeof(InstScal) * c.ninst);
+    CU(cudaMemcpyAsync(c.A.scal, c.h_scal, sizeof(InstScal) * c.ninst, cudaMemcpyHostToDevice, c.stream));
+    CU(cudaEventRecord(e0, c.stream));
+    CU(launch_single(c, which));
+    CU(cudaEventRecord(e1, c.stream));
+    CU(cudaEventSynchronize(e1));
+    float t = 0.f;
+    CU(cudaEventElapsedTime(&t, e0, e1));
+    total += t;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  std::memcpy(c.h_scal, saved.data(), sizeof(InstScal) * c.ninst);
+  if ((rc = push_scal(c))) return rc;
+  *ms = total / reps;
+  return HF_OK;
 }
 
 int hf_get_operator(hf_ctx* h, double* diag, double* cx, double* cy, double* cz) {

@@ -37,6 +37,7 @@ struct Ctx {
   bool any_heater = false, any_power = false, any_em = false, any_case5 = false;
   // graph of one step (host loop replays it)
   cudaGraphExec_t graph_exec = nullptr;
+  int64_t launches = 0;          // kernels launched on the device since creation
 };
 
 }  // namespace hf

@@ -210,6 +210,6 @@ cudaError_t launch_residual(Ctx& c, int mode);
 cudaError_t launch_inner_iteration(Ctx& c, int fp32);
 cudaError_t launch_step_end(Ctx& c);
 cudaError_t launch_apply(Ctx& c, const double* x, double* y);
-cudaError_t launch_final_x(Ctx& c, double* xout);
+cudaError_t launch_single(Ctx& c, int which);
 
 }  // namespace hf

@@ -360,4 +360,28 @@ cudaError_t launch_inner_iteration(Ctx& c, int fp32) {
   return cudaGetLastError();
 }
 
+// One kernel of the step, for timing (hf_time_kernel).
+cudaError_t launch_single(Ctx& c, int which) {
+  const unsigned nb = (unsigned)c.ntiles;
+  const bool fp32 = c.opts.precision == HF_PREC_MIXED;
+  switch (which) {
+    case HF_KERNEL_RHS: return launch_rhs(c);
+    case HF_KERNEL_RESIDUAL: return launch_residual(c, RES_UPDATE);
+    case HF_KERNEL_CG_P:
+      if (fp32) k_cg_p<float><<<nb, kBlock, 0, c.stream>>>(c.A);
+      else k_cg_p<double><<<nb, kBlock, 0, c.stream>>>(c.A);
+      break;
+    case HF_KERNEL_CG_SPMV:
+      if (fp32) k_cg_spmv<float><<<nb, kBlock, 0, c.stream>>>(c.A);
+      else k_cg_spmv<double><<<nb, kBlock, 0, c.stream>>>(c.A);
+      break;
+    case HF_KERNEL_CG_UPDATE:
+      if (fp32) k_cg_upd<float><<<nb, kBlock, 0, c.stream>>>(c.A);
+      else k_cg_upd<double><<<nb, kBlock, 0, c.stream>>>(c.A);
+      break;
+    default: return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
 }  // namespace hf

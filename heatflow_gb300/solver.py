@@ -89,6 +89,17 @@ class HeatFlow:
     def __exit__(self, *a):
         self.close()
 
+    def set_stream(self, stream_handle: int):
+        """Run on an existing CUDA stream (cudaStream_t as an integer, e.g. torch's
+        ``stream.cuda_stream``); 0 returns to the context's own stream."""
+        abi.check(self.lib.hf_set_stream(self.h, C.c_void_p(stream_handle or None)), "hf_set_stream")
+
+    def time_kernel(self, kernel: int, reps: int = 20) -> float:
+        """Mean duration (ms) of one launch of a step kernel, CUDA-event timed."""
+        ms = C.c_double()
+        abi.check(self.lib.hf_time_kernel(self.h, int(kernel), int(reps), C.byref(ms)), "hf_time_kernel")
+        return ms.value
+
     # ---- options
     def set_opts(self, **opts):
         self.opts = make_opts(**opts)

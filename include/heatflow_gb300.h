@@ -111,6 +111,7 @@ typedef struct hf_stats {
   int64_t failed_step;       /* itime of the step that raised an HF_ENAN_* code, else -1 */
   int32_t status;
   int32_t failed_instance;
+  int64_t kernel_launches;   /* kernels this call launched on the device */
 } hf_stats;
 
 typedef struct hf_ctx hf_ctx;
@@ -176,6 +177,19 @@ int hf_solve(hf_ctx* ctx, const double* b, double* x, hf_stats* stats);
  * >= the reference capacity returned in *len; *count receives the entries written. */
 int hf_assemble_coo(hf_ctx* ctx, int64_t instance, int64_t cap, int64_t* irow, int64_t* jcol,
                     double* val, int64_t* len, int64_t* count);
+
+/* ---- measurement (no reference counterpart: the reference times with cpu_time only) ------- */
+enum {
+  HF_KERNEL_RHS = 0,         /* per-step right-hand side */
+  HF_KERNEL_RESIDUAL = 1,    /* FP64 solution update + true residual sweep */
+  HF_KERNEL_CG_P = 2,        /* inner CG direction update (FP32 in mixed mode, else FP64) */
+  HF_KERNEL_CG_SPMV = 3,     /* inner CG SpMV + p.Ap */
+  HF_KERNEL_CG_UPDATE = 4    /* inner CG solution/residual update + r.r */
+};
+/* Launch one kernel `reps` times on the current state, each bracketed by CUDA events on the
+ * context's stream, and return its mean duration in milliseconds.  Solver scalars are restored
+ * afterwards; the temperature state is not modified.  Call after at least one step. */
+int hf_time_kernel(hf_ctx* ctx, int kernel, int reps, double* ms_per_launch);
 
 #ifdef __cplusplus
 }
