@@ -1,0 +1,401 @@
+#!/usr/bin/env python
+"""Benchmark of the HeatFlow time-stepping hot path on GB300.
+
+Metric: time-steps/s (and cell-iterations/s) at 256^3 with the mixed FP32-CG + FP64-refinement
+path at a true relative residual ||S - H T||/||S|| <= 1e-10 per step, beside the plain FP64 GPU
+path at the same residual.  Workload: two-material layered slab (z-layers alternating every 16
+cells between silicon-like kappa 149 and polymer-like kappa 0.2), Cattaneo mode, Dirichlet 300 K
+on all faces, Gaussian heating over the top face, dx = 1 nm, dt = 1e-13 s; synthetic, seeded.
+
+One "step" is one implicit time step (RHS, initial guess, solve, state rotation) of the whole grid.
+`value` is timed with CUDA events on the library's stream with the state resident in HBM;
+`e2e` is the same metric through the C ABI with host buffers: every step uploads T^n, T^(n-1)
+from pinned host memory (hf_set_state), steps (hf_step) and reads both fields back (hf_get_state).
+
+    python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+
+With N > 1 (torchrun, one process per GPU) every rank advances its own replica of the grid
+(replicas only: the path has no data-path collective) and `value` sums the ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "time-steps/s at 256^3, mixed FP32-CG + FP64 refinement, rel-res 1e-10"
+UNIT = "time-steps/s"
+
+# Algorithmic bytes per cell of each kernel (what the kernel must read + write from HBM),
+# for the layered-slab workload (Cattaneo, per-cell heater power array present).
+BYTES_PER_CELL = {
+    # T^n, T^(n-1), rho*c, tau'*rho*c, B, heater power (8 B each) + heater case (1 B); writes S, x0
+    "rhs": 6 * 8 + 1 + 2 * 8,
+    # mixed: x, diag, cx, cy, cz, S (8 B) + 1/sqrt|H_II| (4 B) read; g (4 B) written
+    "residual_mixed": 6 * 8 + 4 + 4,
+    # FP64: the same with g written in FP64
+    "residual_fp64": 6 * 8 + 4 + 8,
+    "cg_p_fp32": 3 * 4, "cg_spmv_fp32": 5 * 4, "cg_update_fp32": 6 * 4,
+    # x read (8) + y (4) + sinv (4) read, x written (8)
+    "xupdate_mixed": 8 + 4 + 4 + 8,
+    # x, y, sinv read and x written (8 B each)
+    "xupdate_fp64": 4 * 8,
+    "cg_p_fp64": 3 * 8, "cg_spmv_fp64": 5 * 8, "cg_update_fp64": 6 * 8,
+}
+# FP64 floating-point operations per cell (an FMA counts 2) of the FP64-pipe kernels: the
+# residual does 7 FMA for S - Hx and 1 FMA for ||r||^2; the RHS 2 mul (rho c T/dt), 1 FMA + 1 mul
+# (S_cat), 1 add, 2 add + 1 sub (x0 and its test), 1 FMA (||S||^2).
+FP64_FLOPS_PER_CELL = {"residual_mixed": 16, "residual_fp64": 18, "rhs": 12}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--fourier", action="store_true", help="Fourier instead of Cattaneo")
+    ap.add_argument("--tol", type=float, default=1e-10)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--host-loop", action="store_true",
+                    help="drive the solve loop from the host instead of the captured graph")
+    ap.add_argument("--cpu-seconds", type=float, default=90.0,
+                    help="wall-clock bound of the reference arm's timed steps")
+    return ap.parse_args()
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peak():
+    path = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """Per-cell DRAM bytes of each kernel from the committed ncu summary, if present."""
+    path = os.path.join(HERE, "profiles", "dram_bytes_per_cell.txt")
+    out = {}
+    if os.path.exists(path):
+        for line in open(path):
+            parts = line.split()
+            if len(parts) == 2 and not line.startswith("#"):
+                try:
+                    out[parts[0]] = float(parts[1])
+                except ValueError:
+                    pass
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.gpu)], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sms, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sms.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        os.unlink(self.path)
+        return {"sm_mhz": float(np.median(sms)) if sms else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sms)}
+
+
+def cpu_baseline(prob, steps_cap: int, seconds: float, tol: float):
+    """The oracle port of the reference's step (COO H, Jacobi BiCG with the reference's itol=1
+    criterion at `tol`, OpenMP-atomic SpMV as in the reference's Parallel build) on all host
+    cores.  Times whole steps until `steps_cap` steps or `seconds` elapse."""
+    from oracle.oracle import Oracle, set_threads
+    cores = os.cpu_count() or 1
+    set_threads(cores)
+    o = Oracle(prob)
+    o.set_state(*prob.initial_state())
+    times, iters = [], []
+    t_all = time.perf_counter()
+    k = 0
+    while k < steps_cap:
+        t0 = time.perf_counter()
+        rc, it, _ = o.simulate(k + 1, mode=0, tol=tol, itmax=50000)
+        times.append(time.perf_counter() - t0)
+        iters.append(it)
+        k += 1
+        if rc != 0 or time.perf_counter() - t_all > seconds:
+            break
+    ms = 1000.0 * float(np.mean(times))
+    return {"value": 1000.0 / ms, "unit": UNIT, "cores": cores, "kind": "port",
+            "ms_per_step": ms, "steps_timed": len(times), "bicg_iters_per_step": iters,
+            "sample": f"{len(times)} full step(s) of the same {prob.nx}^3 workload: COO H, "
+                      f"Jacobi BiCG at itol=1 tol={tol:g}, OpenMP atomic SpMV, {cores} threads"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return 0
+    from heatflow_gb300.problem import layered_slab
+    prob = layered_slab(args.n, icattaneo=0 if args.fourier else 1)
+    warm = 0 if args.warmup < 1 else 1
+    cb = cpu_baseline(prob, args.steps + warm, args.cpu_seconds, args.tol)
+    line = {
+        "metric": METRIC, "value": cb["value"], "unit": UNIT, "impl": "reference",
+        "n_gpus": world, "steps": cb["steps_timed"], "warmup": 0,
+        "ms_per_step": cb["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": workload_config(args, prob),
+        "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "notes": "reference Fortran not buildable on either machine (no Fortran compiler); "
+                 "the oracle port restates it statement by statement",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def workload_config(args, prob):
+    return {
+        "workload": f"layered slab {prob.nx}x{prob.ny}x{prob.nz}, "
+                    f"{'Fourier' if args.fourier else 'Cattaneo'}, top-face Gaussian heating",
+        "cells": prob.ncells, "dx_m": 1e-9, "dt_s": 1e-13, "rel_res": args.tol,
+        "layers": "z-alternating every 16 cells, kappa 149 / 0.2",
+        "l2": "inputs larger than L2: ~3.7 GB resident per grid, no flush needed",
+        "parallelism": f"replicas x{args.gpus}",
+        "step_loop": "host-polled" if args.host_loop else "CUDA graph per step (conditional WHILE/SWITCH)",
+    }
+
+
+def timed_run(hf, torch, stream, itime0, steps):
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    st = hf.run(itime0, steps)
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1), st
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_info()
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import torch
+    from heatflow_gb300 import abi
+    from heatflow_gb300.build import build_library
+    from heatflow_gb300.problem import layered_slab
+    from heatflow_gb300.solver import HeatFlow
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    build_library()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(v):
+        if dist is None:
+            return v
+        t = torch.tensor([v], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    prob = layered_slab(args.n, icattaneo=0 if args.fourier else 1)
+    N = prob.ncells
+    graph = 0 if args.host_loop else 1
+    stream = torch.cuda.Stream()
+    W, K = max(args.warmup, 0), max(args.steps, 1)
+
+    # ---- headline: mixed path, state resident in HBM
+    hf = HeatFlow(prob, precision="mixed", criterion="true", tol=args.tol, use_graph=graph)
+    hf.set_stream(stream.cuda_stream)
+    hf.initial_evolve()
+    if W:
+        hf.run(1, W)
+    barrier()
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        ms, st = timed_run(hf, torch, stream, W + 1, K)
+    ms = max_over_ranks(ms)
+    clocks = clk.summary()
+    steps_per_s = world * K / (ms / 1000.0)
+    cell_iters = N * (st["inner_iterations"] + st["iterations"] + st["refinements"])
+    cell_iters_per_s = world * cell_iters / (ms / 1000.0)
+
+    # ---- kernel roofline: each kernel timed alone with CUDA events on the library's stream
+    kernels = {"rhs": abi.HF_KERNEL_RHS, "residual_mixed": abi.HF_KERNEL_RESIDUAL,
+               "xupdate_mixed": abi.HF_KERNEL_XUPDATE,
+               "cg_p_fp32": abi.HF_KERNEL_CG_P, "cg_spmv_fp32": abi.HF_KERNEL_CG_SPMV,
+               "cg_update_fp32": abi.HF_KERNEL_CG_UPDATE}
+    kms = {name: hf.time_kernel(k, reps=20) for name, k in kernels.items()}
+    per_step_launches = {
+        "rhs": 1.0, "residual_mixed": st["refinements"] / K,
+        "xupdate_mixed": max(st["refinements"] / K - 1.0, 0.0),
+        "cg_p_fp32": st["inner_iterations"] / K, "cg_spmv_fp32": st["inner_iterations"] / K,
+        "cg_update_fp32": st["inner_iterations"] / K,
+    }
+    share = {k: kms[k] * per_step_launches[k] for k in kms}
+    dominant = max(share, key=share.get)
+    peak, peak_kind = measured_peak()
+    f64 = C.c_double()
+    f32 = C.c_double()
+    rc = abi.load_library().hf_measure_fp_rates(C.byref(f64), C.byref(f32))
+    fp_rates = {"fp64_tflops": f64.value, "fp32_tflops": f32.value} if rc == 0 else None
+    bpc = BYTES_PER_CELL[dominant]
+    achieved = bpc * N / (kms[dominant] / 1000.0) / 1e9
+    traffic = ncu_traffic().get(dominant)
+    roofline = {"kernel": dominant, "bound": "hbm", "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak, "peak_kind": f"of {peak_kind}",
+                "traffic": traffic * N if traffic else None,
+                "algorithmic_bytes_per_launch": bpc * N,
+                "kernels": {k: {"ms": kms[k], "GB/s": BYTES_PER_CELL[k] * N / (kms[k] / 1000.0) / 1e9,
+                                "frac": BYTES_PER_CELL[k] * N / (kms[k] / 1000.0) / 1e9 / peak,
+                                "launches_per_step": per_step_launches[k]} for k in kms}}
+    if fp_rates:
+        roofline["fp64"] = {
+            k: {"achieved_tflops": FP64_FLOPS_PER_CELL[k] * N / (kms[k] / 1000.0) / 1e12,
+                "peak_tflops": fp_rates["fp64_tflops"],
+                "frac": FP64_FLOPS_PER_CELL[k] * N / (kms[k] / 1000.0) / 1e12 / fp_rates["fp64_tflops"]}
+            for k in kms if k in FP64_FLOPS_PER_CELL}
+    hf.close()
+
+    # ---- plain FP64 GPU path at the same residual
+    fp64 = None
+    if not args.no_fp64:
+        h2 = HeatFlow(prob, precision="fp64", criterion="true", tol=args.tol, use_graph=graph)
+        h2.set_stream(stream.cuda_stream)
+        h2.initial_evolve()
+        if W:
+            h2.run(1, W)
+        barrier()
+        ms64, st64 = timed_run(h2, torch, stream, W + 1, K)
+        ms64 = max_over_ranks(ms64)
+        k64 = {"residual_fp64": h2.time_kernel(abi.HF_KERNEL_RESIDUAL, 10),
+               "xupdate_fp64": h2.time_kernel(abi.HF_KERNEL_XUPDATE, 10),
+               "cg_spmv_fp64": h2.time_kernel(abi.HF_KERNEL_CG_SPMV, 10),
+               "cg_update_fp64": h2.time_kernel(abi.HF_KERNEL_CG_UPDATE, 10),
+               "cg_p_fp64": h2.time_kernel(abi.HF_KERNEL_CG_P, 10)}
+        fp64 = {"steps_per_s": world * K / (ms64 / 1000.0), "ms_per_step": ms64 / K,
+                "iterations_per_step": st64["iterations"] / K,
+                "refinements_per_step": st64["refinements"] / K,
+                "last_true_relres": st64["last_true_relres"],
+                "kernels": {k: {"ms": v, "GB/s": BYTES_PER_CELL[k] * N / (v / 1000.0) / 1e9}
+                            for k, v in k64.items()}}
+        h2.close()
+
+    # ---- end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        h3 = HeatFlow(prob, precision="mixed", criterion="true", tol=args.tol, use_graph=graph)
+        h3.set_stream(stream.cuda_stream)
+        tp = torch.full((N,), prob.t_system, dtype=torch.float64).pin_memory().numpy()
+        tpp = torch.full((N,), prob.t_system, dtype=torch.float64).pin_memory().numpy()
+        for k in range(W):
+            h3.set_state(tp, tpp)
+            h3.simulate(k + 1)
+            tp[:], tpp[:] = h3.get_state()
+        barrier()
+        t0 = time.perf_counter()
+        for k in range(K):
+            h3.set_state(tp, tpp)
+            h3.simulate(W + 1 + k)
+            a, b = h3.get_state()
+            tp[:] = a
+            tpp[:] = b
+        torch.cuda.synchronize()
+        e2e_s = max_over_ranks(time.perf_counter() - t0)
+        e2e = {"value": world * K / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * N,
+               "d2h_bytes_per_step": 2 * 8 * N, "timing": "wall clock, host-synchronous C ABI calls"}
+        h3.close()
+
+    cb = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cb = cpu_baseline(prob, 2, 60.0, args.tol)
+        cb = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": steps_per_s, "unit": UNIT, "n_gpus": world, "steps": K,
+            "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": workload_config(args, prob),
+            "cell_iters_per_s": cell_iters_per_s,
+            "iterations_per_step": {"fp32_cg": st["inner_iterations"] / K,
+                                    "fp64_refinement_sweeps": st["refinements"] / K},
+            "last_true_relres": st["last_true_relres"],
+            "fp64_gpu": fp64,
+            "mixed_over_fp64": (steps_per_s / fp64["steps_per_s"]) if fp64 else None,
+            "roofline": roofline, "fp_rates_measured": fp_rates,
+            "cpu_baseline": cb, "clocks": clocks, "e2e": e2e,
+            "gpu_launches": st["kernel_launches"],
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

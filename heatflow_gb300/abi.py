@@ -107,8 +107,10 @@ _SIGNATURES = {
     "hf_solve": (C.c_int, [C.c_void_p, _dp, _dp, C.POINTER(HfStats)]),
     "hf_assemble_coo": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, _ip, _ip, _dp, _ip, _ip]),
     "hf_time_kernel": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp]),
+    "hf_measure_fp_rates": (C.c_int, [_dp, _dp]),
 }
 HF_KERNEL_RHS, HF_KERNEL_RESIDUAL, HF_KERNEL_CG_P, HF_KERNEL_CG_SPMV, HF_KERNEL_CG_UPDATE = 0, 1, 2, 3, 4
+HF_KERNEL_XUPDATE = 5
 
 _lib = None
 

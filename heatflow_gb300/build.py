@@ -24,6 +24,7 @@ UNITS = {
     "hf_rhs.cu": ["-fmad=false"],
     "hf_solve.cu": [],
     "hf_abi.cu": ["-fmad=false"],
+    "hf_probe.cu": [],
 }
 
 

@@ -94,8 +94,15 @@ int dalloc(Ctx& c, T** p, size_t count) {
   return HF_OK;
 }
 
-void free_all(Ctx& c) {
+void drop_graph(Ctx& c) {
   if (c.graph_exec) cudaGraphExecDestroy(c.graph_exec);
+  if (c.graph) cudaGraphDestroy(c.graph);
+  c.graph_exec = nullptr;
+  c.graph = nullptr;
+}
+
+void free_all(Ctx& c) {
+  drop_graph(c);
   for (void* p : c.allocs) cudaFree(p);
   c.allocs.clear();
   if (c.h_scal) cudaFreeHost(c.h_scal);
@@ -146,7 +153,19 @@ int push_scal(Ctx& c) {
 int status_code(int bits) {
   for (int k = 0; k <= HF_ENAN_X - HF_ENAN_B; ++k)
     if (bits & (1 << k)) return HF_ENAN_B + k;
+  if (bits & kStatusRhsNan) return HF_ENAN_S;
   return HF_OK;
+}
+
+// A NaN in S was detected through ||S||^2: find which vector failed first, in the reference's
+// check order (mod_evolve.f90:82-127), by re-running the failed step's RHS with per-vector tests.
+int diagnose(Ctx& c) {
+  bool any = false;
+  for (int64_t i = 0; i < c.ninst; ++i) any |= (c.h_scal[i].status & kStatusRhsNan) != 0;
+  if (!any) return HF_OK;
+  CU(launch_rhs_diagnose(c));
+  CU(launch_finalize(c, FIN_RHS_DIAG, nullptr, 0, 0));
+  return sync_scal(c);
 }
 
 // Drive one step's solve after the RHS / initial residual kernels are queued.
@@ -165,10 +184,10 @@ int solve_loop(Ctx& c) {
     if (!any_outer) return HF_OK;
     if (any_inner) {
       for (int k = 0; k < c.opts.check_every; ++k) CU(launch_inner_iteration(c, fp32 ? 1 : 0));
-      c.launches += 3 * c.opts.check_every;
+      c.launches += 5 * c.opts.check_every;
     } else {
       CU(launch_residual(c, 1));
-      c.launches += 1;
+      c.launches += 3;
     }
   }
   return set_err(HF_EDEVICE, "solve loop did not terminate within its bound");
@@ -177,12 +196,112 @@ int solve_loop(Ctx& c) {
 int run_one_step(Ctx& c, int64_t itime) {
   CU(launch_step_begin(c, itime, 0));
   CU(launch_rhs(c));
+  CU(launch_finalize(c, FIN_RHS, nullptr, 0, 0));
   CU(launch_residual(c, 0));
-  c.launches += 3;
+  c.launches += 5;
   int rc = solve_loop(c);
   if (rc) return rc;
   CU(launch_step_end(c));
   c.launches += 1;
+  return HF_OK;
+}
+
+// Capture one step as a CUDA graph: the solve loop is a WHILE node whose body selects, through a
+// SWITCH node, one inner CG iteration or one residual sweep; control kernels set the conditions
+// from the per-instance phase flags, so a step runs without any host round trip.
+int build_graph(Ctx& c) {
+  if (c.graph_exec && c.graph_precision == c.opts.precision && c.graph_criterion == c.opts.criterion)
+    return HF_OK;
+  drop_graph(c);
+  if (!c.d_ctrl) {
+    int r = dalloc(c, &c.d_ctrl, 1);
+    if (r) return r;
+    CU(cudaMemset(c.d_ctrl, 0, sizeof(CtrlState)));
+  }
+  const bool fp32 = c.opts.precision == HF_PREC_MIXED;
+  cudaStream_t cs = nullptr, cs2 = nullptr;
+  CU(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  CU(cudaStreamCreateWithFlags(&cs2, cudaStreamNonBlocking));
+  cudaStream_t saved = c.stream;
+  cudaGraph_t g = nullptr;
+  std::string err;
+  auto chk = [&](cudaError_t e, const char* what) {
+    if (e != cudaSuccess && err.empty()) err = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaSuccess;
+  };
+  do {
+    if (!chk(cudaGraphCreate(&g, 0), "cudaGraphCreate")) break;
+    cudaGraphConditionalHandle hw;
+    if (!chk(cudaGraphConditionalHandleCreate(&hw, g, 0, cudaGraphCondAssignDefault), "handle(while)")) break;
+    if (!chk(cudaStreamBeginCaptureToGraph(cs, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed), "capture")) break;
+    c.stream = cs;
+    chk(launch_graph_step_begin(c, c.d_ctrl), "step begin");
+    chk(launch_rhs(c), "rhs");
+    chk(launch_finalize(c, FIN_RHS, c.d_ctrl, hw, 1), "rhs finalize");
+    chk(launch_residual(c, 0, c.d_ctrl, hw, 1), "residual init");
+    cudaStreamCaptureStatus st;
+    cudaGraph_t cg = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    chk(cudaStreamGetCaptureInfo(cs, &st, nullptr, &cg, &deps, nullptr, &nd), "capture info");
+    cudaGraphNodeParams wp = {};
+    wp.type = cudaGraphNodeTypeConditional;
+    wp.conditional.handle = hw;
+    wp.conditional.type = cudaGraphCondTypeWhile;
+    wp.conditional.size = 1;
+    cudaGraphNode_t wnode = nullptr;
+    if (!chk(cudaGraphAddNode(&wnode, cg, deps, nullptr, nd, &wp), "while node")) { cudaStreamEndCapture(cs, &g); break; }
+    cudaGraph_t body = wp.conditional.phGraph_out[0];
+    chk(cudaStreamUpdateCaptureDependencies(cs, &wnode, nullptr, 1, cudaStreamSetCaptureDependencies), "deps");
+    // loop body: select, switch, condition
+    cudaGraphConditionalHandle hs;
+    chk(cudaGraphConditionalHandleCreate(&hs, body, 2, cudaGraphCondAssignDefault), "handle(switch)");
+    chk(cudaStreamBeginCaptureToGraph(cs2, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed), "capture body");
+    c.stream = cs2;
+    chk(launch_ctrl_select(c, c.d_ctrl, hs, hw), "select");
+    cudaGraph_t cg2 = nullptr;
+    const cudaGraphNode_t* deps2 = nullptr;
+    size_t nd2 = 0;
+    chk(cudaStreamGetCaptureInfo(cs2, &st, nullptr, &cg2, &deps2, nullptr, &nd2), "capture info body");
+    cudaGraphNodeParams sp = {};
+    sp.type = cudaGraphNodeTypeConditional;
+    sp.conditional.handle = hs;
+    sp.conditional.type = cudaGraphCondTypeSwitch;
+    sp.conditional.size = 2;
+    cudaGraphNode_t snode = nullptr;
+    chk(cudaGraphAddNode(&snode, cg2, deps2, nullptr, nd2, &sp), "switch node");
+    chk(cudaStreamUpdateCaptureDependencies(cs2, &snode, nullptr, 1, cudaStreamSetCaptureDependencies), "deps body");
+    cudaGraph_t tmp = nullptr;
+    chk(cudaStreamEndCapture(cs2, &tmp), "end body");
+    if (err.empty()) {
+      chk(cudaStreamBeginCaptureToGraph(cs2, sp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                        cudaStreamCaptureModeRelaxed), "capture cg");
+      chk(launch_inner_iteration(c, fp32 ? 1 : 0, c.d_ctrl, hw, 1), "cg iteration");
+      chk(cudaStreamEndCapture(cs2, &tmp), "end cg");
+      chk(cudaStreamBeginCaptureToGraph(cs2, sp.conditional.phGraph_out[1], nullptr, nullptr, 0,
+                                        cudaStreamCaptureModeRelaxed), "capture residual");
+      chk(launch_residual(c, 1, c.d_ctrl, hw, 1), "residual");
+      chk(cudaStreamEndCapture(cs2, &tmp), "end residual");
+    }
+    c.stream = cs;
+    chk(launch_graph_step_end(c, c.d_ctrl), "step end");
+    cudaGraph_t outg = nullptr;
+    chk(cudaStreamEndCapture(cs, &outg), "end capture");
+    if (err.empty()) chk(cudaGraphInstantiate(&c.graph_exec, g, 0), "instantiate");
+  } while (0);
+  c.stream = saved;
+  cudaStreamDestroy(cs);
+  cudaStreamDestroy(cs2);
+  if (!err.empty()) {
+    if (c.graph_exec) cudaGraphExecDestroy(c.graph_exec);
+    c.graph_exec = nullptr;
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return set_err(HF_ECUDA, "graph capture: " + err);
+  }
+  c.graph = g;
+  c.graph_precision = c.opts.precision;
+  c.graph_criterion = c.opts.criterion;
   return HF_OK;
 }
 
@@ -340,6 +459,11 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
   }
   c.ncells = off;
   c.ntiles = tiles;
+  {
+    int sms = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device);
+    c.grid_tiles = std::min<int64_t>(tiles, (int64_t)std::max(sms, 1) * 6);
+  }
   const size_t N = (size_t)c.ncells;
   // ---- device memory
   DevArrays& A = c.A;
@@ -351,11 +475,15 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
   ALLOC(d_inst, (size_t)count);
   ALLOC(d_scal, (size_t)count);
   ALLOC(d_tile_inst, (size_t)tiles);
+  int8_t* d_tile_heat;
+  ALLOC(d_tile_heat, (size_t)tiles);
+  A.tile_heat = d_tile_heat;
   ALLOC(A.partials, (size_t)tiles * kNR);
   ALLOC(A.counters, (size_t)count);
   ALLOC(c.d_bc, (size_t)count);
   A.inst = d_inst; A.scal = d_scal; A.tile_inst = d_tile_inst;
   ALLOC(A.diag, N); ALLOC(A.cx, N); ALLOC(A.cy, N); ALLOC(A.cz, N); ALLOC(A.sinv, N);
+  ALLOC(A.rsum, N); ALLOC(A.sinv32, N);
   ALLOC(A.a64x, N); ALLOC(A.a64y, N); ALLOC(A.a64z, N);
   ALLOC(A.a32x, N); ALLOC(A.a32y, N); ALLOC(A.a32z, N);
   ALLOC(A.rhoc, N); ALLOC(A.ccat, N); ALLOC(A.bvec, N); ALLOC(A.tau_s, N);
@@ -380,10 +508,10 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
   for (void* p : {(void*)A.diag, (void*)A.cx, (void*)A.cy, (void*)A.cz, (void*)c.asm_.kappa,
                   (void*)d_rho, (void*)d_hc, (void*)d_tau, (void*)A.rhoc, (void*)A.ccat,
                   (void*)A.bvec, (void*)A.tau_s, (void*)A.a64x, (void*)A.a64y, (void*)A.a64z,
-                  (void*)A.b, (void*)A.y, (void*)A.r, (void*)A.p, (void*)A.q})
+                  (void*)A.b, (void*)A.y, (void*)A.r, (void*)A.p, (void*)A.q, (void*)A.rsum})
     CK(cudaMemsetAsync(p, 0, N * sizeof(double), c.stream));
   for (void* p : {(void*)A.a32x, (void*)A.a32y, (void*)A.a32z, (void*)A.y32, (void*)A.r32,
-                  (void*)A.p32, (void*)A.q32})
+                  (void*)A.p32, (void*)A.q32, (void*)A.sinv32})
     CK(cudaMemsetAsync(p, 0, N * sizeof(float), c.stream));
   for (int k = 0; k < 4; ++k) CK(cudaMemsetAsync(A.tbuf[k], 0, N * sizeof(double), c.stream));
   if (d_em) CK(cudaMemsetAsync(d_em, 0, N * sizeof(double), c.stream));
@@ -392,6 +520,16 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
   CK(cudaMemcpyAsync(d_inst, c.h_inst.data(), sizeof(InstDesc) * count, cudaMemcpyHostToDevice, c.stream));
   CK(cudaMemcpyAsync(c.d_bc, c.h_bc.data(), sizeof(InstBC) * count, cudaMemcpyHostToDevice, c.stream));
   CK(cudaMemcpyAsync(d_tile_inst, tile_inst.data(), sizeof(int32_t) * tiles, cudaMemcpyHostToDevice, c.stream));
+  {   // tiles holding a heated cell (the RHS skips heater loads elsewhere)
+    std::vector<int8_t> th((size_t)tiles, 0);
+    for (int64_t i = 0; i < count; ++i) {
+      const InstDesc& d = c.h_inst[i];
+      if (!probs[i].iheater) continue;
+      for (int64_t k = 0; k < d.n; ++k)
+        if (probs[i].iheater[k] != 0) th[(size_t)(d.tile0 + k / kTile)] = 1;
+    }
+    CK(cudaMemcpy(d_tile_heat, th.data(), (size_t)tiles, cudaMemcpyHostToDevice));
+  }
   // per-cell inputs into the padded layout
   std::vector<int8_t> icase;
   for (int64_t i = 0; i < count; ++i) {
@@ -495,6 +633,7 @@ int hf_set_opts(hf_ctx* h, const hf_solver_opts* opts) {
   if (rc) return rc;
   h->c.opts = *opts;
   h->c.A.opts = dev_opts(*opts);
+  drop_graph(h->c);   // captured kernels hold the options by value
   return HF_OK;
 }
 
@@ -592,6 +731,22 @@ int hf_run(hf_ctx* h, int64_t itime0, int64_t nsteps, hf_stats* stats) {
   std::vector<InstScal> before(c.h_scal, c.h_scal + c.ninst);
   const int64_t launches0 = c.launches;
   int64_t done = 0;
+  if (c.opts.use_graph && nsteps > 0) {
+    if ((rc = build_graph(c))) return rc;
+    const bool fp32 = c.opts.precision == HF_PREC_MIXED;
+    const int64_t per = fp32 ? c.opts.inner_itmax : c.opts.itmax;
+    CtrlState cs{};
+    cs.itime = itime0;
+    cs.limit = 2 * (int64_t)(c.opts.max_refine + 3) * (per + 3);
+    CU(cudaMemcpyAsync(c.d_ctrl, &cs, sizeof(cs), cudaMemcpyHostToDevice, c.stream));
+    for (int64_t k = 0; k < nsteps; ++k) CU(cudaGraphLaunch(c.graph_exec, c.stream));
+    CU(cudaMemcpyAsync(&cs, c.d_ctrl, sizeof(cs), cudaMemcpyDeviceToHost, c.stream));
+    CU(cudaStreamSynchronize(c.stream));
+    if (cs.guard_hit) return set_err(HF_EDEVICE, "captured solve loop reached its iteration bound");
+    c.launches += cs.launches;
+    done = nsteps;
+    nsteps = 0;
+  }
   for (int64_t k = 0; k < nsteps; ++k) {
     rc = run_one_step(c, itime0 + k);
     if (rc) return rc;
@@ -602,13 +757,14 @@ int hf_run(hf_ctx* h, int64_t itime0, int64_t nsteps, hf_stats* stats) {
   }
   rc = sync_scal(c);
   if (rc) return rc;
+  if ((rc = diagnose(c))) return rc;
   fill_stats(c, stats, done, before);
   if (stats) stats->kernel_launches = c.launches - launches0;
   return first_error(c);
 }
 
 int hf_time_kernel(hf_ctx* h, int which, int reps, double* ms) {
-  if (!h || !ms || reps < 1 || which < HF_KERNEL_RHS || which > HF_KERNEL_CG_UPDATE)
+  if (!h || !ms || reps < 1 || which < HF_KERNEL_RHS || which > HF_KERNEL_XUPDATE)
     return set_err(HF_EARG, "bad arguments");
   Ctx& c = h->c;
   if (!c.state_set) return set_err(HF_ESTATE, "hf_set_state must be called first");
@@ -618,7 +774,7 @@ int hf_time_kernel(hf_ctx* h, int which, int reps, double* ms) {
   std::vector<InstScal> phase = saved;
   for (auto& s : phase) {
     s.outer_active = 1;
-    s.inner_active = (which >= HF_KERNEL_CG_P) ? 1 : 0;
+    s.inner_active = (which >= HF_KERNEL_CG_P && which <= HF_KERNEL_CG_UPDATE) ? 1 : 0;
     s.refine = 1;
     s.iter = (which == HF_KERNEL_CG_P || which == HF_KERNEL_CG_UPDATE) ? 1 : (which == HF_KERNEL_RESIDUAL ? 1 : 0);
     s.status = 0;
@@ -680,8 +836,10 @@ int hf_get_rhs(hf_ctx* h, int64_t itime, double* B, double* Q, double* Qd, doubl
   // scratch: the FP64 CG vectors are free outside a step
   CU(launch_step_begin(c, itime, 0));
   CU(launch_rhs_parts(c, c.A.y, c.A.r, c.A.p, c.A.q));
+  CU(launch_finalize(c, FIN_RHS, nullptr, 0, 0));
   int rc = sync_scal(c);
   if (rc) return rc;
+  if ((rc = diagnose(c))) return rc;
   if (B && (rc = download_padded(c, B, (const double*)c.A.y))) return rc;
   if (Q && (rc = download_padded(c, Q, (const double*)c.A.r))) return rc;
   if (Qd && (rc = download_padded(c, Qd, (const double*)c.A.p))) return rc;

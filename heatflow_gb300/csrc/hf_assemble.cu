@@ -218,6 +218,7 @@ __global__ void k_sinv(DevArrays A) {
   double dg = A.diag[g];
   if (dg >= 0.0) atomicOr(&A.scal[A.tile_inst[g / kTile]].devcheck, 2);   // NaN passes: B check reports it
   A.sinv[g] = 1.0 / sqrt(fabs(dg));
+  A.sinv32[g] = (float)A.sinv[g];
 }
 
 __global__ void k_scale(DevArrays A) {
@@ -237,6 +238,15 @@ __global__ void k_scale(DevArrays A) {
   double az = -A.cz[g] * si * A.sinv[ez];
   A.a64x[g] = ax; A.a64y[g] = ay; A.a64z[g] = az;
   A.a32x[g] = (float)ax; A.a32y[g] = (float)ay; A.a32z[g] = (float)az;
+  // H*1: the diagonal plus every face of the row
+  double rs = A.diag[g];
+  if (nx > 1 && (x + 1 < nx || d.px)) rs += A.cx[g];
+  if (nx > 1 && (x > 0 || d.px)) rs += A.cx[x > 0 ? g - 1 : g + nx - 1];
+  if (ny > 1 && (y + 1 < ny || d.py)) rs += A.cy[g];
+  if (ny > 1 && (y > 0 || d.py)) rs += A.cy[y > 0 ? g - nx : g + (ny - 1) * nx];
+  if (nz > 1 && (z + 1 < nz || d.pz)) rs += A.cz[g];
+  if (nz > 1 && (z > 0 || d.pz)) rs += A.cz[z > 0 ? g - nxy : g + (nz - 1) * nxy];
+  A.rsum[g] = rs;
 }
 
 // ---- parity probe: COO in the reference's storage order (sparse_Hmatrix) --------------------

@@ -24,6 +24,7 @@ struct Ctx {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   int64_t ninst = 0, ncells = 0, ntiles = 0;
+  int64_t grid_tiles = 0;        // blocks of the tile kernels (resident set, grid-stride)
   std::vector<InstDesc> h_inst;
   std::vector<InstBC> h_bc;
   std::vector<int64_t> h_tile0;
@@ -35,8 +36,12 @@ struct Ctx {
   InstScal* h_scal = nullptr;    // pinned mirror for polling
   bool state_set = false;
   bool any_heater = false, any_power = false, any_em = false, any_case5 = false;
-  // graph of one step (host loop replays it)
+  // graph of one step (hf_run replays it once per step, no host synchronisation in between)
   cudaGraphExec_t graph_exec = nullptr;
+  cudaGraph_t graph = nullptr;
+  CtrlState* d_ctrl = nullptr;
+  int graph_precision = -1;     // options the graph was captured with
+  int graph_criterion = -1;
   int64_t launches = 0;          // kernels launched on the device since creation
 };
 

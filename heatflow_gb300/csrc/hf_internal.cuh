@@ -29,7 +29,9 @@ constexpr double kStefBoltz = 5.670373e-8;   // mod_constants.f90:16
 constexpr int kBlock = 256;                  // threads per block of the cell kernels
 constexpr int kCellsPerThread = 4;
 constexpr int kTile = kBlock * kCellsPerThread;   // cells per tile (one block per tile)
-constexpr int kNR = 8;                       // reduction slots per tile
+constexpr int kNR = 8;
+// InstScal::status bit: some S was NaN; the failing vector is found by the diagnosis kernel.
+constexpr int kStatusRhsNan = 1 << 16;                       // reduction slots per tile
 // Instances are laid out at multiples of kTile cells, so tile t covers cells
 // [t*kTile, (t+1)*kTile) of exactly one instance; cells past an instance's end are padding.
 
@@ -78,10 +80,22 @@ struct InstScal {
   int32_t x0flag;       // any(x0 - Tp < TINY) (mod_evolve.f90:141)
   int32_t status;       // bit k set: HF_ENAN_B + k raised
   int32_t devcheck;     // nonzero: a device-side consistency check failed
+  int32_t tiny_pending; // x still needs the reference's +TINY (applied with the next update)
+  int32_t pad2;
   int32_t role[4];      // temperature buffers: [0]=T^n, [1]=T^(n-1), [2]=x read, [3]=x write
   double sigma_prev;    // scale used by the previous residual sweep
   double last_err, last_relres;   // of the last finished step
   int64_t last_iter;
+};
+
+// Device-side control of a captured step (CUDA graph with conditional nodes).
+struct CtrlState {
+  int64_t itime;      // step index of the next step
+  int64_t loop_iter;  // body iterations of the current step's solve loop
+  int64_t limit;      // bound on body iterations per step (termination guarantee)
+  int32_t guard_hit;  // the bound was reached (reported as HF_EDEVICE)
+  uint32_t fin_count; // finalize blocks arrived (last one sets the loop condition)
+  int64_t launches;   // kernels the captured steps launched
 };
 
 // Options mirrored on the device.
@@ -103,6 +117,8 @@ struct DevArrays {
   DevOpts opts;
   // static
   double *diag, *cx, *cy, *cz, *sinv, *a64x, *a64y, *a64z;
+  double* rsum;           // H*1 per cell (residual of x0 + TINY from that of x0)
+  float* sinv32;          // FP32 copy of sinv (scaling of FP32 right-hand sides/corrections)
   float *a32x, *a32y, *a32z;
   double *rhoc, *ccat, *bvec, *power, *emc;
   int8_t* icase;
@@ -112,10 +128,62 @@ struct DevArrays {
   // solver
   double *b, *y, *r, *p, *q;
   float *y32, *r32, *p32, *q32;
+  const int8_t* tile_heat;  // per tile: some cell needs the heater/radiation terms
   int64_t ncells, ntiles, ninst;
 };
 
 // ---- helpers ---------------------------------------------------------------------------------
+// IEEE-754 bit access through inline PTX, so that tests and format conversions stay integer
+// instructions instead of being turned back into FP64 compares/conversions: on GB300 the FP64
+// pipe (~1 TFLOP/s) is the scarce resource of every FP64 kernel.
+__device__ __forceinline__ unsigned long long dbits(double v) {
+  unsigned long long b;
+  asm("mov.b64 %0, %1;" : "=l"(b) : "d"(v));
+  return b;
+}
+__device__ __forceinline__ double bitsd(unsigned long long b) {
+  double v;
+  asm("mov.b64 %0, %1;" : "=d"(v) : "l"(b));
+  return v;
+}
+__device__ __forceinline__ bool dbl_is_zero(double v) { return (dbits(v) << 1) == 0ull; }
+__device__ __forceinline__ bool dbl_is_nan(double v) {
+  const unsigned long long b = dbits(v);
+  return ((b >> 52) & 0x7ffull) == 0x7ffull && (b & 0xfffffffffffffull) != 0ull;
+}
+// v < t for finite t > 0 and non-NaN v (sign-magnitude order of the bit patterns).
+__device__ __forceinline__ bool dbl_lt_pos(double v, double t) {
+  const long long b = (long long)dbits(v);
+  return b < 0 || (unsigned long long)b < dbits(t);
+}
+// FP64 -> FP32 by truncation of the mantissa (integer instructions only).  Magnitudes outside
+// the FP32 normal range saturate to 0 or infinity; NaN stays NaN.
+__device__ __forceinline__ float f64_to_f32_trunc(double v) {
+  const unsigned long long u = dbits(v);
+  const unsigned sign = (unsigned)(u >> 63) << 31;
+  const int e = (int)((u >> 52) & 0x7ffull);
+  if (e == 0x7ff) return __uint_as_float(sign | 0x7f800000u | ((u & 0xfffffffffffffull) ? 0x400000u : 0u));
+  const int fe = e - 1023 + 127;
+  if (fe >= 255) return __uint_as_float(sign | 0x7f800000u);
+  if (fe <= 0) return __uint_as_float(sign);
+  return __uint_as_float(sign | ((unsigned)fe << 23) | (unsigned)((u >> 29) & 0x7fffffull));
+}
+// FP32 -> FP64, exact (integer instructions only).
+__device__ __forceinline__ double f32_to_f64(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+  const unsigned e = (u >> 23) & 0xffu;
+  unsigned long long m = u & 0x7fffffu;
+  if (e == 0xffu) return bitsd(sign | 0x7ff0000000000000ull | (m << 29));
+  if (e == 0u) {
+    if (m == 0ull) return bitsd(sign);
+    const int p = 31 - __clz((int)m);                  // subnormal: normalise
+    const unsigned long long mant = (m << (52 - p)) & 0xfffffffffffffull;
+    return bitsd(sign | ((unsigned long long)(p - 149 + 1023) << 52) | mant);
+  }
+  return bitsd(sign | ((unsigned long long)(e - 127 + 1023) << 52) | (m << 29));
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -144,43 +212,53 @@ __device__ __forceinline__ void block_sum(double (&v)[NRV], double* smem /* [32*
   __syncthreads();
 }
 
-// Write this tile's partial sums; returns true (in all threads) for the last tile of the
-// instance to arrive, which then holds the instance totals in tot[] (fixed summation order).
+// Write this tile's partial sums (fixed slot per tile; summed by a finalize kernel).
+// FP64 values go through shared memory and only warp 0 adds them (8 + 5 adds per value per
+// block): on GB300 every FP64 warp instruction costs the slow FP64 pipe, so a shuffle tree in
+// all eight warps would cost more than the kernel's own arithmetic.
 template <int NRV>
-__device__ bool tile_reduce(const DevArrays& A, int inst, int64_t tile, double (&v)[NRV],
-                            double (&tot)[NRV]) {
-  __shared__ double red[32 * NRV];
-  __shared__ bool last;
-  block_sum<NRV>(v, red);
-  if (threadIdx.x == 0) {
+__device__ __forceinline__ void tile_store(const DevArrays& A, int64_t tile, const double (&v)[NRV]) {
+  __shared__ double stage[NRV][kBlock];
+  __syncthreads();   // the previous tile of this block has finished reading the stage
 #pragma unroll
-    for (int k = 0; k < NRV; ++k) A.partials[tile * kNR + k] = v[k];
-    __threadfence();
-    unsigned prev = atomicAdd(&A.counters[inst], 1u);
-    last = (prev == (unsigned)A.inst[inst].ntiles - 1u);
+  for (int k = 0; k < NRV; ++k) stage[k][threadIdx.x] = v[k];
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
+#pragma unroll
+    for (int k = 0; k < NRV; ++k) {
+      double t = stage[k][lane];
+#pragma unroll
+      for (int w = 1; w < kBlock / 32; ++w) t += stage[k][lane + 32 * w];
+      t = warp_sum(t);
+      if (lane == 0) A.partials[tile * kNR + k] = t;
+    }
+  }
+}
+
+// FP32 partials: block sum in FP32, one conversion to FP64 per tile.
+template <int NRV>
+__device__ __forceinline__ void tile_store_f(const DevArrays& A, int64_t tile, const float (&v)[NRV]) {
+  __shared__ float red[NRV][kBlock / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();   // the previous tile of this block has finished reading red
+#pragma unroll
+  for (int k = 0; k < NRV; ++k) {
+    float t = v[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (lane == 0) red[k][warp] = t;
   }
   __syncthreads();
-  if (!last) return false;
-  __threadfence();
-  const InstDesc& d = A.inst[inst];
-  double acc[NRV];
+  if (warp == 0) {
 #pragma unroll
-  for (int k = 0; k < NRV; ++k) acc[k] = 0.0;
-  for (int64_t t = threadIdx.x; t < d.ntiles; t += blockDim.x) {
+    for (int k = 0; k < NRV; ++k) {
+      float t = lane < kBlock / 32 ? red[k][lane] : 0.f;
 #pragma unroll
-    for (int k = 0; k < NRV; ++k) acc[k] += __ldcg(&A.partials[(d.tile0 + t) * kNR + k]);
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+      if (lane == 0) A.partials[tile * kNR + k] = (double)t;
+    }
   }
-  block_sum<NRV>(acc, red);
-  __shared__ double out[NRV];
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int k = 0; k < NRV; ++k) out[k] = acc[k];
-    A.counters[inst] = 0u;
-  }
-  __syncthreads();
-#pragma unroll
-  for (int k = 0; k < NRV; ++k) tot[k] = out[k];
-  return true;
 }
 
 // Coordinates of local cell l in an instance.
@@ -206,10 +284,22 @@ cudaError_t launch_coo(Ctx& c, int64_t instance, int64_t* d_counts, int64_t* d_i
 cudaError_t launch_step_begin(Ctx& c, int64_t itime, int first_of_run);
 cudaError_t launch_rhs(Ctx& c);
 cudaError_t launch_rhs_parts(Ctx& c, double* B, double* Q, double* Qd, double* Sc);
-cudaError_t launch_residual(Ctx& c, int mode);
-cudaError_t launch_inner_iteration(Ctx& c, int fp32);
+cudaError_t launch_rhs_diagnose(Ctx& c);
+cudaError_t launch_residual(Ctx& c, int mode, CtrlState* ctrl = nullptr,
+                            cudaGraphConditionalHandle hw = 0, int graph = 0);
+cudaError_t launch_inner_iteration(Ctx& c, int fp32, CtrlState* ctrl = nullptr,
+                                   cudaGraphConditionalHandle hw = 0, int graph = 0);
 cudaError_t launch_step_end(Ctx& c);
 cudaError_t launch_apply(Ctx& c, const double* x, double* y);
 cudaError_t launch_single(Ctx& c, int which);
+cudaError_t launch_graph_step_begin(Ctx& c, CtrlState* ctrl);
+cudaError_t launch_graph_step_end(Ctx& c, CtrlState* ctrl);
+cudaError_t launch_ctrl_select(Ctx& c, CtrlState* ctrl, cudaGraphConditionalHandle hs,
+                               cudaGraphConditionalHandle hw);
+// Finalize kernels: sum the tile partials of each instance and run the scalar epilogue of the
+// kernel that produced them.  With graph != 0 the last block also sets the loop condition hw.
+enum { FIN_RHS = 0, FIN_RHS_DIAG, FIN_RES_INIT, FIN_RES, FIN_SPMV, FIN_UPD };
+cudaError_t launch_finalize(Ctx& c, int kind, CtrlState* ctrl, cudaGraphConditionalHandle hw,
+                            int graph);
 
 }  // namespace hf

@@ -1,8 +1,14 @@
 // Per-step right-hand side: heater (mod_heating.f90:27-169), Cattaneo term
 // (mod_cattaneo.f90:23-42), S and the initial guess (mod_evolve.f90:112-141), in one pass.
 //
-// Compiled with -fmad=false so that S is rounded exactly as the reference writes it; the kernel
-// is HBM-bound, so separate rounding costs nothing.
+// GB300 executes FP64 at ~1 TFLOP/s (measured), so an FP64 pass over the grid is bound by FP64
+// instructions, not by HBM.  This kernel therefore spends FP64 instructions only on the values
+// the reference computes: S, x0 = T + (T - T_pp) and x0 - T, plus ||S||^2.  The x0 test and
+// the NaN screening use integer operations on the IEEE bits: any NaN among Q, Qdens, S_cat
+// propagates into S and so into ||S||^2, and only then does the host run the diagnosis variant
+// (DIAG) that finds the first failing vector in the reference's check order.
+//
+// Compiled with -fmad=false so that S is rounded exactly as the reference writes it.
 #include "hf_ctx.cuh"
 
 namespace hf {
@@ -33,92 +39,122 @@ __device__ __forceinline__ double heat_case(int cs, double P, double tau, int64_
 }
 
 // One block per tile.  PARTS: also write B, Q, Qdens and S_cat (parity probe hf_get_rhs).
-template <bool PARTS>
-__global__ void __launch_bounds__(kBlock) k_rhs(DevArrays A, double* oB, double* oQ, double* oQd,
-                                                double* oSc) {
-  const int64_t tile = blockIdx.x;
+// DIAG: count NaNs per vector (failure path only).
+template <bool PARTS, bool DIAG>
+__device__ __forceinline__ void rhs_tile(const DevArrays& A, int64_t tile, double* oB, double* oQ,
+                                         double* oQd, double* oSc) {
   const int inst = A.tile_inst[tile];
   const InstDesc& d = A.inst[inst];
   InstScal& s = A.scal[inst];
-  if (!s.outer_active) return;
-  const int64_t itime = s.itime;
-  const double* Tp = A.tbuf[s.role[0]] + d.off;
-  const double* Tpp = A.tbuf[s.role[1]] + d.off;
-  double* X = A.tbuf[s.role[2]] + d.off;
-  double acc[6] = {0, 0, 0, 0, 0, 0};  // bb, x0 flags, nan Q, nan Qdens, nan S_cat, nan S
-  const double tb4 = d.has_em ? pow(d.t_bath, 4.0) : 0.0;
+  if (!DIAG && !s.outer_active) return;
+  if (DIAG && !(s.status & kStatusRhsNan)) return;
+  const int64_t itime = DIAG ? s.failed_step : s.itime;
+  const int64_t off = d.off;
+  const int32_t n = d.n;
+  // heater() runs for every cell when any exists (mod_evolve.f90:79); with emissivity every cell
+  // has a radiative term, otherwise only tiles holding a heated cell have nonzero Q
+  const bool heater = d.heater && (d.has_em || A.tile_heat[tile]), has_power = d.has_power,
+             has_em = d.has_em, case5 = d.has_case5;
+  const bool cat = d.icattaneo == 1, steady = d.isteady != 0;
+  const int qmode = d.qdens_mode;
+  const double inv_dt = d.inv_dt, vol = d.volume, hvol = d.heated_volume, power_in = d.power_in;
+  const double* __restrict__ Tp = A.tbuf[s.role[0]] + off;
+  const double* __restrict__ Tpp = A.tbuf[s.role[1]] + off;
+  double* __restrict__ X = A.tbuf[s.role[2]] + off;
+  const double* __restrict__ rhoc = A.rhoc + off;
+  const double* __restrict__ ccat = A.ccat + off;
+  const double* __restrict__ bvec = A.bvec + off;
+  double* __restrict__ bout = A.b + off;
+  const double tb4 = has_em ? pow(d.t_bath, 4.0) : 0.0;
+  const double dt2 = case5 ? pow(d.time_step, 2.0) : 0.0;
+  double bb = 0.0;
+  int flag = 0;
+  int nan_q = 0, nan_qd = 0, nan_sc = 0, nan_s = 0;
 #pragma unroll
   for (int k = 0; k < kCellsPerThread; ++k) {
-    const int64_t g = tile * kTile + k * kBlock + threadIdx.x;
-    const int64_t l = g - d.off;
-    if (l >= d.n) continue;
+    const int32_t l = (int32_t)(tile * kTile - off) + k * kBlock + threadIdx.x;
+    if (l >= n) continue;
     const double tp = Tp[l], tpp = Tpp[l];
     double q = 0.0, qd = 0.0;
-    if (d.heater) {
-      const double P = d.has_power ? A.power[g] : d.power_in;
-      const double tau = d.has_case5 ? A.tau_s[g] * pow(d.time_step, 2.0) : 0.0;
-      q = heat_case(A.icase[g], P, tau, itime, d);
-      if (d.has_em) q = q - A.emc[g] * (pow(tp, 4.0) - tb4);
-      if (d.qdens_mode == HF_QDENS_CELL_VOLUME) qd = q / d.volume;
-      else if (d.heated_volume > 0.0) qd = q / d.heated_volume;
-      acc[2] += isnan(q) ? 1.0 : 0.0;
-      acc[3] += isnan(qd) ? 1.0 : 0.0;
+    if (heater) {
+      const int cs = A.icase[off + l];
+      if (cs > 0 && cs < 7) {
+        const double P = has_power ? A.power[off + l] : power_in;
+        const double tau = case5 ? A.tau_s[off + l] * dt2 : 0.0;
+        q = heat_case(cs, P, tau, itime, d);
+      }
+      if (has_em) q = q - A.emc[off + l] * (pow(tp, 4.0) - tb4);
+      if (!dbl_is_zero(q)) {
+        if (qmode == HF_QDENS_CELL_VOLUME) qd = q / vol;
+        else if (hvol > 0.0) qd = q / hvol;
+      }
+      if (DIAG) { nan_q += dbl_is_nan(q); nan_qd += dbl_is_nan(qd); }
     }
     double sc = 0.0;
-    if (d.icattaneo == 1) {
-      sc = (tpp - 2.0 * tp) * A.ccat[g];
-      acc[4] += isnan(sc) ? 1.0 : 0.0;
+    if (cat) {
+      sc = fma(-2.0, tp, tpp) * ccat[l];   // = (tpp - 2 tp) * ccat: 2 tp is exact
+      if (DIAG) nan_sc += dbl_is_nan(sc);
     }
-    const double B = A.bvec[g];
+    const double B = bvec[l];
     double S;
-    if (d.isteady == 0) {
-      S = -d.inv_dt * tp * A.rhoc[g] - qd - B;
-      if (d.icattaneo == 1) S = S + sc;
+    if (!steady) {
+      S = -inv_dt * tp * rhoc[l];
+      if (!dbl_is_zero(qd)) S = S - qd;
+      if (!dbl_is_zero(B)) S = S - B;
+      if (cat) S = S + sc;
     } else {
-      S = -qd - B;
+      S = -qd;
+      if (!dbl_is_zero(B)) S = S - B;
     }
-    acc[5] += isnan(S) ? 1.0 : 0.0;
+    if (DIAG) nan_s += dbl_is_nan(S);
     const double x0 = tp + (tp - tpp);
-    acc[1] += (x0 - tp < kTiny) ? 1.0 : 0.0;
-    A.b[g] = S;
+    flag |= dbl_lt_pos(x0 - tp, kTiny) ? 1 : 0;
+    bout[l] = S;
     X[l] = x0;
-    acc[0] += S * S;
+    bb = fma(S, S, bb);
     if (PARTS) {
-      oB[g] = B;
-      oQ[g] = q;
-      oQd[g] = qd;
-      oSc[g] = sc;
+      oB[off + l] = B;
+      oQ[off + l] = q;
+      oQd[off + l] = qd;
+      oSc[off + l] = sc;
     }
   }
-  double tot[6];
-  if (!tile_reduce<6>(A, inst, tile, acc, tot)) return;
-  if (threadIdx.x == 0) {
-    s.bb = tot[0];
-    s.x0flag = tot[1] > 0.0 ? 1 : 0;
-    int st = 0;
-    if (tot[2] > 0) st |= 1 << (HF_ENAN_Q - HF_ENAN_B);
-    if (tot[3] > 0) st |= 1 << (HF_ENAN_QDENS - HF_ENAN_B);
-    if (tot[4] > 0) st |= 1 << (HF_ENAN_SCAT - HF_ENAN_B);
-    if (tot[5] > 0) st |= 1 << (HF_ENAN_S - HF_ENAN_B);
-    if (st) {
-      s.status |= st;
-      s.outer_active = 0;
-      s.failed_step = itime;
+  const int any_flag = __syncthreads_or(flag);
+  if (DIAG) {
+    const int c1 = __syncthreads_count(nan_q), c2 = __syncthreads_count(nan_qd);
+    const int c3 = __syncthreads_count(nan_sc), c4 = __syncthreads_count(nan_s);
+    if (threadIdx.x == 0) {
+      A.partials[tile * kNR + 1] = (double)c1;
+      A.partials[tile * kNR + 2] = (double)c2;
+      A.partials[tile * kNR + 3] = (double)c3;
+      A.partials[tile * kNR + 4] = (double)c4;
     }
-    // scale of the first FP32 residual: a power of two near rms(S)/rms(|H_II|^(1/2)) * 1e-6
-    double rms = sqrt(tot[0] / (double)d.n) * d.mean_sinv * 1e-6;
-    s.sigma = (A.opts.precision == HF_PREC_MIXED && rms > 0.0 && isfinite(rms))
-                  ? exp2(rint(log2(rms))) : 1.0;
+  } else if (threadIdx.x == 0) {
+    A.partials[tile * kNR + 1] = any_flag ? 1.0 : 0.0;
   }
+  const double v[1] = {bb};
+  tile_store<1>(A, tile, v);
+}
+
+template <bool PARTS, bool DIAG>
+__global__ void __launch_bounds__(kBlock) k_rhs(DevArrays A, double* oB, double* oQ, double* oQd,
+                                                double* oSc) {
+  for (int64_t tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x)
+    rhs_tile<PARTS, DIAG>(A, tile, oB, oQ, oQd, oSc);
 }
 
 cudaError_t launch_rhs(Ctx& c) {
-  k_rhs<false><<<(unsigned)c.ntiles, kBlock, 0, c.stream>>>(c.A, nullptr, nullptr, nullptr, nullptr);
+  k_rhs<false, false><<<(unsigned)c.grid_tiles, kBlock, 0, c.stream>>>(c.A, nullptr, nullptr, nullptr, nullptr);
   return cudaGetLastError();
 }
 
 cudaError_t launch_rhs_parts(Ctx& c, double* B, double* Q, double* Qd, double* Sc) {
-  k_rhs<true><<<(unsigned)c.ntiles, kBlock, 0, c.stream>>>(c.A, B, Q, Qd, Sc);
+  k_rhs<true, false><<<(unsigned)c.grid_tiles, kBlock, 0, c.stream>>>(c.A, B, Q, Qd, Sc);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rhs_diagnose(Ctx& c) {
+  k_rhs<false, true><<<(unsigned)c.grid_tiles, kBlock, 0, c.stream>>>(c.A, nullptr, nullptr, nullptr, nullptr);
   return cudaGetLastError();
 }
 

@@ -6,61 +6,72 @@
 // is 1: identical iterates, no divisions and one coefficient array fewer per pass.
 //
 // Each step is a refinement loop:
-//   x = x0 (+TINY)                                         k_residual<INIT>
-//   repeat:  r = S - H x (FP64, true residual), test ||r||/||S||
-//            g = -S^-1 r / sigma ; solve Ah y = g by CG       (FP64, or FP32 in mixed mode)
-//            x += sigma S^-1 y                              k_residual<UPDATE> (fused with the next r)
-// The FP64 path asks its CG for the whole reduction at once (one sweep normally suffices); the
-// mixed path runs FP32 CG with FP32 SpMV accumulation and refines in FP64.
+//   x = x0                                                 (RHS kernel)
+//   repeat:  r = S - H x (FP64, true residual), test ||r||/||S||        k_residual
+//            g = -S^-1 r / sigma ; solve Ah y = g by CG   (FP64, or FP32 in mixed mode)
+//            x += sigma S^-1 y                                           k_xupdate
+// The reference adds TINY to every x0 when any x0 - T < TINY (mod_evolve.f90:141).  Here the
+// first residual is that of x0 + TINY, formed as r(x0) - TINY * (H 1) from a stored row-sum
+// vector, and the TINY itself joins x with the first update: the same iterate, without seven
+// extra FP64 additions per cell.
+//
+// GB300 issues FP64 at ~1 TFLOP/s, so the FP64 kernels (residual, x update, FP64 CG) are bound by
+// FP64 instructions: they spend them only on the arithmetic itself (no FP64 compares, no FP64
+// accumulation of FP32 quantities).  The FP32 kernels accumulate in FP32 within a block.
 //
 // All solver state is per instance in device memory; tiles of instances that are not in the
 // phase a kernel serves return at once (per-instance convergence masks).
+#include <algorithm>
+
 #include "hf_ctx.cuh"
 
 namespace hf {
 
-enum { RES_INIT = 0, RES_UPDATE = 1 };
+// Register copy of the geometry of one instance.
+struct Geo {
+  int64_t off;
+  int32_t n, nx, ny, nz;
+  bool px, py, pz;
+  __device__ explicit Geo(const InstDesc& d)
+      : off(d.off), n(d.n), nx(d.nx), ny(d.ny), nz(d.nz), px(d.px), py(d.py), pz(d.pz) {}
+};
 
-// y = H x for local cell l (unscaled operator, FP64).  xv(n) yields x at local cell n.
-template <class XF>
-__device__ __forceinline__ double apply_H(const DevArrays& A, const InstDesc& d, int64_t g,
-                                          int64_t l, const Coord& c, XF xv) {
-  const int64_t nx = d.nx, nxy = (int64_t)d.nx * d.ny;
-  double acc = A.diag[g] * xv(l);
-  if (c.x + 1 < d.nx) acc = fma(A.cx[g], xv(l + 1), acc);
-  else if (d.px && d.nx > 1) acc = fma(A.cx[g], xv(l - (nx - 1)), acc);
-  if (c.x > 0) acc = fma(A.cx[g - 1], xv(l - 1), acc);
-  else if (d.px && d.nx > 1) acc = fma(A.cx[g + nx - 1], xv(l + nx - 1), acc);
-  if (c.y + 1 < d.ny) acc = fma(A.cy[g], xv(l + nx), acc);
-  else if (d.py && d.ny > 1) acc = fma(A.cy[g], xv(l - (int64_t)(d.ny - 1) * nx), acc);
-  if (c.y > 0) acc = fma(A.cy[g - nx], xv(l - nx), acc);
-  else if (d.py && d.ny > 1) acc = fma(A.cy[g + (int64_t)(d.ny - 1) * nx], xv(l + (int64_t)(d.ny - 1) * nx), acc);
-  if (c.z + 1 < d.nz) acc = fma(A.cz[g], xv(l + nxy), acc);
-  else if (d.pz && d.nz > 1) acc = fma(A.cz[g], xv(l - (int64_t)(d.nz - 1) * nxy), acc);
-  if (c.z > 0) acc = fma(A.cz[g - nxy], xv(l - nxy), acc);
-  else if (d.pz && d.nz > 1) acc = fma(A.cz[g + (int64_t)(d.nz - 1) * nxy], xv(l + (int64_t)(d.nz - 1) * nxy), acc);
-  return acc;
+// Folds the six face terms of cell l: fold(c_face, v(neighbour)).  c_a[I] is the face to the +
+// neighbour stored at the cell; the - face is stored at the neighbour; periodic axes wrap.
+template <typename C, class V, class F>
+__device__ __forceinline__ void stencil(const Geo& G, const C* __restrict__ cx,
+                                        const C* __restrict__ cy, const C* __restrict__ cz,
+                                        int32_t l, const Coord& c, V v, F fold) {
+  const int32_t nx = G.nx, nxy = G.nx * G.ny;
+  if (c.x + 1 < G.nx) fold(cx[l], v(l + 1));
+  else if (G.px && G.nx > 1) fold(cx[l], v(l - (nx - 1)));
+  if (c.x > 0) fold(cx[l - 1], v(l - 1));
+  else if (G.px && G.nx > 1) fold(cx[l + nx - 1], v(l + nx - 1));
+  if (c.y + 1 < G.ny) fold(cy[l], v(l + nx));
+  else if (G.py && G.ny > 1) fold(cy[l], v(l - (G.ny - 1) * nx));
+  if (c.y > 0) fold(cy[l - nx], v(l - nx));
+  else if (G.py && G.ny > 1) fold(cy[l + (G.ny - 1) * nx], v(l + (G.ny - 1) * nx));
+  if (c.z + 1 < G.nz) fold(cz[l], v(l + nxy));
+  else if (G.pz && G.nz > 1) fold(cz[l], v(l - (G.nz - 1) * nxy));
+  if (c.z > 0) fold(cz[l - nxy], v(l - nxy));
+  else if (G.pz && G.nz > 1) fold(cz[l + (G.nz - 1) * nxy], v(l + (G.nz - 1) * nxy));
 }
 
-// q = Ah p for local cell l (unit diagonal, coefficients a already carry the minus sign).
-template <typename T, class PF>
-__device__ __forceinline__ T apply_Ah(const T* ax, const T* ay, const T* az, const InstDesc& d,
-                                      int64_t g, int64_t l, const Coord& c, PF pv) {
-  const int64_t nx = d.nx, nxy = (int64_t)d.nx * d.ny;
-  T acc = pv(l);
-  if (c.x + 1 < d.nx) acc = fma(ax[g], pv(l + 1), acc);
-  else if (d.px && d.nx > 1) acc = fma(ax[g], pv(l - (nx - 1)), acc);
-  if (c.x > 0) acc = fma(ax[g - 1], pv(l - 1), acc);
-  else if (d.px && d.nx > 1) acc = fma(ax[g + nx - 1], pv(l + nx - 1), acc);
-  if (c.y + 1 < d.ny) acc = fma(ay[g], pv(l + nx), acc);
-  else if (d.py && d.ny > 1) acc = fma(ay[g], pv(l - (int64_t)(d.ny - 1) * nx), acc);
-  if (c.y > 0) acc = fma(ay[g - nx], pv(l - nx), acc);
-  else if (d.py && d.ny > 1) acc = fma(ay[g + (int64_t)(d.ny - 1) * nx], pv(l + (int64_t)(d.ny - 1) * nx), acc);
-  if (c.z + 1 < d.nz) acc = fma(az[g], pv(l + nxy), acc);
-  else if (d.pz && d.nz > 1) acc = fma(az[g], pv(l - (int64_t)(d.nz - 1) * nxy), acc);
-  if (c.z > 0) acc = fma(az[g - nxy], pv(l - nxy), acc);
-  else if (d.pz && d.nz > 1) acc = fma(az[g + (int64_t)(d.nz - 1) * nxy], pv(l + (int64_t)(d.nz - 1) * nxy), acc);
-  return acc;
+__device__ __forceinline__ Coord coord3(const Geo& G, int32_t l) {
+  Coord c;
+  const uint32_t ul = (uint32_t)l;
+  const uint32_t row = ul / (uint32_t)G.nx;
+  c.x = (int32_t)(ul - row * (uint32_t)G.nx);
+  const uint32_t pl = row / (uint32_t)G.ny;
+  c.y = (int32_t)(row - pl * (uint32_t)G.ny);
+  c.z = (int32_t)pl;
+  return c;
+}
+
+__device__ __forceinline__ float warp_sumf(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
 }
 
 template <typename T> struct Vec;
@@ -83,11 +94,13 @@ template <> struct Vec<float> {
   __device__ static const float* az(const DevArrays& A) { return A.a32z; }
 };
 
+// Local cell index of the k-th cell of this thread in the block's tile.
+__device__ __forceinline__ int32_t tile_cell(int64_t tile, const Geo& G, int k) {
+  return (int32_t)(tile * kTile - G.off) + k * kBlock + (int32_t)threadIdx.x;
+}
+
 // ---- step bookkeeping ------------------------------------------------------------------------
-__global__ void k_step_begin(DevArrays A, int64_t itime) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= A.ninst) return;
-  InstScal& s = A.scal[i];
+__device__ __forceinline__ void begin_step(InstScal& s, int64_t itime) {
   s.itime = itime;
   s.outer_active = (s.status == 0) ? 1 : 0;
   s.inner_active = 0;
@@ -95,91 +108,309 @@ __global__ void k_step_begin(DevArrays A, int64_t itime) {
   s.iter = 0;
   s.step_iters = 0;
   s.x0flag = 0;
+  s.tiny_pending = 0;
   s.err = 0.0;
 }
 
 // Finished steps rotate the temperature roles: T^(n-1) <- T^n, T^n <- x (mod_evolve.f90:169-170).
-__global__ void k_step_end(DevArrays A) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= A.ninst) return;
-  InstScal& s = A.scal[i];
+__device__ __forceinline__ void end_step(InstScal& s) {
   if (s.status != 0) return;
-  int r0 = s.role[0], r1 = s.role[1], r2 = s.role[2], r3 = s.role[3];
+  const int r0 = s.role[0], r1 = s.role[1], r2 = s.role[2], r3 = s.role[3];
   s.role[0] = r2;  // x
   s.role[1] = r0;  // old T^n
   s.role[2] = r1;  // free
   s.role[3] = r3;  // free
 }
 
-// ---- FP64 residual sweep (+ solution update) ---------------------------------------------------
-// MODE RES_INIT:   x = x0 + TINY*flag (mod_evolve.f90:140-141), x0 from the RHS kernel.
-// MODE RES_UPDATE: x = x + sigma_prev * S^-1 y (y from the inner solve, type TY).
-// Writes x (into the x-write buffer), g = -S^-1 (S - H x) / sigma into the inner residual r (type
-// TR) and the inner solution is restarted from 0.
-template <int MODE, typename TY, typename TR>
-__global__ void __launch_bounds__(kBlock) k_residual(DevArrays A) {
-  const int64_t tile = blockIdx.x;
+__global__ void k_step_begin(DevArrays A, int64_t itime) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < A.ninst) begin_step(A.scal[i], itime);
+}
+
+__global__ void k_step_end(DevArrays A) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < A.ninst) end_step(A.scal[i]);
+}
+
+// ---- FP64 true residual ------------------------------------------------------------------------
+// r = S - H x with x in the x-read buffer (INIT: x0 from the RHS kernel) or, after an update, in
+// the x-write buffer (then the roles swap).  Writes g = -S^-1 r / sigma into the inner residual
+// (type TR).  FP64 work per cell: 7 FMA for S - Hx and 1 FMA for ||r||^2.
+template <bool INIT, typename TR>
+__device__ __forceinline__ void residual_tile(const DevArrays& A, int64_t tile) {
   const int inst = A.tile_inst[tile];
-  const InstDesc& d = A.inst[inst];
   InstScal& s = A.scal[inst];
   if (!s.outer_active || s.inner_active) return;
-  if (MODE == RES_INIT && s.refine != 0) return;
-  if (MODE == RES_UPDATE && s.refine == 0) return;
-  const double* XR = A.tbuf[s.role[2]] + d.off;
-  double* XW = A.tbuf[s.role[3]] + d.off;
-  const double* sinv = A.sinv + d.off;
-  const TY* Y = Vec<TY>::y(A) + d.off;
-  TR* R = Vec<TR>::r(A) + d.off;
-  const double tadd = s.x0flag ? kTiny : 0.0;
-  const double sig_prev = s.sigma_prev;
-  const double sig = s.sigma;
-  const double isig = 1.0 / sig;
-  const bool use_y = (s.iter > 0);   // the last inner solve produced a correction
-  auto xv = [&](int64_t n) -> double {
-    if (MODE == RES_INIT) return XR[n] + tadd;
-    return use_y ? fma(sig_prev * sinv[n], (double)Y[n], XR[n]) : XR[n];
-  };
-  double acc[3] = {0, 0, 0};  // ||r||^2, ||g||^2, NaN count of x
+  if (INIT != (s.refine == 0)) return;
+  const Geo G(A.inst[inst]);
+  const double* __restrict__ X = A.tbuf[INIT ? s.role[2] : s.role[3]] + G.off;
+  const double* __restrict__ diag = A.diag + G.off;
+  const double* __restrict__ b = A.b + G.off;
+  const double* __restrict__ cx = A.cx + G.off;
+  const double* __restrict__ cy = A.cy + G.off;
+  const double* __restrict__ cz = A.cz + G.off;
+  const float* __restrict__ sinv32 = A.sinv32 + G.off;
+  const double* __restrict__ sinv = A.sinv + G.off;
+  TR* __restrict__ R = Vec<TR>::r(A) + G.off;
+  const float isig = (float)(1.0 / s.sigma);
+  double gg64 = 0.0;
+  // INIT: the residual of x0 + TINY (mod_evolve.f90:141) is r(x0) - TINY * H1
+  const bool tiny = INIT && s.x0flag;
+  const double* __restrict__ rsum = A.rsum + G.off;
+  double rr = 0.0;
+  float gg = 0.f;
 #pragma unroll
   for (int k = 0; k < kCellsPerThread; ++k) {
-    const int64_t g = tile * kTile + k * kBlock + threadIdx.x;
-    const int64_t l = g - d.off;
-    if (l >= d.n) continue;
-    const Coord c = coord_of(d, (int32_t)l);
-    const double xc = xv(l);
-    const double hx = apply_H(A, d, g, l, c, xv);
-    const double rv = A.b[g] - hx;
-    XW[l] = xc;
-    const double gv = -sinv[l] * rv * isig;
-    R[l] = (TR)gv;
-    acc[0] = fma(rv, rv, acc[0]);
-    acc[1] = fma(gv, gv, acc[1]);
-    acc[2] += isnan(xc) ? 1.0 : 0.0;
+    const int32_t l = tile_cell(tile, G, k);
+    if (l >= G.n) continue;
+    const Coord c = coord3(G, l);
+    double acc = fma(-diag[l], X[l], b[l]);
+    if (tiny) acc = fma(-kTiny, rsum[l], acc);
+    stencil(G, cx, cy, cz, l, c, [&](int32_t m) { return X[m]; },
+            [&](double cf, double xv) { acc = fma(-cf, xv, acc); });
+    rr = fma(acc, acc, rr);
+    if (sizeof(TR) == 4) {               // mixed: g in FP32, scaled by 1/sigma
+      const float g = -sinv32[l] * f64_to_f32_trunc(acc) * isig;
+      R[l] = (TR)g;
+      gg = fmaf(g, g, gg);
+    } else {                             // FP64 path: sigma = 1
+      const double g = -sinv[l] * acc;
+      R[l] = (TR)g;
+      gg64 = fma(g, g, gg64);
+    }
   }
-  double tot[3];
-  if (!tile_reduce<3>(A, inst, tile, acc, tot)) return;
-  if (threadIdx.x != 0) return;
-  // epilogue: the instance's residual is complete
+  if (sizeof(TR) == 4) {
+    const float f[1] = {gg};
+    __syncthreads();   // also orders this tile after the previous tile's use of red
+    {
+      __shared__ float red[kBlock / 32];
+      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+      float t = f[0];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+      if (lane == 0) red[warp] = t;
+      __syncthreads();
+      if (warp == 0) {
+        t = lane < kBlock / 32 ? red[lane] : 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (lane == 0) A.partials[tile * kNR + 1] = (double)t;
+      }
+    }
+    const double v[1] = {rr};
+    tile_store<1>(A, tile, v);
+  } else {
+    const double v[2] = {rr, gg64};
+    tile_store<2>(A, tile, v);
+  }
+}
+
+// ---- solution update: x_new = x + sigma S^-1 y (+ TINY once) -----------------------------------
+template <typename TY>
+__device__ __forceinline__ void xupdate_tile(const DevArrays& A, int64_t tile) {
+  const int inst = A.tile_inst[tile];
+  const InstScal& s = A.scal[inst];
+  if (!s.outer_active || s.inner_active || s.refine == 0) return;
+  const Geo G(A.inst[inst]);
+  const double* __restrict__ XR = A.tbuf[s.role[2]] + G.off;
+  double* __restrict__ XW = A.tbuf[s.role[3]] + G.off;
+  const TY* __restrict__ Y = Vec<TY>::y(A) + G.off;
+  const double* __restrict__ sinv = A.sinv + G.off;
+  const float* __restrict__ sinv32 = A.sinv32 + G.off;
+  const bool use_y = s.iter > 0;
+  const bool tiny = s.tiny_pending != 0;
+  const float sig = (float)s.sigma_prev;
+#pragma unroll
+  for (int k = 0; k < kCellsPerThread; ++k) {
+    const int32_t l = tile_cell(tile, G, k);
+    if (l >= G.n) continue;
+    double x = XR[l];
+    if (tiny) x = x + kTiny;
+    if (use_y) {
+      if (sizeof(TY) == 8) x = fma(sinv[l], (double)Y[l], x);   // sigma = 1 on the FP64 path
+      else x = x + f32_to_f64(sig * sinv32[l] * (float)Y[l]);
+    }
+    XW[l] = x;
+  }
+}
+
+// ---- inner CG on Ah (type T) -------------------------------------------------------------------
+// k_cg_p:    p = r + beta p  (beta = 0 on the first iteration)
+template <typename T>
+__device__ __forceinline__ void cg_p_tile(const DevArrays& A, int64_t tile) {
+  const int inst = A.tile_inst[tile];
+  const InstScal& s = A.scal[inst];
+  if (!s.inner_active) return;
+  const Geo G(A.inst[inst]);
+  const T beta = (T)s.beta;
+  const bool first = (s.iter == 0);
+  const T* __restrict__ R = Vec<T>::r(A) + G.off;
+  T* __restrict__ P = Vec<T>::p(A) + G.off;
+#pragma unroll
+  for (int k = 0; k < kCellsPerThread; ++k) {
+    const int32_t l = tile_cell(tile, G, k);
+    if (l >= G.n) continue;
+    P[l] = first ? R[l] : fma(beta, P[l], R[l]);
+  }
+}
+
+// k_cg_spmv: q = Ah p, p.q
+template <typename T>
+__device__ __forceinline__ void cg_spmv_tile(const DevArrays& A, int64_t tile) {
+  const int inst = A.tile_inst[tile];
+  InstScal& s = A.scal[inst];
+  if (!s.inner_active) return;
+  const Geo G(A.inst[inst]);
+  const T* __restrict__ P = Vec<T>::p(A) + G.off;
+  T* __restrict__ Q = Vec<T>::q(A) + G.off;
+  const T* __restrict__ ax = Vec<T>::ax(A) + G.off;
+  const T* __restrict__ ay = Vec<T>::ay(A) + G.off;
+  const T* __restrict__ az = Vec<T>::az(A) + G.off;
+  T pq = 0;
+#pragma unroll
+  for (int k = 0; k < kCellsPerThread; ++k) {
+    const int32_t l = tile_cell(tile, G, k);
+    if (l >= G.n) continue;
+    const Coord c = coord3(G, l);
+    const T pc = P[l];
+    T acc = pc;
+    stencil(G, ax, ay, az, l, c, [&](int32_t m) { return P[m]; },
+            [&](T cf, T pv) { acc = fma(cf, pv, acc); });
+    Q[l] = acc;
+    pq = fma(pc, acc, pq);
+  }
+  if (sizeof(T) == 4) {
+    const float f[1] = {(float)pq};
+    tile_store_f<1>(A, tile, f);
+  } else {
+    const double v[1] = {(double)pq};
+    tile_store<1>(A, tile, v);
+  }
+}
+
+// k_cg_upd: y += alpha p, r -= alpha q, r.r (and the unscaled ||r||^2 for the reference rule)
+template <typename T>
+__device__ __forceinline__ void cg_upd_tile(const DevArrays& A, int64_t tile) {
+  const int inst = A.tile_inst[tile];
+  InstScal& s = A.scal[inst];
+  if (!s.inner_active) return;
+  const Geo G(A.inst[inst]);
   const DevOpts& o = A.opts;
-  int t = s.role[2]; s.role[2] = s.role[3]; s.role[3] = t;
+  const bool weighted = (o.criterion == HF_STOP_RECURSIVE);
+  const T alpha = (T)s.alpha;
+  const bool first = (s.iter == 0);
+  T* __restrict__ Y = Vec<T>::y(A) + G.off;
+  T* __restrict__ R = Vec<T>::r(A) + G.off;
+  const T* __restrict__ P = Vec<T>::p(A) + G.off;
+  const T* __restrict__ Q = Vec<T>::q(A) + G.off;
+  const double* __restrict__ diag = A.diag + G.off;
+  T rr = 0;
+  double rw = 0.0;
+#pragma unroll
+  for (int k = 0; k < kCellsPerThread; ++k) {
+    const int32_t l = tile_cell(tile, G, k);
+    if (l >= G.n) continue;
+    const T pv = P[l];
+    Y[l] = first ? alpha * pv : fma(alpha, pv, Y[l]);
+    const T rv = fma(-alpha, Q[l], R[l]);
+    R[l] = rv;
+    rr = fma(rv, rv, rr);
+    if (weighted) rw = fma(-diag[l] * (double)rv, (double)rv, rw);
+  }
+  if (sizeof(T) == 4 && !weighted) {
+    const float f[1] = {(float)rr};
+    tile_store_f<1>(A, tile, f);
+  } else {
+    const double v[2] = {(double)rr, rw};
+    tile_store<2>(A, tile, v);
+  }
+}
+
+// Grid-stride wrappers: a resident set of blocks walks all tiles (instance data stays in L1
+// between consecutive tiles of one instance instead of being refetched by 16K short blocks).
+template <bool INIT, typename TR>
+__global__ void __launch_bounds__(kBlock) k_residual(DevArrays A) {
+  for (int64_t t = blockIdx.x; t < A.ntiles; t += gridDim.x) residual_tile<INIT, TR>(A, t);
+}
+template <typename TY>
+__global__ void __launch_bounds__(kBlock) k_xupdate(DevArrays A) {
+  for (int64_t t = blockIdx.x; t < A.ntiles; t += gridDim.x) xupdate_tile<TY>(A, t);
+}
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_cg_p(DevArrays A) {
+  for (int64_t t = blockIdx.x; t < A.ntiles; t += gridDim.x) cg_p_tile<T>(A, t);
+}
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_cg_spmv(DevArrays A) {
+  for (int64_t t = blockIdx.x; t < A.ntiles; t += gridDim.x) cg_spmv_tile<T>(A, t);
+}
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_cg_upd(DevArrays A) {
+  for (int64_t t = blockIdx.x; t < A.ntiles; t += gridDim.x) cg_upd_tile<T>(A, t);
+}
+
+// ---- finalize kernels: one block per instance sums the tile partials in tile order ----------
+// (deterministic), then runs the scalar epilogue of the producing kernel.
+
+// Epilogue of the RHS kernel (mod_evolve.f90:70-127 checks, initial scale of the FP32 rhs).
+__device__ void epi_rhs(const DevArrays& A, int inst, const double* tot) {
+  InstScal& s = A.scal[inst];
+  const InstDesc& d = A.inst[inst];
+  s.bb = tot[0];
+  s.x0flag = tot[1] > 0.0 ? 1 : 0;
+  if (isnan(tot[0])) {              // some S is NaN: which vector failed is diagnosed later
+    s.status |= kStatusRhsNan;
+    s.outer_active = 0;
+    s.failed_step = s.itime;
+    return;
+  }
+  // scale of the first FP32 residual: a power of two near rms(S)/rms(|H_II|^(1/2)) * 1e-6
+  const double rms = sqrt(tot[0] / (double)d.n) * d.mean_sinv * 1e-6;
+  s.sigma = (A.opts.precision == HF_PREC_MIXED && rms > 0.0 && isfinite(rms))
+                ? exp2(rint(log2(rms))) : 1.0;
+}
+
+// Epilogue of the diagnosis pass: the first failing vector in the reference's order.
+__device__ void epi_rhs_diag(const DevArrays& A, int inst, const double* tot) {
+  InstScal& s = A.scal[inst];
+  int st = 0;
+  if (tot[1] > 0) st = 1 << (HF_ENAN_Q - HF_ENAN_B);
+  else if (tot[2] > 0) st = 1 << (HF_ENAN_QDENS - HF_ENAN_B);
+  else if (tot[3] > 0) st = 1 << (HF_ENAN_SCAT - HF_ENAN_B);
+  else if (tot[4] > 0) st = 1 << (HF_ENAN_S - HF_ENAN_B);
+  s.status = st ? st : (1 << (HF_ENAN_S - HF_ENAN_B));
+}
+
+// Epilogue of a residual sweep: convergence test and set-up of the next inner solve.
+template <bool INIT>
+__device__ void epi_residual(const DevArrays& A, int inst, const double* tot) {
+  InstScal& s = A.scal[inst];
+  const InstDesc& G = A.inst[inst];
+  const DevOpts& o = A.opts;
+  if (!INIT) {
+    const int t = s.role[2]; s.role[2] = s.role[3]; s.role[3] = t;
+    s.tiny_pending = 0;
+  } else {
+    s.tiny_pending = s.x0flag;
+  }
   s.rr_true = tot[0];
   s.relres = s.bb > 0.0 ? sqrt(tot[0] / s.bb) : (tot[0] > 0.0 ? INFINITY : 0.0);
   s.refine += 1;
   s.tot_refine += 1;
-  if (tot[2] > 0.0) {
+  if (isnan(tot[0])) {                   // x holds a NaN (mod_evolve.f90:153-158)
     s.status |= 1 << (HF_ENAN_X - HF_ENAN_B);
     s.failed_step = s.itime;
     s.outer_active = 0;
     return;
   }
-  bool done;
-  bool converged;
+  bool done, converged;
   if (o.criterion == HF_STOP_RECURSIVE) {
-    done = (s.refine >= 2);       // the reference solves once; this sweep only forms x
+    done = (s.refine >= 2);              // the reference solves once; this sweep only forms x
     converged = true;
   } else {
     converged = (s.relres <= o.tol);
-    done = converged || (s.refine > o.max_refine) || (tot[0] == 0.0);
+    done = (converged && !s.tiny_pending) || (s.refine > o.max_refine) ||
+           (tot[0] == 0.0 && !s.tiny_pending);
   }
   if (done) {
     s.outer_active = 0;
@@ -189,73 +420,30 @@ __global__ void __launch_bounds__(kBlock) k_residual(DevArrays A) {
     s.last_iter = s.step_iters;
     return;
   }
-  s.inner_active = 1;
   s.iter = 0;
+  if (o.criterion != HF_STOP_RECURSIVE && converged) {   // only the +TINY is left to apply
+    s.inner_active = 0;
+    return;
+  }
+  s.inner_active = 1;
   s.gg0 = tot[1];
   s.rho = tot[1];
   s.beta = 0.0;
-  s.sigma_prev = sig;
+  s.sigma_prev = s.sigma;
   if (o.precision == HF_PREC_MIXED) {
     s.eta = fmax(o.inner_tol, 0.1 * o.tol / fmax(s.relres, 1e-300));
-    double rms = sqrt(tot[0] / (double)d.n) * d.mean_sinv;
+    const double rms = sqrt(tot[0] / (double)G.n) * G.mean_sinv;
     s.sigma = (rms > 0.0 && isfinite(rms)) ? exp2(rint(log2(rms))) : 1.0;
   } else {
     s.eta = fmax(0.1 * o.tol / fmax(s.relres, 1e-300), 1e-15);
     s.sigma = 1.0;
   }
-  if (!(tot[1] > 0.0)) s.inner_active = 0;  // exact already: go straight to the update sweep
+  if (!(tot[1] > 0.0)) s.inner_active = 0;  // exact already: go straight to the update
 }
 
-// ---- inner CG on Ah (type T) -------------------------------------------------------------------
-// k_cg_p:    p = r + beta p  (beta = 0 on the first iteration)
-template <typename T>
-__global__ void __launch_bounds__(kBlock) k_cg_p(DevArrays A) {
-  const int64_t tile = blockIdx.x;
-  const int inst = A.tile_inst[tile];
-  const InstDesc& d = A.inst[inst];
-  const InstScal& s = A.scal[inst];
-  if (!s.inner_active) return;
-  const T beta = (T)s.beta;
-  const bool first = (s.iter == 0);
-  const T* R = Vec<T>::r(A) + d.off;
-  T* P = Vec<T>::p(A) + d.off;
-#pragma unroll
-  for (int k = 0; k < kCellsPerThread; ++k) {
-    const int64_t g = tile * kTile + k * kBlock + threadIdx.x;
-    const int64_t l = g - d.off;
-    if (l >= d.n) continue;
-    P[l] = first ? R[l] : fma(beta, P[l], R[l]);
-  }
-}
 
-// k_cg_spmv: q = Ah p, p.q
-template <typename T>
-__global__ void __launch_bounds__(kBlock) k_cg_spmv(DevArrays A) {
-  const int64_t tile = blockIdx.x;
-  const int inst = A.tile_inst[tile];
-  const InstDesc& d = A.inst[inst];
+__device__ void epi_spmv(const DevArrays& A, int inst, const double* tot) {
   InstScal& s = A.scal[inst];
-  if (!s.inner_active) return;
-  const T* P = Vec<T>::p(A) + d.off;
-  T* Q = Vec<T>::q(A) + d.off;
-  const T* ax = Vec<T>::ax(A);
-  const T* ay = Vec<T>::ay(A);
-  const T* az = Vec<T>::az(A);
-  auto pv = [&](int64_t n) -> T { return P[n]; };
-  double acc[1] = {0.0};
-#pragma unroll
-  for (int k = 0; k < kCellsPerThread; ++k) {
-    const int64_t g = tile * kTile + k * kBlock + threadIdx.x;
-    const int64_t l = g - d.off;
-    if (l >= d.n) continue;
-    const Coord c = coord_of(d, (int32_t)l);
-    const T qv = apply_Ah<T>(ax, ay, az, d, g, l, c, pv);
-    Q[l] = qv;
-    acc[0] += (double)(P[l] * qv);
-  }
-  double tot[1];
-  if (!tile_reduce<1>(A, inst, tile, acc, tot)) return;
-  if (threadIdx.x != 0) return;
   s.pq = tot[0];
   if (tot[0] > 0.0 && isfinite(tot[0])) {
     s.alpha = s.rho / tot[0];
@@ -265,38 +453,12 @@ __global__ void __launch_bounds__(kBlock) k_cg_spmv(DevArrays A) {
   }
 }
 
-// k_cg_upd: y += alpha p, r -= alpha q, r.r (and the unscaled ||r||^2 for the reference rule)
+
 template <typename T>
-__global__ void __launch_bounds__(kBlock) k_cg_upd(DevArrays A) {
-  const int64_t tile = blockIdx.x;
-  const int inst = A.tile_inst[tile];
-  const InstDesc& d = A.inst[inst];
+__device__ void epi_upd(const DevArrays& A, int inst, const double* tot) {
   InstScal& s = A.scal[inst];
-  if (!s.inner_active) return;
   const DevOpts& o = A.opts;
   const bool weighted = (o.criterion == HF_STOP_RECURSIVE);
-  const T alpha = (T)s.alpha;
-  const bool first = (s.iter == 0);
-  T* Y = Vec<T>::y(A) + d.off;
-  T* R = Vec<T>::r(A) + d.off;
-  const T* P = Vec<T>::p(A) + d.off;
-  const T* Q = Vec<T>::q(A) + d.off;
-  double acc[2] = {0.0, 0.0};
-#pragma unroll
-  for (int k = 0; k < kCellsPerThread; ++k) {
-    const int64_t g = tile * kTile + k * kBlock + threadIdx.x;
-    const int64_t l = g - d.off;
-    if (l >= d.n) continue;
-    const T pv = P[l];
-    Y[l] = first ? alpha * pv : fma(alpha, pv, Y[l]);
-    const T rv = fma(-alpha, Q[l], R[l]);
-    R[l] = rv;
-    acc[0] += (double)(rv * rv);
-    if (weighted) acc[1] += -A.diag[g] * (double)rv * (double)rv;
-  }
-  double tot[2];
-  if (!tile_reduce<2>(A, inst, tile, acc, tot)) return;
-  if (threadIdx.x != 0) return;
   const double rho_new = tot[0];
   s.beta = rho_new / s.rho;
   s.rho = rho_new;
@@ -322,6 +484,107 @@ __global__ void __launch_bounds__(kBlock) k_cg_upd(DevArrays A) {
   if (stop) s.inner_active = 0;
 }
 
+
+// Whether instance s took part in the producing kernel (the producers' own entry tests).
+template <int KIND>
+__device__ __forceinline__ bool took_part(const InstScal& s) {
+  switch (KIND) {
+    case FIN_RHS: return s.outer_active != 0;
+    case FIN_RHS_DIAG: return (s.status & kStatusRhsNan) != 0;
+    case FIN_RES_INIT: return s.outer_active && !s.inner_active && s.refine == 0;
+    case FIN_RES: return s.outer_active && !s.inner_active && s.refine != 0;
+    default: return s.inner_active != 0;      // FIN_SPMV, FIN_UPD
+  }
+}
+
+template <int KIND, bool FP32>
+__global__ void __launch_bounds__(256) k_finalize(DevArrays A, CtrlState* ctrl,
+                                                  cudaGraphConditionalHandle hw, int graph) {
+  constexpr int NR = (KIND == FIN_RHS_DIAG) ? 5 : (KIND == FIN_SPMV ? 1 : 2);
+  const int inst = blockIdx.x;
+  const InstDesc& d = A.inst[inst];
+  if (took_part<KIND>(A.scal[inst])) {
+    double acc[NR];
+#pragma unroll
+    for (int k = 0; k < NR; ++k) acc[k] = 0.0;
+    for (int64_t t = threadIdx.x; t < d.ntiles; t += blockDim.x) {
+#pragma unroll
+      for (int k = 0; k < NR; ++k) acc[k] += A.partials[(d.tile0 + t) * kNR + k];
+    }
+    __shared__ double red[32 * NR];
+    block_sum<NR>(acc, red);
+    if (threadIdx.x == 0) {
+      switch (KIND) {
+        case FIN_RHS: epi_rhs(A, inst, acc); break;
+        case FIN_RHS_DIAG: epi_rhs_diag(A, inst, acc); break;
+        case FIN_RES_INIT: epi_residual<true>(A, inst, acc); break;
+        case FIN_RES: epi_residual<false>(A, inst, acc); break;
+        case FIN_SPMV: epi_spmv(A, inst, acc); break;
+        default:
+          if (FP32) epi_upd<float>(A, inst, acc); else epi_upd<double>(A, inst, acc);
+          break;
+      }
+    }
+  }
+  // loop condition of the captured solve loop: set by the last instance block to finish
+  if (graph && (KIND == FIN_RES_INIT || KIND == FIN_RES || KIND == FIN_UPD)) {
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+      __threadfence();
+      const unsigned prev = atomicAdd(&ctrl->fin_count, 1u);
+      last = (prev == gridDim.x - 1u);
+    }
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+      __threadfence();
+      int any_outer = 0;
+      for (int64_t i = 0; i < A.ninst; ++i) any_outer |= __ldcg(&A.scal[i].outer_active);
+      ctrl->fin_count = 0u;
+      cudaGraphSetConditional(hw, any_outer ? 1u : 0u);
+    }
+  }
+}
+
+// ---- captured step: control kernels of the conditional nodes -----------------------------------
+__global__ void k_graph_step_begin(DevArrays A, CtrlState* ctrl) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) {
+    ctrl->loop_iter = 0;
+    ctrl->launches += 6;   // step begin, RHS + finalize, initial residual + finalize, step end
+  }
+  if (i < A.ninst) begin_step(A.scal[i], ctrl->itime);
+}
+
+// One block: every instance rotates, then the step counter advances.
+__global__ void k_graph_step_end(DevArrays A, CtrlState* ctrl) {
+  for (int64_t i = threadIdx.x; i < A.ninst; i += blockDim.x) end_step(A.scal[i]);
+  __syncthreads();
+  if (threadIdx.x == 0) ctrl->itime += 1;
+}
+
+// Branch of the solve loop body: 0 = one inner CG iteration, 1 = update + residual, 2 = nothing.
+// It also bounds the loop: past ctrl->limit body iterations (or with nothing to do) it clears the
+// loop condition, so the WHILE node always terminates.
+__global__ void k_ctrl_select(DevArrays A, CtrlState* ctrl, cudaGraphConditionalHandle hs,
+                              cudaGraphConditionalHandle hw) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int any_inner = 0, any_outer = 0;
+  for (int64_t i = 0; i < A.ninst; ++i) {
+    any_inner |= A.scal[i].inner_active;
+    any_outer |= A.scal[i].outer_active;
+  }
+  unsigned branch = any_inner ? 0u : (any_outer ? 1u : 2u);
+  const int64_t it = ctrl->loop_iter + 1;
+  ctrl->loop_iter = it;
+  if (it > ctrl->limit) {
+    ctrl->guard_hit = 1;
+    branch = 2u;
+  }
+  ctrl->launches += 1 + (branch == 0u ? 5 : (branch == 1u ? 3 : 0));
+  if (branch == 2u) cudaGraphSetConditional(hw, 0u);
+  cudaGraphSetConditional(hs, branch);
+}
+
 // ---- launchers ---------------------------------------------------------------------------------
 cudaError_t launch_step_begin(Ctx& c, int64_t itime, int) {
   k_step_begin<<<(unsigned)((c.ninst + 127) / 128), 128, 0, c.stream>>>(c.A, itime);
@@ -333,40 +596,90 @@ cudaError_t launch_step_end(Ctx& c) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_residual(Ctx& c, int mode) {
-  const unsigned nb = (unsigned)c.ntiles;
+// mode 0: initial residual (+ finalize); mode 1: solution update + residual (+ finalize)
+cudaError_t launch_residual(Ctx& c, int mode, CtrlState* ctrl, cudaGraphConditionalHandle hw,
+                            int graph) {
+  const unsigned nb = (unsigned)c.grid_tiles;
   const bool mixed = c.opts.precision == HF_PREC_MIXED;
-  if (mode == RES_INIT) {
-    if (mixed) k_residual<RES_INIT, float, float><<<nb, kBlock, 0, c.stream>>>(c.A);
-    else k_residual<RES_INIT, double, double><<<nb, kBlock, 0, c.stream>>>(c.A);
-  } else {
-    if (mixed) k_residual<RES_UPDATE, float, float><<<nb, kBlock, 0, c.stream>>>(c.A);
-    else k_residual<RES_UPDATE, double, double><<<nb, kBlock, 0, c.stream>>>(c.A);
+  if (mode == 0) {
+    if (mixed) k_residual<true, float><<<nb, kBlock, 0, c.stream>>>(c.A);
+    else k_residual<true, double><<<nb, kBlock, 0, c.stream>>>(c.A);
+    return launch_finalize(c, FIN_RES_INIT, ctrl, hw, graph);
   }
-  return cudaGetLastError();
+  if (mixed) {
+    k_xupdate<float><<<nb, kBlock, 0, c.stream>>>(c.A);
+    k_residual<false, float><<<nb, kBlock, 0, c.stream>>>(c.A);
+  } else {
+    k_xupdate<double><<<nb, kBlock, 0, c.stream>>>(c.A);
+    k_residual<false, double><<<nb, kBlock, 0, c.stream>>>(c.A);
+  }
+  return launch_finalize(c, FIN_RES, ctrl, hw, graph);
 }
 
-cudaError_t launch_inner_iteration(Ctx& c, int fp32) {
-  const unsigned nb = (unsigned)c.ntiles;
+cudaError_t launch_inner_iteration(Ctx& c, int fp32, CtrlState* ctrl,
+                                   cudaGraphConditionalHandle hw, int graph) {
+  const unsigned nb = (unsigned)c.grid_tiles;
   if (fp32) {
     k_cg_p<float><<<nb, kBlock, 0, c.stream>>>(c.A);
     k_cg_spmv<float><<<nb, kBlock, 0, c.stream>>>(c.A);
-    k_cg_upd<float><<<nb, kBlock, 0, c.stream>>>(c.A);
   } else {
     k_cg_p<double><<<nb, kBlock, 0, c.stream>>>(c.A);
     k_cg_spmv<double><<<nb, kBlock, 0, c.stream>>>(c.A);
-    k_cg_upd<double><<<nb, kBlock, 0, c.stream>>>(c.A);
+  }
+  cudaError_t e = launch_finalize(c, FIN_SPMV, ctrl, hw, graph);
+  if (e != cudaSuccess) return e;
+  if (fp32) k_cg_upd<float><<<nb, kBlock, 0, c.stream>>>(c.A);
+  else k_cg_upd<double><<<nb, kBlock, 0, c.stream>>>(c.A);
+  return launch_finalize(c, FIN_UPD, ctrl, hw, graph);
+}
+
+cudaError_t launch_graph_step_begin(Ctx& c, CtrlState* ctrl) {
+  k_graph_step_begin<<<(unsigned)((c.ninst + 127) / 128), 128, 0, c.stream>>>(c.A, ctrl);
+  return cudaGetLastError();
+}
+cudaError_t launch_graph_step_end(Ctx& c, CtrlState* ctrl) {
+  k_graph_step_end<<<1, 256, 0, c.stream>>>(c.A, ctrl);
+  return cudaGetLastError();
+}
+cudaError_t launch_ctrl_select(Ctx& c, CtrlState* ctrl, cudaGraphConditionalHandle hs,
+                               cudaGraphConditionalHandle hw) {
+  k_ctrl_select<<<1, 32, 0, c.stream>>>(c.A, ctrl, hs, hw);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(Ctx& c, int kind, CtrlState* ctrl, cudaGraphConditionalHandle hw,
+                            int graph) {
+  const unsigned nb = (unsigned)c.ninst;
+  const bool fp32 = c.opts.precision == HF_PREC_MIXED;
+  switch (kind) {
+    case FIN_RHS: k_finalize<FIN_RHS, false><<<nb, 256, 0, c.stream>>>(c.A, ctrl, hw, graph); break;
+    case FIN_RHS_DIAG: k_finalize<FIN_RHS_DIAG, false><<<nb, 256, 0, c.stream>>>(c.A, ctrl, hw, graph); break;
+    case FIN_RES_INIT: k_finalize<FIN_RES_INIT, false><<<nb, 256, 0, c.stream>>>(c.A, ctrl, hw, graph); break;
+    case FIN_RES: k_finalize<FIN_RES, false><<<nb, 256, 0, c.stream>>>(c.A, ctrl, hw, graph); break;
+    case FIN_SPMV: k_finalize<FIN_SPMV, false><<<nb, 256, 0, c.stream>>>(c.A, ctrl, hw, graph); break;
+    case FIN_UPD:
+      if (fp32) k_finalize<FIN_UPD, true><<<nb, 256, 0, c.stream>>>(c.A, ctrl, hw, graph);
+      else k_finalize<FIN_UPD, false><<<nb, 256, 0, c.stream>>>(c.A, ctrl, hw, graph);
+      break;
+    default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();
 }
 
 // One kernel of the step, for timing (hf_time_kernel).
 cudaError_t launch_single(Ctx& c, int which) {
-  const unsigned nb = (unsigned)c.ntiles;
+  const unsigned nb = (unsigned)c.grid_tiles;
   const bool fp32 = c.opts.precision == HF_PREC_MIXED;
   switch (which) {
     case HF_KERNEL_RHS: return launch_rhs(c);
-    case HF_KERNEL_RESIDUAL: return launch_residual(c, RES_UPDATE);
+    case HF_KERNEL_RESIDUAL:
+      if (fp32) k_residual<false, float><<<nb, kBlock, 0, c.stream>>>(c.A);
+      else k_residual<false, double><<<nb, kBlock, 0, c.stream>>>(c.A);
+      break;
+    case HF_KERNEL_XUPDATE:
+      if (fp32) k_xupdate<float><<<nb, kBlock, 0, c.stream>>>(c.A);
+      else k_xupdate<double><<<nb, kBlock, 0, c.stream>>>(c.A);
+      break;
     case HF_KERNEL_CG_P:
       if (fp32) k_cg_p<float><<<nb, kBlock, 0, c.stream>>>(c.A);
       else k_cg_p<double><<<nb, kBlock, 0, c.stream>>>(c.A);

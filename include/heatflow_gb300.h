@@ -184,12 +184,16 @@ enum {
   HF_KERNEL_RESIDUAL = 1,    /* FP64 solution update + true residual sweep */
   HF_KERNEL_CG_P = 2,        /* inner CG direction update (FP32 in mixed mode, else FP64) */
   HF_KERNEL_CG_SPMV = 3,     /* inner CG SpMV + p.Ap */
-  HF_KERNEL_CG_UPDATE = 4    /* inner CG solution/residual update + r.r */
+  HF_KERNEL_CG_UPDATE = 4,   /* inner CG solution/residual update + r.r */
+  HF_KERNEL_XUPDATE = 5      /* FP64 solution update x += S^-1 y */
 };
 /* Launch one kernel `reps` times on the current state, each bracketed by CUDA events on the
  * context's stream, and return its mean duration in milliseconds.  Solver scalars are restored
  * afterwards; the temperature state is not modified.  Call after at least one step. */
 int hf_time_kernel(hf_ctx* ctx, int kernel, int reps, double* ms_per_launch);
+/* FP64 and FP32 FMA throughput of the current device in TFLOP/s (independent FMA chains over
+ * every SM, CUDA-event timed).  On GB300 the FP64 rate bounds the FP64 kernels of a step. */
+int hf_measure_fp_rates(double* fp64_tflops, double* fp32_tflops);
 
 #ifdef __cplusplus
 }

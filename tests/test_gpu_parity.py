@@ -242,3 +242,37 @@ def test_full_size_residual_property(cuda_lib, precision):
     assert rel <= 1e-10, rel
     assert st["last_true_relres"] <= 1e-10
     assert np.isfinite(T).all() and T.max() > 300.0
+
+
+@pytest.mark.parametrize("opts", [
+    dict(precision="fp64", criterion="recursive", tol=1e-32),
+    dict(precision="fp64", criterion="true", tol=1e-10),
+    dict(precision="mixed", criterion="true", tol=1e-10),
+])
+def test_graph_equals_host_loop(cuda_lib, opts):
+    """The captured step (CUDA graph, conditional WHILE/SWITCH nodes, no host round trips)
+    runs the same kernels as the host-driven loop: identical fields and iteration counts."""
+    rng = np.random.default_rng(11)
+    probs = [point_source_cube(10)] + [random_instance(rng, lo=6, hi=14) for _ in range(3)]
+    out = []
+    for g in (0, 1):
+        with HeatFlow(probs, use_graph=g, **opts) as hf:
+            hf.initial_evolve()
+            st = hf.run(1, 8)
+            out.append((hf.get_state(), st))
+    (a, sa), (b, sb) = out
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    for k in ("iterations", "inner_iterations", "refinements", "unconverged"):
+        assert sa[k] == sb[k], k
+    assert sb["kernel_launches"] > 0
+
+
+def test_graph_nan_stops(cuda_lib):
+    prob = point_source_cube(4, icattaneo=0)
+    tp, tpp = prob.initial_state()
+    tp[3] = np.nan
+    with HeatFlow(prob, use_graph=1) as hf:
+        hf.set_state(tp, tpp)
+        with pytest.raises(abi.HeatFlowError) as e:
+            hf.run(1, 3)
+        assert e.value.code == abi.HF_ENAN_S
