@@ -459,11 +459,19 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
   }
   c.ncells = off;
   c.ntiles = tiles;
-  {
-    int sms = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c.device);
-    c.grid_tiles = std::min<int64_t>(tiles, (int64_t)std::max(sms, 1) * 6);
+  // tasks of the step kernels: kTX x kTY columns x kZC planes, ordered (z, y, x) per instance
+  std::vector<int4> tasks;
+  for (int64_t i = 0; i < count; ++i) {
+    InstDesc& d = c.h_inst[i];
+    const int nbx = (d.nx + kTX - 1) / kTX, nby = (d.ny + kTY - 1) / kTY, nbz = (d.nz + kZC - 1) / kZC;
+    d.task0 = (int64_t)tasks.size();
+    d.ntask = nbx * nby * nbz;
+    for (int bz = 0; bz < nbz; ++bz)
+      for (int by = 0; by < nby; ++by)
+        for (int bx = 0; bx < nbx; ++bx)
+          tasks.push_back(make_int4((int)i, bx * kTX, by * kTY, bz * kZC));
   }
+  c.ntasks = (int64_t)tasks.size();
   const size_t N = (size_t)c.ncells;
   // ---- device memory
   DevArrays& A = c.A;
@@ -475,10 +483,14 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
   ALLOC(d_inst, (size_t)count);
   ALLOC(d_scal, (size_t)count);
   ALLOC(d_tile_inst, (size_t)tiles);
-  int8_t* d_tile_heat;
-  ALLOC(d_tile_heat, (size_t)tiles);
-  A.tile_heat = d_tile_heat;
-  ALLOC(A.partials, (size_t)tiles * kNR);
+  int8_t* d_task_heat;
+  int4* d_tasks;
+  ALLOC(d_task_heat, (size_t)c.ntasks);
+  ALLOC(d_tasks, (size_t)c.ntasks);
+  A.task_heat = d_task_heat;
+  A.tasks = d_tasks;
+  A.ntasks = c.ntasks;
+  ALLOC(A.partials, (size_t)c.ntasks * kNR);
   ALLOC(A.counters, (size_t)count);
   ALLOC(c.d_bc, (size_t)count);
   A.inst = d_inst; A.scal = d_scal; A.tile_inst = d_tile_inst;
@@ -520,15 +532,20 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
   CK(cudaMemcpyAsync(d_inst, c.h_inst.data(), sizeof(InstDesc) * count, cudaMemcpyHostToDevice, c.stream));
   CK(cudaMemcpyAsync(c.d_bc, c.h_bc.data(), sizeof(InstBC) * count, cudaMemcpyHostToDevice, c.stream));
   CK(cudaMemcpyAsync(d_tile_inst, tile_inst.data(), sizeof(int32_t) * tiles, cudaMemcpyHostToDevice, c.stream));
-  {   // tiles holding a heated cell (the RHS skips heater loads elsewhere)
-    std::vector<int8_t> th((size_t)tiles, 0);
+  CK(cudaMemcpy(d_tasks, tasks.data(), sizeof(int4) * (size_t)c.ntasks, cudaMemcpyHostToDevice));
+  {   // tasks holding a heated cell (the RHS skips heater loads elsewhere)
+    std::vector<int8_t> th((size_t)c.ntasks, 0);
     for (int64_t i = 0; i < count; ++i) {
       const InstDesc& d = c.h_inst[i];
       if (!probs[i].iheater) continue;
-      for (int64_t k = 0; k < d.n; ++k)
-        if (probs[i].iheater[k] != 0) th[(size_t)(d.tile0 + k / kTile)] = 1;
+      const int nbx = (d.nx + kTX - 1) / kTX, nby = (d.ny + kTY - 1) / kTY;
+      for (int64_t k = 0; k < d.n; ++k) {
+        if (probs[i].iheater[k] == 0) continue;
+        const int64_t ix = k % d.nx, iy = (k / d.nx) % d.ny, iz = k / ((int64_t)d.nx * d.ny);
+        th[(size_t)(d.task0 + ((iz / kZC) * nby + iy / kTY) * nbx + ix / kTX)] = 1;
+      }
     }
-    CK(cudaMemcpy(d_tile_heat, th.data(), (size_t)tiles, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d_task_heat, th.data(), (size_t)c.ntasks, cudaMemcpyHostToDevice));
   }
   // per-cell inputs into the padded layout
   std::vector<int8_t> icase;

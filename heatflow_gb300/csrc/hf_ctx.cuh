@@ -24,7 +24,7 @@ struct Ctx {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   int64_t ninst = 0, ncells = 0, ntiles = 0;
-  int64_t grid_tiles = 0;        // blocks of the tile kernels (resident set, grid-stride)
+  int64_t ntasks = 0;            // blocks of the step kernels
   std::vector<InstDesc> h_inst;
   std::vector<InstBC> h_bc;
   std::vector<int64_t> h_tile0;

@@ -30,6 +30,9 @@ constexpr int kBlock = 256;                  // threads per block of the cell ke
 constexpr int kCellsPerThread = 4;
 constexpr int kTile = kBlock * kCellsPerThread;   // cells per tile (one block per tile)
 constexpr int kNR = 8;
+// Step kernels work on tasks: a block of kTX x kTY threads owns kTX x kTY columns of one
+// instance (x fastest, one warp per row) and marches kZC planes along z.
+constexpr int kTX = 32, kTY = 8, kZC = 16;
 // InstScal::status bit: some S was NaN; the failing vector is found by the diagnosis kernel.
 constexpr int kStatusRhsNan = 1 << 16;                       // reduction slots per tile
 // Instances are laid out at multiples of kTile cells, so tile t covers cells
@@ -51,6 +54,9 @@ struct InstDesc {
   double inv_dt, time_step, freq, power_in, time_pulse, t_bath, heated_volume, volume;
   double len[3];
   double mean_sinv;   // mean of 1/sqrt|H_II| (scaling of the FP32 inner right-hand side)
+  int64_t task0;      // first task of the step kernels
+  int32_t ntask;      // tasks of this instance
+  int32_t pad1;
 };
 
 // Per-instance mutable scalars (device memory).
@@ -128,8 +134,9 @@ struct DevArrays {
   // solver
   double *b, *y, *r, *p, *q;
   float *y32, *r32, *p32, *q32;
-  const int8_t* tile_heat;  // per tile: some cell needs the heater/radiation terms
-  int64_t ncells, ntiles, ninst;
+  const int8_t* task_heat;  // per task: some cell holds a heater
+  const int4* tasks;        // (instance, x0, y0, z0) per task
+  int64_t ncells, ntiles, ninst, ntasks;
 };
 
 // ---- helpers ---------------------------------------------------------------------------------
@@ -218,6 +225,7 @@ __device__ __forceinline__ void block_sum(double (&v)[NRV], double* smem /* [32*
 // all eight warps would cost more than the kernel's own arithmetic.
 template <int NRV>
 __device__ __forceinline__ void tile_store(const DevArrays& A, int64_t tile, const double (&v)[NRV]) {
+  static_assert(NRV <= kNR, "reduction slots");
   __shared__ double stage[NRV][kBlock];
   __syncthreads();   // the previous tile of this block has finished reading the stage
 #pragma unroll
@@ -259,6 +267,34 @@ __device__ __forceinline__ void tile_store_f(const DevArrays& A, int64_t tile, c
       if (lane == 0) A.partials[tile * kNR + k] = (double)t;
     }
   }
+}
+
+// The column of a task that this thread owns.
+struct TCell {
+  int inst;
+  int64_t off;
+  int nx, ny, nz, nxy;
+  bool px, py, pz;
+  int x, y, z0, z1, lane;
+  bool act;          // the column lies inside the grid
+  int base;          // local index of (x, y, 0)
+};
+__device__ __forceinline__ TCell task_cell(const DevArrays& A, int64_t task) {
+  const int4 t = A.tasks[task];
+  const InstDesc& d = A.inst[t.x];
+  TCell c;
+  c.inst = t.x;
+  c.off = d.off;
+  c.nx = d.nx; c.ny = d.ny; c.nz = d.nz; c.nxy = d.nx * d.ny;
+  c.px = d.px; c.py = d.py; c.pz = d.pz;
+  c.lane = threadIdx.x & 31;
+  c.x = t.y + c.lane;
+  c.y = t.z + (int)(threadIdx.x >> 5);
+  c.z0 = t.w;
+  c.z1 = min(t.w + kZC, d.nz);
+  c.act = c.x < d.nx && c.y < d.ny;
+  c.base = c.y * d.nx + c.x;
+  return c;
 }
 
 // Coordinates of local cell l in an instance.

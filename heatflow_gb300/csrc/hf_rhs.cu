@@ -38,23 +38,23 @@ __device__ __forceinline__ double heat_case(int cs, double P, double tau, int64_
   }
 }
 
-// One block per tile.  PARTS: also write B, Q, Qdens and S_cat (parity probe hf_get_rhs).
+// One block per task.  PARTS: also write B, Q, Qdens and S_cat (parity probe hf_get_rhs).
 // DIAG: count NaNs per vector (failure path only).
 template <bool PARTS, bool DIAG>
-__device__ __forceinline__ void rhs_tile(const DevArrays& A, int64_t tile, double* oB, double* oQ,
-                                         double* oQd, double* oSc) {
-  const int inst = A.tile_inst[tile];
-  const InstDesc& d = A.inst[inst];
-  InstScal& s = A.scal[inst];
+__global__ void __launch_bounds__(kBlock) k_rhs(DevArrays A, double* oB, double* oQ, double* oQd,
+                                                double* oSc) {
+  const int64_t task = blockIdx.x;
+  const TCell c = task_cell(A, task);
+  const InstDesc& d = A.inst[c.inst];
+  InstScal& s = A.scal[c.inst];
   if (!DIAG && !s.outer_active) return;
   if (DIAG && !(s.status & kStatusRhsNan)) return;
   const int64_t itime = DIAG ? s.failed_step : s.itime;
-  const int64_t off = d.off;
-  const int32_t n = d.n;
+  const int64_t off = c.off;
   // heater() runs for every cell when any exists (mod_evolve.f90:79); with emissivity every cell
-  // has a radiative term, otherwise only tiles holding a heated cell have nonzero Q
-  const bool heater = d.heater && (d.has_em || A.tile_heat[tile]), has_power = d.has_power,
-             has_em = d.has_em, case5 = d.has_case5;
+  // has a radiative term, otherwise only tasks holding a heated cell have nonzero Q
+  const bool heater = d.heater && (d.has_em || A.task_heat[task]);
+  const bool has_power = d.has_power, has_em = d.has_em, case5 = d.has_case5;
   const bool cat = d.icattaneo == 1, steady = d.isteady != 0;
   const int qmode = d.qdens_mode;
   const double inv_dt = d.inv_dt, vol = d.volume, hvol = d.heated_volume, power_in = d.power_in;
@@ -70,53 +70,54 @@ __device__ __forceinline__ void rhs_tile(const DevArrays& A, int64_t tile, doubl
   double bb = 0.0;
   int flag = 0;
   int nan_q = 0, nan_qd = 0, nan_sc = 0, nan_s = 0;
-#pragma unroll
-  for (int k = 0; k < kCellsPerThread; ++k) {
-    const int32_t l = (int32_t)(tile * kTile - off) + k * kBlock + threadIdx.x;
-    if (l >= n) continue;
-    const double tp = Tp[l], tpp = Tpp[l];
-    double q = 0.0, qd = 0.0;
-    if (heater) {
-      const int cs = A.icase[off + l];
-      if (cs > 0 && cs < 7) {
-        const double P = has_power ? A.power[off + l] : power_in;
-        const double tau = case5 ? A.tau_s[off + l] * dt2 : 0.0;
-        q = heat_case(cs, P, tau, itime, d);
+  if (c.act) {
+#pragma unroll 4
+    for (int z = c.z0; z < c.z1; ++z) {
+      const int l = c.base + z * c.nxy;
+      const double tp = Tp[l], tpp = Tpp[l];
+      double q = 0.0, qd = 0.0;
+      if (heater) {
+        const int cs = A.icase[off + l];
+        if (cs > 0 && cs < 7) {
+          const double P = has_power ? A.power[off + l] : power_in;
+          const double tau = case5 ? A.tau_s[off + l] * dt2 : 0.0;
+          q = heat_case(cs, P, tau, itime, d);
+        }
+        if (has_em) q = q - A.emc[off + l] * (pow(tp, 4.0) - tb4);
+        if (!dbl_is_zero(q)) {
+          if (qmode == HF_QDENS_CELL_VOLUME) qd = q / vol;
+          else if (hvol > 0.0) qd = q / hvol;
+        }
+        if (DIAG) { nan_q += dbl_is_nan(q); nan_qd += dbl_is_nan(qd); }
       }
-      if (has_em) q = q - A.emc[off + l] * (pow(tp, 4.0) - tb4);
-      if (!dbl_is_zero(q)) {
-        if (qmode == HF_QDENS_CELL_VOLUME) qd = q / vol;
-        else if (hvol > 0.0) qd = q / hvol;
+      double sc = 0.0;
+      if (cat) {
+        sc = fma(-2.0, tp, tpp) * ccat[l];   // = (tpp - 2 tp) * ccat: 2 tp is exact
+        if (DIAG) nan_sc += dbl_is_nan(sc);
       }
-      if (DIAG) { nan_q += dbl_is_nan(q); nan_qd += dbl_is_nan(qd); }
-    }
-    double sc = 0.0;
-    if (cat) {
-      sc = fma(-2.0, tp, tpp) * ccat[l];   // = (tpp - 2 tp) * ccat: 2 tp is exact
-      if (DIAG) nan_sc += dbl_is_nan(sc);
-    }
-    const double B = bvec[l];
-    double S;
-    if (!steady) {
-      S = -inv_dt * tp * rhoc[l];
-      if (!dbl_is_zero(qd)) S = S - qd;
-      if (!dbl_is_zero(B)) S = S - B;
-      if (cat) S = S + sc;
-    } else {
-      S = -qd;
-      if (!dbl_is_zero(B)) S = S - B;
-    }
-    if (DIAG) nan_s += dbl_is_nan(S);
-    const double x0 = tp + (tp - tpp);
-    flag |= dbl_lt_pos(x0 - tp, kTiny) ? 1 : 0;
-    bout[l] = S;
-    X[l] = x0;
-    bb = fma(S, S, bb);
-    if (PARTS) {
-      oB[off + l] = B;
-      oQ[off + l] = q;
-      oQd[off + l] = qd;
-      oSc[off + l] = sc;
+      const double B = bvec[l];
+      double S;
+      if (!steady) {
+        S = -inv_dt * tp * rhoc[l];
+        if (!dbl_is_zero(qd)) S = S - qd;
+        if (!dbl_is_zero(B)) S = S - B;
+        if (cat) S = S + sc;
+      } else {
+        S = -qd;
+        if (!dbl_is_zero(B)) S = S - B;
+      }
+      if (DIAG) nan_s += dbl_is_nan(S);
+      const double x0 = tp + (tp - tpp);
+      flag |= dbl_lt_pos(x0 - tp, kTiny) ? 1 : 0;
+      bout[l] = S;
+      X[l] = x0;
+      bb = fma(S, S, bb);
+      if (PARTS) {
+        oB[off + l] = B;
+        oQ[off + l] = q;
+        oQd[off + l] = qd;
+        oSc[off + l] = sc;
+      }
     }
   }
   const int any_flag = __syncthreads_or(flag);
@@ -124,37 +125,30 @@ __device__ __forceinline__ void rhs_tile(const DevArrays& A, int64_t tile, doubl
     const int c1 = __syncthreads_count(nan_q), c2 = __syncthreads_count(nan_qd);
     const int c3 = __syncthreads_count(nan_sc), c4 = __syncthreads_count(nan_s);
     if (threadIdx.x == 0) {
-      A.partials[tile * kNR + 1] = (double)c1;
-      A.partials[tile * kNR + 2] = (double)c2;
-      A.partials[tile * kNR + 3] = (double)c3;
-      A.partials[tile * kNR + 4] = (double)c4;
+      A.partials[task * kNR + 1] = (double)c1;
+      A.partials[task * kNR + 2] = (double)c2;
+      A.partials[task * kNR + 3] = (double)c3;
+      A.partials[task * kNR + 4] = (double)c4;
     }
   } else if (threadIdx.x == 0) {
-    A.partials[tile * kNR + 1] = any_flag ? 1.0 : 0.0;
+    A.partials[task * kNR + 1] = any_flag ? 1.0 : 0.0;
   }
   const double v[1] = {bb};
-  tile_store<1>(A, tile, v);
-}
-
-template <bool PARTS, bool DIAG>
-__global__ void __launch_bounds__(kBlock) k_rhs(DevArrays A, double* oB, double* oQ, double* oQd,
-                                                double* oSc) {
-  for (int64_t tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x)
-    rhs_tile<PARTS, DIAG>(A, tile, oB, oQ, oQd, oSc);
+  tile_store<1>(A, task, v);
 }
 
 cudaError_t launch_rhs(Ctx& c) {
-  k_rhs<false, false><<<(unsigned)c.grid_tiles, kBlock, 0, c.stream>>>(c.A, nullptr, nullptr, nullptr, nullptr);
+  k_rhs<false, false><<<(unsigned)c.ntasks, kBlock, 0, c.stream>>>(c.A, nullptr, nullptr, nullptr, nullptr);
   return cudaGetLastError();
 }
 
 cudaError_t launch_rhs_parts(Ctx& c, double* B, double* Q, double* Qd, double* Sc) {
-  k_rhs<true, false><<<(unsigned)c.grid_tiles, kBlock, 0, c.stream>>>(c.A, B, Q, Qd, Sc);
+  k_rhs<true, false><<<(unsigned)c.ntasks, kBlock, 0, c.stream>>>(c.A, B, Q, Qd, Sc);
   return cudaGetLastError();
 }
 
 cudaError_t launch_rhs_diagnose(Ctx& c) {
-  k_rhs<false, true><<<(unsigned)c.grid_tiles, kBlock, 0, c.stream>>>(c.A, nullptr, nullptr, nullptr, nullptr);
+  k_rhs<false, true><<<(unsigned)c.ntasks, kBlock, 0, c.stream>>>(c.A, nullptr, nullptr, nullptr, nullptr);
   return cudaGetLastError();
 }
 

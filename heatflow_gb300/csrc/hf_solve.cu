@@ -27,53 +27,6 @@
 
 namespace hf {
 
-// Register copy of the geometry of one instance.
-struct Geo {
-  int64_t off;
-  int32_t n, nx, ny, nz;
-  bool px, py, pz;
-  __device__ explicit Geo(const InstDesc& d)
-      : off(d.off), n(d.n), nx(d.nx), ny(d.ny), nz(d.nz), px(d.px), py(d.py), pz(d.pz) {}
-};
-
-// Folds the six face terms of cell l: fold(c_face, v(neighbour)).  c_a[I] is the face to the +
-// neighbour stored at the cell; the - face is stored at the neighbour; periodic axes wrap.
-template <typename C, class V, class F>
-__device__ __forceinline__ void stencil(const Geo& G, const C* __restrict__ cx,
-                                        const C* __restrict__ cy, const C* __restrict__ cz,
-                                        int32_t l, const Coord& c, V v, F fold) {
-  const int32_t nx = G.nx, nxy = G.nx * G.ny;
-  if (c.x + 1 < G.nx) fold(cx[l], v(l + 1));
-  else if (G.px && G.nx > 1) fold(cx[l], v(l - (nx - 1)));
-  if (c.x > 0) fold(cx[l - 1], v(l - 1));
-  else if (G.px && G.nx > 1) fold(cx[l + nx - 1], v(l + nx - 1));
-  if (c.y + 1 < G.ny) fold(cy[l], v(l + nx));
-  else if (G.py && G.ny > 1) fold(cy[l], v(l - (G.ny - 1) * nx));
-  if (c.y > 0) fold(cy[l - nx], v(l - nx));
-  else if (G.py && G.ny > 1) fold(cy[l + (G.ny - 1) * nx], v(l + (G.ny - 1) * nx));
-  if (c.z + 1 < G.nz) fold(cz[l], v(l + nxy));
-  else if (G.pz && G.nz > 1) fold(cz[l], v(l - (G.nz - 1) * nxy));
-  if (c.z > 0) fold(cz[l - nxy], v(l - nxy));
-  else if (G.pz && G.nz > 1) fold(cz[l + (G.nz - 1) * nxy], v(l + (G.nz - 1) * nxy));
-}
-
-__device__ __forceinline__ Coord coord3(const Geo& G, int32_t l) {
-  Coord c;
-  const uint32_t ul = (uint32_t)l;
-  const uint32_t row = ul / (uint32_t)G.nx;
-  c.x = (int32_t)(ul - row * (uint32_t)G.nx);
-  const uint32_t pl = row / (uint32_t)G.ny;
-  c.y = (int32_t)(row - pl * (uint32_t)G.ny);
-  c.z = (int32_t)pl;
-  return c;
-}
-
-__device__ __forceinline__ float warp_sumf(float v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
 template <typename T> struct Vec;
 template <> struct Vec<double> {
   __device__ static double* y(const DevArrays& A) { return A.y; }
@@ -93,11 +46,6 @@ template <> struct Vec<float> {
   __device__ static const float* ay(const DevArrays& A) { return A.a32y; }
   __device__ static const float* az(const DevArrays& A) { return A.a32z; }
 };
-
-// Local cell index of the k-th cell of this thread in the block's tile.
-__device__ __forceinline__ int32_t tile_cell(int64_t tile, const Geo& G, int k) {
-  return (int32_t)(tile * kTile - G.off) + k * kBlock + (int32_t)threadIdx.x;
-}
 
 // ---- step bookkeeping ------------------------------------------------------------------------
 __device__ __forceinline__ void begin_step(InstScal& s, int64_t itime) {
@@ -132,98 +80,174 @@ __global__ void k_step_end(DevArrays A) {
   if (i < A.ninst) end_step(A.scal[i]);
 }
 
+// ---- neighbour access for a task column ----------------------------------------------------
+// Values of the x +/- neighbours come from the lanes of the same warp (a warp owns one row
+// segment); lanes at a task edge, periodic wraps and the y neighbours are loaded; the z
+// neighbours roll through registers as the block marches along z.
+template <typename T>
+__device__ __forceinline__ T shfl_up1(T v) { return __shfl_up_sync(0xffffffffu, v, 1); }
+template <typename T>
+__device__ __forceinline__ T shfl_dn1(T v) { return __shfl_down_sync(0xffffffffu, v, 1); }
+
+// Sum over the six faces of cell l: fold(coef, neighbour value).  v[] is the field, c{x,y,z}
+// the face arrays; vc/cxc are this cell's value and x-face (for the shuffles); vm/czm the value
+// and z-face of plane z-1, vn the value of plane z+1 (registers).
+template <typename T, typename C, class F>
+__device__ __forceinline__ void faces(const TCell& c, const T* __restrict__ v, const C* __restrict__ cx,
+                                      const C* __restrict__ cy, int l, T vc, C cxc, C cyc, C czc,
+                                      T vm, C czm, T vn, F fold) {
+  // x (all lanes shuffle; inactive lanes hold zeros)
+  T vw = shfl_up1(vc);
+  C cxw = shfl_up1(cxc);
+  T ve = shfl_dn1(vc);
+  if (!c.act) return;
+  const int nx = c.nx;
+  if (c.lane == 0) {
+    if (c.x > 0) { vw = v[l - 1]; cxw = cx[l - 1]; }
+    else if (c.px && nx > 1) { vw = v[l + nx - 1]; cxw = cx[l + nx - 1]; }
+    else { vw = T(0); cxw = C(0); }
+  }
+  if (c.x + 1 < nx) { if (c.lane == 31) ve = v[l + 1]; }
+  else if (c.px && nx > 1) ve = v[l - (nx - 1)];
+  else ve = T(0);
+  fold(cxc, ve);
+  fold(cxw, vw);
+  // y
+  if (c.ny > 1) {
+    if (c.y + 1 < c.ny) fold(cyc, v[l + nx]);
+    else if (c.py) fold(cyc, v[l - (c.ny - 1) * nx]);
+    if (c.y > 0) fold(cy[l - nx], v[l - nx]);
+    else if (c.py) fold(cy[l + (c.ny - 1) * nx], v[l + (c.ny - 1) * nx]);
+  }
+  // z
+  if (c.nz > 1) {
+    fold(czc, vn);
+    fold(czm, vm);
+  }
+}
+
+// Value and z-face of plane z-1 for the first plane of a task.
+template <typename T, typename C>
+__device__ __forceinline__ void plane_below(const TCell& c, const T* __restrict__ v,
+                                            const C* __restrict__ cz, T& vm, C& czm) {
+  vm = T(0);
+  czm = C(0);
+  if (!c.act || c.nz < 2) return;
+  if (c.z0 > 0) {
+    const int l = c.base + (c.z0 - 1) * c.nxy;
+    vm = v[l]; czm = cz[l];
+  } else if (c.pz) {
+    const int l = c.base + (c.nz - 1) * c.nxy;
+    vm = v[l]; czm = cz[l];
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ T plane_above(const TCell& c, const T* __restrict__ v, int z) {
+  if (!c.act || c.nz < 2) return T(0);
+  if (z + 1 < c.nz) return v[c.base + (z + 1) * c.nxy];
+  if (c.pz) return v[c.base];
+  return T(0);
+}
+
 // ---- FP64 true residual ------------------------------------------------------------------------
 // r = S - H x with x in the x-read buffer (INIT: x0 from the RHS kernel) or, after an update, in
-// the x-write buffer (then the roles swap).  Writes g = -S^-1 r / sigma into the inner residual
-// (type TR).  FP64 work per cell: 7 FMA for S - Hx and 1 FMA for ||r||^2.
+// the x-write buffer (the finalize then swaps the roles).  Writes g = -S^-1 r / sigma into the
+// inner residual (type TR).  FP64 work per cell: 7 FMA for S - Hx, 1 FMA for ||r||^2.
 template <bool INIT, typename TR>
-__device__ __forceinline__ void residual_tile(const DevArrays& A, int64_t tile) {
-  const int inst = A.tile_inst[tile];
-  InstScal& s = A.scal[inst];
+__global__ void __launch_bounds__(kBlock) k_residual(DevArrays A) {
+  const int64_t task = blockIdx.x;
+  const TCell c = task_cell(A, task);
+  const InstScal& s = A.scal[c.inst];
   if (!s.outer_active || s.inner_active) return;
   if (INIT != (s.refine == 0)) return;
-  const Geo G(A.inst[inst]);
-  const double* __restrict__ X = A.tbuf[INIT ? s.role[2] : s.role[3]] + G.off;
-  const double* __restrict__ diag = A.diag + G.off;
-  const double* __restrict__ b = A.b + G.off;
-  const double* __restrict__ cx = A.cx + G.off;
-  const double* __restrict__ cy = A.cy + G.off;
-  const double* __restrict__ cz = A.cz + G.off;
-  const float* __restrict__ sinv32 = A.sinv32 + G.off;
-  const double* __restrict__ sinv = A.sinv + G.off;
-  TR* __restrict__ R = Vec<TR>::r(A) + G.off;
+  const int64_t off = c.off;
+  const double* __restrict__ X = A.tbuf[INIT ? s.role[2] : s.role[3]] + off;
+  const double* __restrict__ diag = A.diag + off;
+  const double* __restrict__ b = A.b + off;
+  const double* __restrict__ cx = A.cx + off;
+  const double* __restrict__ cy = A.cy + off;
+  const double* __restrict__ cz = A.cz + off;
+  const double* __restrict__ rsum = A.rsum + off;
+  const float* __restrict__ sinv32 = A.sinv32 + off;
+  const double* __restrict__ sinv = A.sinv + off;
+  TR* __restrict__ R = Vec<TR>::r(A) + off;
   const float isig = (float)(1.0 / s.sigma);
-  double gg64 = 0.0;
   // INIT: the residual of x0 + TINY (mod_evolve.f90:141) is r(x0) - TINY * H1
   const bool tiny = INIT && s.x0flag;
-  const double* __restrict__ rsum = A.rsum + G.off;
-  double rr = 0.0;
+  double xm, czm;
+  plane_below(c, X, cz, xm, czm);
+  double xc = c.act ? X[c.base + c.z0 * c.nxy] : 0.0;
+  double rr = 0.0, gg64 = 0.0;
   float gg = 0.f;
-#pragma unroll
-  for (int k = 0; k < kCellsPerThread; ++k) {
-    const int32_t l = tile_cell(tile, G, k);
-    if (l >= G.n) continue;
-    const Coord c = coord3(G, l);
-    double acc = fma(-diag[l], X[l], b[l]);
-    if (tiny) acc = fma(-kTiny, rsum[l], acc);
-    stencil(G, cx, cy, cz, l, c, [&](int32_t m) { return X[m]; },
-            [&](double cf, double xv) { acc = fma(-cf, xv, acc); });
-    rr = fma(acc, acc, rr);
-    if (sizeof(TR) == 4) {               // mixed: g in FP32, scaled by 1/sigma
-      const float g = -sinv32[l] * f64_to_f32_trunc(acc) * isig;
-      R[l] = (TR)g;
-      gg = fmaf(g, g, gg);
-    } else {                             // FP64 path: sigma = 1
-      const double g = -sinv[l] * acc;
-      R[l] = (TR)g;
-      gg64 = fma(g, g, gg64);
+  for (int z = c.z0; z < c.z1; ++z) {
+    const int l = c.base + z * c.nxy;
+    const double xn = plane_above(c, X, z);
+    const double cxc = c.act ? cx[l] : 0.0, cyc = c.act ? cy[l] : 0.0, czc = c.act ? cz[l] : 0.0;
+    double acc = 0.0;
+    if (c.act) {
+      acc = fma(-diag[l], xc, b[l]);
+      if (tiny) acc = fma(-kTiny, rsum[l], acc);
     }
+    faces(c, X, cx, cy, l, xc, cxc, cyc, czc, xm, czm, xn,
+          [&](double cf, double xv) { acc = fma(-cf, xv, acc); });
+    if (c.act) {
+      rr = fma(acc, acc, rr);
+      if (sizeof(TR) == 4) {             // mixed: g in FP32, scaled by 1/sigma
+        const float g = -sinv32[l] * f64_to_f32_trunc(acc) * isig;
+        R[l] = (TR)g;
+        gg = fmaf(g, g, gg);
+      } else {                           // FP64 path: sigma = 1
+        const double g = -sinv[l] * acc;
+        R[l] = (TR)g;
+        gg64 = fma(g, g, gg64);
+      }
+    }
+    xm = xc; xc = xn; czm = czc;
   }
   if (sizeof(TR) == 4) {
     const float f[1] = {gg};
-    __syncthreads();   // also orders this tile after the previous tile's use of red
+    __syncthreads();
     {
       __shared__ float red[kBlock / 32];
-      const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
       float t = f[0];
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-      if (lane == 0) red[warp] = t;
+      if (c.lane == 0) red[threadIdx.x >> 5] = t;
       __syncthreads();
-      if (warp == 0) {
-        t = lane < kBlock / 32 ? red[lane] : 0.f;
+      if (threadIdx.x < 32) {
+        t = c.lane < kBlock / 32 ? red[c.lane] : 0.f;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-        if (lane == 0) A.partials[tile * kNR + 1] = (double)t;
+        if (c.lane == 0) A.partials[task * kNR + 1] = (double)t;
       }
     }
     const double v[1] = {rr};
-    tile_store<1>(A, tile, v);
+    tile_store<1>(A, task, v);
   } else {
     const double v[2] = {rr, gg64};
-    tile_store<2>(A, tile, v);
+    tile_store<2>(A, task, v);
   }
 }
 
 // ---- solution update: x_new = x + sigma S^-1 y (+ TINY once) -----------------------------------
 template <typename TY>
-__device__ __forceinline__ void xupdate_tile(const DevArrays& A, int64_t tile) {
-  const int inst = A.tile_inst[tile];
-  const InstScal& s = A.scal[inst];
-  if (!s.outer_active || s.inner_active || s.refine == 0) return;
-  const Geo G(A.inst[inst]);
-  const double* __restrict__ XR = A.tbuf[s.role[2]] + G.off;
-  double* __restrict__ XW = A.tbuf[s.role[3]] + G.off;
-  const TY* __restrict__ Y = Vec<TY>::y(A) + G.off;
-  const double* __restrict__ sinv = A.sinv + G.off;
-  const float* __restrict__ sinv32 = A.sinv32 + G.off;
+__global__ void __launch_bounds__(kBlock) k_xupdate(DevArrays A) {
+  const TCell c = task_cell(A, blockIdx.x);
+  const InstScal& s = A.scal[c.inst];
+  if (!s.outer_active || s.inner_active || s.refine == 0 || !c.act) return;
+  const int64_t off = c.off;
+  const double* __restrict__ XR = A.tbuf[s.role[2]] + off;
+  double* __restrict__ XW = A.tbuf[s.role[3]] + off;
+  const TY* __restrict__ Y = Vec<TY>::y(A) + off;
+  const double* __restrict__ sinv = A.sinv + off;
+  const float* __restrict__ sinv32 = A.sinv32 + off;
   const bool use_y = s.iter > 0;
   const bool tiny = s.tiny_pending != 0;
   const float sig = (float)s.sigma_prev;
-#pragma unroll
-  for (int k = 0; k < kCellsPerThread; ++k) {
-    const int32_t l = tile_cell(tile, G, k);
-    if (l >= G.n) continue;
+#pragma unroll 4
+  for (int z = c.z0; z < c.z1; ++z) {
+    const int l = c.base + z * c.nxy;
     double x = XR[l];
     if (tiny) x = x + kTiny;
     if (use_y) {
@@ -237,119 +261,101 @@ __device__ __forceinline__ void xupdate_tile(const DevArrays& A, int64_t tile) {
 // ---- inner CG on Ah (type T) -------------------------------------------------------------------
 // k_cg_p:    p = r + beta p  (beta = 0 on the first iteration)
 template <typename T>
-__device__ __forceinline__ void cg_p_tile(const DevArrays& A, int64_t tile) {
-  const int inst = A.tile_inst[tile];
-  const InstScal& s = A.scal[inst];
-  if (!s.inner_active) return;
-  const Geo G(A.inst[inst]);
+__global__ void __launch_bounds__(kBlock) k_cg_p(DevArrays A) {
+  const TCell c = task_cell(A, blockIdx.x);
+  const InstScal& s = A.scal[c.inst];
+  if (!s.inner_active || !c.act) return;
   const T beta = (T)s.beta;
   const bool first = (s.iter == 0);
-  const T* __restrict__ R = Vec<T>::r(A) + G.off;
-  T* __restrict__ P = Vec<T>::p(A) + G.off;
-#pragma unroll
-  for (int k = 0; k < kCellsPerThread; ++k) {
-    const int32_t l = tile_cell(tile, G, k);
-    if (l >= G.n) continue;
+  const T* __restrict__ R = Vec<T>::r(A) + c.off;
+  T* __restrict__ P = Vec<T>::p(A) + c.off;
+#pragma unroll 4
+  for (int z = c.z0; z < c.z1; ++z) {
+    const int l = c.base + z * c.nxy;
     P[l] = first ? R[l] : fma(beta, P[l], R[l]);
   }
 }
 
 // k_cg_spmv: q = Ah p, p.q
 template <typename T>
-__device__ __forceinline__ void cg_spmv_tile(const DevArrays& A, int64_t tile) {
-  const int inst = A.tile_inst[tile];
-  InstScal& s = A.scal[inst];
+__global__ void __launch_bounds__(kBlock) k_cg_spmv(DevArrays A) {
+  const int64_t task = blockIdx.x;
+  const TCell c = task_cell(A, task);
+  const InstScal& s = A.scal[c.inst];
   if (!s.inner_active) return;
-  const Geo G(A.inst[inst]);
-  const T* __restrict__ P = Vec<T>::p(A) + G.off;
-  T* __restrict__ Q = Vec<T>::q(A) + G.off;
-  const T* __restrict__ ax = Vec<T>::ax(A) + G.off;
-  const T* __restrict__ ay = Vec<T>::ay(A) + G.off;
-  const T* __restrict__ az = Vec<T>::az(A) + G.off;
-  T pq = 0;
-#pragma unroll
-  for (int k = 0; k < kCellsPerThread; ++k) {
-    const int32_t l = tile_cell(tile, G, k);
-    if (l >= G.n) continue;
-    const Coord c = coord3(G, l);
-    const T pc = P[l];
+  const int64_t off = c.off;
+  const T* __restrict__ P = Vec<T>::p(A) + off;
+  T* __restrict__ Q = Vec<T>::q(A) + off;
+  const T* __restrict__ ax = Vec<T>::ax(A) + off;
+  const T* __restrict__ ay = Vec<T>::ay(A) + off;
+  const T* __restrict__ az = Vec<T>::az(A) + off;
+  T pm, azm;
+  plane_below(c, P, az, pm, azm);
+  T pc = c.act ? P[c.base + c.z0 * c.nxy] : T(0);
+  T pq = T(0);
+  for (int z = c.z0; z < c.z1; ++z) {
+    const int l = c.base + z * c.nxy;
+    const T pn = plane_above(c, P, z);
+    const T axc = c.act ? ax[l] : T(0), ayc = c.act ? ay[l] : T(0), azc = c.act ? az[l] : T(0);
     T acc = pc;
-    stencil(G, ax, ay, az, l, c, [&](int32_t m) { return P[m]; },
-            [&](T cf, T pv) { acc = fma(cf, pv, acc); });
-    Q[l] = acc;
-    pq = fma(pc, acc, pq);
+    faces(c, P, ax, ay, l, pc, axc, ayc, azc, pm, azm, pn,
+          [&](T cf, T pv) { acc = fma(cf, pv, acc); });
+    if (c.act) {
+      Q[l] = acc;
+      pq = fma(pc, acc, pq);
+    }
+    pm = pc; pc = pn; azm = azc;
   }
   if (sizeof(T) == 4) {
     const float f[1] = {(float)pq};
-    tile_store_f<1>(A, tile, f);
+    tile_store_f<1>(A, task, f);
   } else {
     const double v[1] = {(double)pq};
-    tile_store<1>(A, tile, v);
+    tile_store<1>(A, task, v);
   }
 }
 
 // k_cg_upd: y += alpha p, r -= alpha q, r.r (and the unscaled ||r||^2 for the reference rule)
 template <typename T>
-__device__ __forceinline__ void cg_upd_tile(const DevArrays& A, int64_t tile) {
-  const int inst = A.tile_inst[tile];
-  InstScal& s = A.scal[inst];
+__global__ void __launch_bounds__(kBlock) k_cg_upd(DevArrays A) {
+  const int64_t task = blockIdx.x;
+  const TCell c = task_cell(A, task);
+  const InstScal& s = A.scal[c.inst];
   if (!s.inner_active) return;
-  const Geo G(A.inst[inst]);
   const DevOpts& o = A.opts;
   const bool weighted = (o.criterion == HF_STOP_RECURSIVE);
   const T alpha = (T)s.alpha;
   const bool first = (s.iter == 0);
-  T* __restrict__ Y = Vec<T>::y(A) + G.off;
-  T* __restrict__ R = Vec<T>::r(A) + G.off;
-  const T* __restrict__ P = Vec<T>::p(A) + G.off;
-  const T* __restrict__ Q = Vec<T>::q(A) + G.off;
-  const double* __restrict__ diag = A.diag + G.off;
-  T rr = 0;
+  const int64_t off = c.off;
+  T* __restrict__ Y = Vec<T>::y(A) + off;
+  T* __restrict__ R = Vec<T>::r(A) + off;
+  const T* __restrict__ P = Vec<T>::p(A) + off;
+  const T* __restrict__ Q = Vec<T>::q(A) + off;
+  const double* __restrict__ diag = A.diag + off;
+  T rr = T(0);
   double rw = 0.0;
-#pragma unroll
-  for (int k = 0; k < kCellsPerThread; ++k) {
-    const int32_t l = tile_cell(tile, G, k);
-    if (l >= G.n) continue;
-    const T pv = P[l];
-    Y[l] = first ? alpha * pv : fma(alpha, pv, Y[l]);
-    const T rv = fma(-alpha, Q[l], R[l]);
-    R[l] = rv;
-    rr = fma(rv, rv, rr);
-    if (weighted) rw = fma(-diag[l] * (double)rv, (double)rv, rw);
+  if (c.act) {
+#pragma unroll 4
+    for (int z = c.z0; z < c.z1; ++z) {
+      const int l = c.base + z * c.nxy;
+      const T pv = P[l];
+      Y[l] = first ? alpha * pv : fma(alpha, pv, Y[l]);
+      const T rv = fma(-alpha, Q[l], R[l]);
+      R[l] = rv;
+      rr = fma(rv, rv, rr);
+      if (weighted) rw = fma(-diag[l] * (double)rv, (double)rv, rw);
+    }
   }
   if (sizeof(T) == 4 && !weighted) {
     const float f[1] = {(float)rr};
-    tile_store_f<1>(A, tile, f);
+    tile_store_f<1>(A, task, f);
   } else {
     const double v[2] = {(double)rr, rw};
-    tile_store<2>(A, tile, v);
+    tile_store<2>(A, task, v);
   }
 }
 
-// Grid-stride wrappers: a resident set of blocks walks all tiles (instance data stays in L1
-// between consecutive tiles of one instance instead of being refetched by 16K short blocks).
-template <bool INIT, typename TR>
-__global__ void __launch_bounds__(kBlock) k_residual(DevArrays A) {
-  for (int64_t t = blockIdx.x; t < A.ntiles; t += gridDim.x) residual_tile<INIT, TR>(A, t);
-}
-template <typename TY>
-__global__ void __launch_bounds__(kBlock) k_xupdate(DevArrays A) {
-  for (int64_t t = blockIdx.x; t < A.ntiles; t += gridDim.x) xupdate_tile<TY>(A, t);
-}
-template <typename T>
-__global__ void __launch_bounds__(kBlock) k_cg_p(DevArrays A) {
-  for (int64_t t = blockIdx.x; t < A.ntiles; t += gridDim.x) cg_p_tile<T>(A, t);
-}
-template <typename T>
-__global__ void __launch_bounds__(kBlock) k_cg_spmv(DevArrays A) {
-  for (int64_t t = blockIdx.x; t < A.ntiles; t += gridDim.x) cg_spmv_tile<T>(A, t);
-}
-template <typename T>
-__global__ void __launch_bounds__(kBlock) k_cg_upd(DevArrays A) {
-  for (int64_t t = blockIdx.x; t < A.ntiles; t += gridDim.x) cg_upd_tile<T>(A, t);
-}
-
-// ---- finalize kernels: one block per instance sums the tile partials in tile order ----------
+// ---- finalize kernels: one block per instance sums the task partials in task order ----------
 // (deterministic), then runs the scalar epilogue of the producing kernel.
 
 // Epilogue of the RHS kernel (mod_evolve.f90:70-127 checks, initial scale of the FP32 rhs).
@@ -507,9 +513,9 @@ __global__ void __launch_bounds__(256) k_finalize(DevArrays A, CtrlState* ctrl,
     double acc[NR];
 #pragma unroll
     for (int k = 0; k < NR; ++k) acc[k] = 0.0;
-    for (int64_t t = threadIdx.x; t < d.ntiles; t += blockDim.x) {
+    for (int64_t t = threadIdx.x; t < d.ntask; t += blockDim.x) {
 #pragma unroll
-      for (int k = 0; k < NR; ++k) acc[k] += A.partials[(d.tile0 + t) * kNR + k];
+      for (int k = 0; k < NR; ++k) acc[k] += A.partials[(d.task0 + t) * kNR + k];
     }
     __shared__ double red[32 * NR];
     block_sum<NR>(acc, red);
@@ -599,7 +605,7 @@ cudaError_t launch_step_end(Ctx& c) {
 // mode 0: initial residual (+ finalize); mode 1: solution update + residual (+ finalize)
 cudaError_t launch_residual(Ctx& c, int mode, CtrlState* ctrl, cudaGraphConditionalHandle hw,
                             int graph) {
-  const unsigned nb = (unsigned)c.grid_tiles;
+  const unsigned nb = (unsigned)c.ntasks;
   const bool mixed = c.opts.precision == HF_PREC_MIXED;
   if (mode == 0) {
     if (mixed) k_residual<true, float><<<nb, kBlock, 0, c.stream>>>(c.A);
@@ -618,7 +624,7 @@ cudaError_t launch_residual(Ctx& c, int mode, CtrlState* ctrl, cudaGraphConditio
 
 cudaError_t launch_inner_iteration(Ctx& c, int fp32, CtrlState* ctrl,
                                    cudaGraphConditionalHandle hw, int graph) {
-  const unsigned nb = (unsigned)c.grid_tiles;
+  const unsigned nb = (unsigned)c.ntasks;
   if (fp32) {
     k_cg_p<float><<<nb, kBlock, 0, c.stream>>>(c.A);
     k_cg_spmv<float><<<nb, kBlock, 0, c.stream>>>(c.A);
@@ -668,7 +674,7 @@ cudaError_t launch_finalize(Ctx& c, int kind, CtrlState* ctrl, cudaGraphConditio
 
 // One kernel of the step, for timing (hf_time_kernel).
 cudaError_t launch_single(Ctx& c, int which) {
-  const unsigned nb = (unsigned)c.grid_tiles;
+  const unsigned nb = (unsigned)c.ntasks;
   const bool fp32 = c.opts.precision == HF_PREC_MIXED;
   switch (which) {
     case HF_KERNEL_RHS: return launch_rhs(c);
