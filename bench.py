@@ -45,6 +45,7 @@ BYTES_PER_CELL = {
     "residual_mixed": 6 * 8 + 4 + 4,
     # FP64: the same with g written in FP64
     "residual_fp64": 6 * 8 + 4 + 8,
+    # direction update: r, p_old read, p written; SpMV: p, ax, ay, az read, q written
     "cg_p_fp32": 3 * 4, "cg_spmv_fp32": 5 * 4, "cg_update_fp32": 6 * 4,
     # x read (8) + y (4) + sinv (4) read, x written (8)
     "xupdate_mixed": 8 + 4 + 4 + 8,
@@ -286,8 +287,8 @@ def main():
 
     # ---- kernel roofline: each kernel timed alone with CUDA events on the library's stream
     kernels = {"rhs": abi.HF_KERNEL_RHS, "residual_mixed": abi.HF_KERNEL_RESIDUAL,
-               "xupdate_mixed": abi.HF_KERNEL_XUPDATE,
-               "cg_p_fp32": abi.HF_KERNEL_CG_P, "cg_spmv_fp32": abi.HF_KERNEL_CG_SPMV,
+               "xupdate_mixed": abi.HF_KERNEL_XUPDATE, "cg_p_fp32": abi.HF_KERNEL_CG_P,
+               "cg_spmv_fp32": abi.HF_KERNEL_CG_SPMV,
                "cg_update_fp32": abi.HF_KERNEL_CG_UPDATE}
     kms = {name: hf.time_kernel(k, reps=20) for name, k in kernels.items()}
     per_step_launches = {

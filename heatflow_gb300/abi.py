@@ -108,6 +108,12 @@ _SIGNATURES = {
     "hf_assemble_coo": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, _ip, _ip, _dp, _ip, _ip]),
     "hf_time_kernel": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp]),
     "hf_measure_fp_rates": (C.c_int, [_dp, _dp]),
+    "hf_set_state_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "hf_get_state_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "hf_solve_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(HfStats)]),
+    "hf_adjoint_rhs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "hf_adjoint_accumulate": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
+                                        C.c_void_p]),
 }
 HF_KERNEL_RHS, HF_KERNEL_RESIDUAL, HF_KERNEL_CG_P, HF_KERNEL_CG_SPMV, HF_KERNEL_CG_UPDATE = 0, 1, 2, 3, 4
 HF_KERNEL_XUPDATE = 5

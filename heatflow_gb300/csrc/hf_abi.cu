@@ -504,8 +504,8 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
   if (c.any_em) ALLOC(A.emc, N);
   if (c.any_heater) ALLOC(A.icase, N);
   for (int k = 0; k < 4; ++k) ALLOC(A.tbuf[k], N);
-  ALLOC(A.b, N); ALLOC(A.y, N); ALLOC(A.r, N); ALLOC(A.p, N); ALLOC(A.q, N);
-  ALLOC(A.y32, N); ALLOC(A.r32, N); ALLOC(A.p32, N); ALLOC(A.q32, N);
+  ALLOC(A.b, N); ALLOC(A.y, N); ALLOC(A.r, N); ALLOC(A.p, N); ALLOC(A.q, N); ALLOC(A.p2, N);
+  ALLOC(A.y32, N); ALLOC(A.r32, N); ALLOC(A.p32, N); ALLOC(A.q32, N); ALLOC(A.p232, N);
   double *d_rho, *d_hc, *d_tau, *d_em = nullptr;
   ALLOC(d_rho, N); ALLOC(d_hc, N); ALLOC(d_tau, N);
   if (c.any_em) ALLOC(d_em, N);
@@ -520,10 +520,11 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
   for (void* p : {(void*)A.diag, (void*)A.cx, (void*)A.cy, (void*)A.cz, (void*)c.asm_.kappa,
                   (void*)d_rho, (void*)d_hc, (void*)d_tau, (void*)A.rhoc, (void*)A.ccat,
                   (void*)A.bvec, (void*)A.tau_s, (void*)A.a64x, (void*)A.a64y, (void*)A.a64z,
-                  (void*)A.b, (void*)A.y, (void*)A.r, (void*)A.p, (void*)A.q, (void*)A.rsum})
+                  (void*)A.b, (void*)A.y, (void*)A.r, (void*)A.p, (void*)A.q, (void*)A.rsum,
+                  (void*)A.p2})
     CK(cudaMemsetAsync(p, 0, N * sizeof(double), c.stream));
   for (void* p : {(void*)A.a32x, (void*)A.a32y, (void*)A.a32z, (void*)A.y32, (void*)A.r32,
-                  (void*)A.p32, (void*)A.q32, (void*)A.sinv32})
+                  (void*)A.p32, (void*)A.q32, (void*)A.sinv32, (void*)A.p232})
     CK(cudaMemsetAsync(p, 0, N * sizeof(float), c.stream));
   for (int k = 0; k < 4; ++k) CK(cudaMemsetAsync(A.tbuf[k], 0, N * sizeof(double), c.stream));
   if (d_em) CK(cudaMemsetAsync(d_em, 0, N * sizeof(double), c.stream));
@@ -917,6 +918,88 @@ int hf_solve(hf_ctx* h, const double* b, double* x, hf_stats* stats) {
   CU(cudaStreamSynchronize(c.stream));
   fill_stats(c, stats, 0, before);
   return first_error(c);
+}
+
+int hf_set_state_device(hf_ctx* h, const double* tp, const double* tpp) {
+  if (!h || !tp || !tpp) return set_err(HF_EARG, "null argument");
+  Ctx& c = h->c;
+  if (c.ninst != 1) return set_err(HF_EARG, "device state transfer takes single-grid contexts");
+  int rc = sync_scal(c);
+  if (rc) return rc;
+  const InstDesc& d = c.h_inst[0];
+  const InstScal& s = c.h_scal[0];
+  CU(cudaMemcpyAsync(c.A.tbuf[s.role[0]] + d.off, tp, 8 * d.n, cudaMemcpyDeviceToDevice, c.stream));
+  CU(cudaMemcpyAsync(c.A.tbuf[s.role[1]] + d.off, tpp, 8 * d.n, cudaMemcpyDeviceToDevice, c.stream));
+  CU(cudaStreamSynchronize(c.stream));
+  c.state_set = true;
+  return HF_OK;
+}
+
+int hf_get_state_device(hf_ctx* h, double* tp, double* tpp) {
+  if (!h) return set_err(HF_EARG, "null context");
+  Ctx& c = h->c;
+  if (c.ninst != 1) return set_err(HF_EARG, "device state transfer takes single-grid contexts");
+  int rc = sync_scal(c);
+  if (rc) return rc;
+  const InstDesc& d = c.h_inst[0];
+  const InstScal& s = c.h_scal[0];
+  if (tp) CU(cudaMemcpyAsync(tp, c.A.tbuf[s.role[0]] + d.off, 8 * d.n, cudaMemcpyDeviceToDevice, c.stream));
+  if (tpp) CU(cudaMemcpyAsync(tpp, c.A.tbuf[s.role[1]] + d.off, 8 * d.n, cudaMemcpyDeviceToDevice, c.stream));
+  CU(cudaStreamSynchronize(c.stream));
+  return HF_OK;
+}
+
+int hf_solve_device(hf_ctx* h, const double* b, double* x, hf_stats* stats) {
+  if (!h || !b || !x) return set_err(HF_EARG, "null argument");
+  Ctx& c = h->c;
+  if (c.ninst != 1) return set_err(HF_EARG, "hf_solve_device takes single-grid contexts");
+  int rc = sync_scal(c);
+  if (rc) return rc;
+  std::vector<InstScal> before(c.h_scal, c.h_scal + 1);
+  const InstDesc& d = c.h_inst[0];
+  InstScal& s = c.h_scal[0];
+  s.itime = 0;
+  s.outer_active = 1;
+  s.inner_active = 0;
+  s.refine = 0;
+  s.iter = 0;
+  s.step_iters = 0;
+  s.x0flag = 0;
+  s.tiny_pending = 0;
+  s.status = 0;
+  if ((rc = push_scal(c))) return rc;
+  CU(cudaMemcpyAsync(c.A.b + d.off, b, 8 * d.n, cudaMemcpyDeviceToDevice, c.stream));
+  CU(cudaMemcpyAsync(c.A.tbuf[s.role[2]] + d.off, x, 8 * d.n, cudaMemcpyDeviceToDevice, c.stream));
+  CU(launch_sumsq(c, c.A.b + d.off, d.n));
+  CU(launch_residual(c, 0));
+  if ((rc = solve_loop(c))) return rc;
+  if ((rc = sync_scal(c))) return rc;
+  CU(cudaMemcpyAsync(x, c.A.tbuf[c.h_scal[0].role[2]] + d.off, 8 * d.n, cudaMemcpyDeviceToDevice, c.stream));
+  CU(cudaStreamSynchronize(c.stream));
+  fill_stats(c, stats, 0, before);
+  return first_error(c);
+}
+
+int hf_adjoint_rhs(hf_ctx* h, const double* g, const double* l1, const double* l2, double* out) {
+  if (!h || !g || !l1 || !l2 || !out) return set_err(HF_EARG, "null argument");
+  Ctx& c = h->c;
+  if (c.ninst != 1) return set_err(HF_EARG, "the adjoint takes single-grid contexts");
+  CU(launch_adj_rhs(c, g, l1, l2, out));
+  CU(cudaStreamSynchronize(c.stream));
+  return HF_OK;
+}
+
+int hf_adjoint_accumulate(hf_ctx* h, const double* lam, const double* x, int64_t itime,
+                          double* grad_logk, double* grad_src) {
+  if (!h || !lam || !x || !grad_logk) return set_err(HF_EARG, "null argument");
+  Ctx& c = h->c;
+  if (c.ninst != 1) return set_err(HF_EARG, "the adjoint takes single-grid contexts");
+  for (int f = 0; f < 6; ++f)
+    if (c.h_bc[0].cg[f]) return set_err(HF_EARG, "the adjoint does not differentiate Neumann (CG) faces");
+  if (c.h_inst[0].has_em) return set_err(HF_EARG, "the adjoint does not differentiate the radiative term");
+  CU(launch_adj_grad(c, lam, x, itime, grad_logk, grad_src));
+  CU(cudaStreamSynchronize(c.stream));
+  return HF_OK;
 }
 
 int hf_assemble_coo(hf_ctx* h, int64_t inst, int64_t cap, int64_t* irow, int64_t* jcol, double* val,

@@ -30,9 +30,10 @@ constexpr int kBlock = 256;                  // threads per block of the cell ke
 constexpr int kCellsPerThread = 4;
 constexpr int kTile = kBlock * kCellsPerThread;   // cells per tile (one block per tile)
 constexpr int kNR = 8;
-// Step kernels work on tasks: a block of kTX x kTY threads owns kTX x kTY columns of one
-// instance (x fastest, one warp per row) and marches kZC planes along z.
-constexpr int kTX = 32, kTY = 8, kZC = 16;
+// Step kernels work on tasks: a block of 32 x kTY threads owns kXC*32 x kTY columns of one
+// instance (one warp per row; lane L holds columns x0 + L + 32 j, j < kXC) and marches kZC planes
+// along z.  (kXC > 1 trades occupancy for per-thread parallelism; on GB300 kXC = 1 is faster.)
+constexpr int kXC = 1, kTX = 32 * kXC, kTY = 8, kZC = 16;
 // InstScal::status bit: some S was NaN; the failing vector is found by the diagnosis kernel.
 constexpr int kStatusRhsNan = 1 << 16;                       // reduction slots per tile
 // Instances are laid out at multiples of kTile cells, so tile t covers cells
@@ -132,8 +133,8 @@ struct DevArrays {
   // state: four temperature-sized buffers, roles per instance in InstScal::role
   double* tbuf[4];
   // solver
-  double *b, *y, *r, *p, *q;
-  float *y32, *r32, *p32, *q32;
+  double *b, *y, *r, *p, *q, *p2;
+  float *y32, *r32, *p32, *q32, *p232;   // p / p2: search directions, ping-pong by iteration
   const int8_t* task_heat;  // per task: some cell holds a heater
   const int4* tasks;        // (instance, x0, y0, z0) per task
   int64_t ncells, ntiles, ninst, ntasks;
@@ -269,15 +270,16 @@ __device__ __forceinline__ void tile_store_f(const DevArrays& A, int64_t tile, c
   }
 }
 
-// The column of a task that this thread owns.
+// The columns of a task that this thread owns.
 struct TCell {
   int inst;
   int64_t off;
   int nx, ny, nz, nxy;
   bool px, py, pz;
-  int x, y, z0, z1, lane;
-  bool act;          // the column lies inside the grid
-  int base;          // local index of (x, y, 0)
+  int x0, y, z0, z1, lane;
+  __device__ int x(int j) const { return x0 + 32 * j + lane; }
+  __device__ bool act(int j) const { return x(j) < nx && y < ny; }   // column inside the grid
+  __device__ int base(int j) const { return y * nx + x(j); }          // local index of (x, y, 0)
 };
 __device__ __forceinline__ TCell task_cell(const DevArrays& A, int64_t task) {
   const int4 t = A.tasks[task];
@@ -288,12 +290,10 @@ __device__ __forceinline__ TCell task_cell(const DevArrays& A, int64_t task) {
   c.nx = d.nx; c.ny = d.ny; c.nz = d.nz; c.nxy = d.nx * d.ny;
   c.px = d.px; c.py = d.py; c.pz = d.pz;
   c.lane = threadIdx.x & 31;
-  c.x = t.y + c.lane;
+  c.x0 = t.y;
   c.y = t.z + (int)(threadIdx.x >> 5);
   c.z0 = t.w;
   c.z1 = min(t.w + kZC, d.nz);
-  c.act = c.x < d.nx && c.y < d.ny;
-  c.base = c.y * d.nx + c.x;
   return c;
 }
 
@@ -321,6 +321,10 @@ cudaError_t launch_step_begin(Ctx& c, int64_t itime, int first_of_run);
 cudaError_t launch_rhs(Ctx& c);
 cudaError_t launch_rhs_parts(Ctx& c, double* B, double* Q, double* Qd, double* Sc);
 cudaError_t launch_rhs_diagnose(Ctx& c);
+cudaError_t launch_adj_rhs(Ctx& c, const double* g, const double* l1, const double* l2, double* out);
+cudaError_t launch_adj_grad(Ctx& c, const double* lam, const double* x, int64_t itime,
+                            double* grad_logk, double* grad_src);
+cudaError_t launch_sumsq(Ctx& c, const double* b, int64_t n);
 cudaError_t launch_residual(Ctx& c, int mode, CtrlState* ctrl = nullptr,
                             cudaGraphConditionalHandle hw = 0, int graph = 0);
 cudaError_t launch_inner_iteration(Ctx& c, int fp32, CtrlState* ctrl = nullptr,

@@ -9,6 +9,8 @@
 // (DIAG) that finds the first failing vector in the reference's check order.
 //
 // Compiled with -fmad=false so that S is rounded exactly as the reference writes it.
+#include <algorithm>
+
 #include "hf_ctx.cuh"
 
 namespace hf {
@@ -70,10 +72,11 @@ __global__ void __launch_bounds__(kBlock) k_rhs(DevArrays A, double* oB, double*
   double bb = 0.0;
   int flag = 0;
   int nan_q = 0, nan_qd = 0, nan_sc = 0, nan_s = 0;
-  if (c.act) {
-#pragma unroll 4
-    for (int z = c.z0; z < c.z1; ++z) {
-      const int l = c.base + z * c.nxy;
+  for (int z = c.z0; z < c.z1; ++z) {
+#pragma unroll
+    for (int j = 0; j < kXC; ++j) {
+      if (!c.act(j)) continue;
+      const int l = c.base(j) + z * c.nxy;
       const double tp = Tp[l], tpp = Tpp[l];
       double q = 0.0, qd = 0.0;
       if (heater) {
@@ -149,6 +152,155 @@ cudaError_t launch_rhs_parts(Ctx& c, double* B, double* Q, double* Qd, double* S
 
 cudaError_t launch_rhs_diagnose(Ctx& c) {
   k_rhs<false, true><<<(unsigned)c.ntasks, kBlock, 0, c.stream>>>(c.A, nullptr, nullptr, nullptr, nullptr);
+  return cudaGetLastError();
+}
+
+}  // namespace hf
+
+// ---- adjoint (no counterpart in the reference: HeatFlow computes no gradients) -----------------
+// Forward step k:  H x_k = S_k,  S_k = a x_(k-1) + c x_(k-2) - Qdens_k - B   (per cell, diagonal a, c)
+// with a = -rho c / dt - 2 tau' rho c, c = tau' rho c (Cattaneo; c = 0 in Fourier mode).
+// Discrete adjoint, k = K..1:  H lambda_k = dJ/dx_k + a lambda_(k+1) + c lambda_(k+2)   (H = H^T),
+// dJ/dtheta = sum_k lambda_k^T (dS_k/dtheta - dH/dtheta x_k).
+
+namespace hf {
+
+__global__ void k_adj_rhs(DevArrays A, const double* g, const double* l1, const double* l2,
+                          double* out) {
+  const int64_t gi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gi >= A.ncells) return;
+  const InstDesc& d = A.inst[A.tile_inst[gi / kTile]];
+  const int64_t l = gi - d.off;
+  if (l >= d.n) return;
+  double v = g[l];
+  if (d.isteady == 0) {
+    const double cc = d.icattaneo == 1 ? A.ccat[gi] : 0.0;
+    const double a = -d.inv_dt * A.rhoc[gi] - 2.0 * cc;
+    v = fma(a, l1[l], v);
+    if (d.icattaneo == 1) v = fma(cc, l2[l], v);
+  }
+  out[l] = v;
+}
+
+// d c / d log(kappa_i) of a harmonic-mean face between kappa_i and kappa_j of length L
+// (c = 2 ki kj / ((ki + kj) L^2), times BR when ki != kj; mod_hmatrix.f90:289-314).
+__device__ __forceinline__ double dface(double ki, double kj, double L, double br) {
+  const double s = ki + kj;
+  double v = 2.0 * ki * kj * kj / (s * s * L * L);
+  return ki != kj ? v * br : v;
+}
+
+// grad_logk[i] += dJ/dlog(kappa_i) of step k; grad_src[i] += dJ/dP_i of step k (P: the cell's
+// heater power), for lambda_k, x_k.
+__global__ void k_adj_grad(DevArrays A, const InstBC* bcs, const double* kappa, const double* lam,
+                           const double* x, int64_t itime, double* grad_logk, double* grad_src) {
+  const int64_t gi = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gi >= A.ncells) return;
+  const int inst = A.tile_inst[gi / kTile];
+  const InstDesc& d = A.inst[inst];
+  const InstBC& bc = bcs[inst];
+  const int64_t l = gi - d.off;
+  if (l >= d.n) return;
+  const int64_t nx = d.nx, ny = d.ny, nz = d.nz, nxy = nx * ny;
+  const int64_t c3[3] = {l % nx, (l / nx) % ny, l / nxy};
+  const int64_t n3[3] = {nx, ny, nz}, st[3] = {1, nx, nxy};
+  const int per[3] = {d.px, d.py, d.pz};
+  const double* cf[3] = {A.cx + d.off, A.cy + d.off, A.cz + d.off};
+  const double* K = kappa + d.off;
+  const double ki = K[l], li = lam[l], xi = x[l];
+  double g = 0.0;
+  for (int a = 0; a < 3; ++a) {
+    const double L = d.len[a];
+    if (n3[a] == 1) {
+      // a lone cell along this axis has two outside faces (none when periodic)
+      if (!per[a]) {
+        for (int f = 2 * a; f <= 2 * a + 1; ++f) {
+          const double kb = bc.kb[f], s = kb + ki;
+          g += li * (xi - bc.tb[f]) * (2.0 * kb * kb * ki / (s * s * L * L)) * (ki != kb ? bc.br : 1.0);
+        }
+      }
+      continue;
+    }
+    // + face (stored at this cell)
+    const bool has_p = c3[a] + 1 < n3[a] || per[a];
+    if (has_p) {
+      const int64_t j = c3[a] + 1 < n3[a] ? l + st[a] : l - (n3[a] - 1) * st[a];
+      if (cf[a][l] != 0.0) g += -(li - lam[j]) * (x[j] - xi) * dface(ki, K[j], L, bc.br);
+    } else {
+      const int f = 2 * a + 1;
+      const double kb = bc.kb[f], s = kb + ki;
+      g += li * (xi - bc.tb[f]) * (2.0 * kb * kb * ki / (s * s * L * L)) * (ki != kb ? bc.br : 1.0);
+    }
+    // - face (stored at the - neighbour)
+    const bool has_m = c3[a] > 0 || per[a];
+    if (has_m) {
+      const int64_t j = c3[a] > 0 ? l - st[a] : l + (n3[a] - 1) * st[a];
+      if (cf[a][j] != 0.0) g += -(li - lam[j]) * (x[j] - xi) * dface(ki, K[j], L, bc.br);
+    } else {
+      const int f = 2 * a;
+      const double kb = bc.kb[f], s = kb + ki;
+      g += li * (xi - bc.tb[f]) * (2.0 * kb * kb * ki / (s * s * L * L)) * (ki != kb ? bc.br : 1.0);
+    }
+  }
+  grad_logk[l] += g;
+  if (grad_src && d.heater) {
+    const int cs = A.icase[gi];
+    if (cs > 0 && cs < 7) {
+      const double tau = d.has_case5 ? A.tau_s[gi] * pow(d.time_step, 2.0) : 0.0;
+      const double f = heat_case(cs, 1.0, tau, itime, d);
+      const double vn = d.qdens_mode == HF_QDENS_CELL_VOLUME ? d.volume : d.heated_volume;
+      grad_src[l] += -li * f / vn;
+    }
+  }
+}
+
+cudaError_t launch_adj_rhs(Ctx& c, const double* g, const double* l1, const double* l2, double* out) {
+  k_adj_rhs<<<(unsigned)((c.ncells + 255) / 256), 256, 0, c.stream>>>(c.A, g, l1, l2, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adj_grad(Ctx& c, const double* lam, const double* x, int64_t itime,
+                            double* grad_logk, double* grad_src) {
+  k_adj_grad<<<(unsigned)((c.ncells + 255) / 256), 256, 0, c.stream>>>(
+      c.A, c.d_bc, c.asm_.kappa, lam, x, itime, grad_logk, grad_src);
+  return cudaGetLastError();
+}
+
+}  // namespace hf
+
+namespace hf {
+
+// ||b||^2 of a single-instance device vector (for hf_solve_device): per-block partials in a
+// fixed order, then one block sums them and sets the instance's ||S||^2 and FP32 scale.
+__global__ void k_sumsq_partial(DevArrays A, const double* b, int64_t n) {
+  double acc = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    acc = fma(b[i], b[i], acc);
+  const double v[1] = {acc};
+  tile_store<1>(A, blockIdx.x, v);
+}
+
+__global__ void k_sumsq_final(DevArrays A, int nparts) {
+  double acc = 0.0;
+  for (int t = threadIdx.x; t < nparts; t += blockDim.x) acc += A.partials[(int64_t)t * kNR];
+  __shared__ double red[32];
+  double v[1] = {acc};
+  block_sum<1>(v, red);
+  if (threadIdx.x == 0) {
+    InstScal& s = A.scal[0];
+    const InstDesc& d = A.inst[0];
+    s.bb = v[0];
+    const double rms = sqrt(v[0] / (double)d.n) * d.mean_sinv * 1e-6;
+    s.sigma = (A.opts.precision == HF_PREC_MIXED && rms > 0.0 && isfinite(rms))
+                  ? exp2(rint(log2(rms))) : 1.0;
+  }
+}
+
+cudaError_t launch_sumsq(Ctx& c, const double* b, int64_t n) {
+  const int nparts = (int)std::min<int64_t>(std::min<int64_t>((n + 255) / 256, 1024), c.ntasks);
+  k_sumsq_partial<<<nparts, kBlock, 0, c.stream>>>(c.A, b, n);
+  k_sumsq_final<<<1, 256, 0, c.stream>>>(c.A, nparts);
   return cudaGetLastError();
 }
 

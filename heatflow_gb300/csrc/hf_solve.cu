@@ -32,6 +32,7 @@ template <> struct Vec<double> {
   __device__ static double* y(const DevArrays& A) { return A.y; }
   __device__ static double* r(const DevArrays& A) { return A.r; }
   __device__ static double* p(const DevArrays& A) { return A.p; }
+  __device__ static double* pb(const DevArrays& A, int64_t k) { return (k & 1) ? A.p2 : A.p; }
   __device__ static double* q(const DevArrays& A) { return A.q; }
   __device__ static const double* ax(const DevArrays& A) { return A.a64x; }
   __device__ static const double* ay(const DevArrays& A) { return A.a64y; }
@@ -41,6 +42,7 @@ template <> struct Vec<float> {
   __device__ static float* y(const DevArrays& A) { return A.y32; }
   __device__ static float* r(const DevArrays& A) { return A.r32; }
   __device__ static float* p(const DevArrays& A) { return A.p32; }
+  __device__ static float* pb(const DevArrays& A, int64_t k) { return (k & 1) ? A.p232 : A.p32; }
   __device__ static float* q(const DevArrays& A) { return A.q32; }
   __device__ static const float* ax(const DevArrays& A) { return A.a32x; }
   __device__ static const float* ay(const DevArrays& A) { return A.a32y; }
@@ -80,74 +82,90 @@ __global__ void k_step_end(DevArrays A) {
   if (i < A.ninst) end_step(A.scal[i]);
 }
 
-// ---- neighbour access for a task column ----------------------------------------------------
-// Values of the x +/- neighbours come from the lanes of the same warp (a warp owns one row
-// segment); lanes at a task edge, periodic wraps and the y neighbours are loaded; the z
-// neighbours roll through registers as the block marches along z.
-template <typename T>
-__device__ __forceinline__ T shfl_up1(T v) { return __shfl_up_sync(0xffffffffu, v, 1); }
-template <typename T>
-__device__ __forceinline__ T shfl_dn1(T v) { return __shfl_down_sync(0xffffffffu, v, 1); }
+// ---- neighbour access for the columns of a task ------------------------------------------------
+// x neighbours come from the lanes of the same warp (shuffles; across chunk boundaries from the
+// first/last lane of the next/previous chunk); lanes at a task edge, periodic wraps and the y
+// neighbours are loaded; the z neighbours roll through registers as the block marches along z.
+// Inactive lanes hold zeros, so every lane can take part in the shuffles.
+constexpr unsigned kFull = 0xffffffffu;
 
-// Sum over the six faces of cell l: fold(coef, neighbour value).  v[] is the field, c{x,y,z}
-// the face arrays; vc/cxc are this cell's value and x-face (for the shuffles); vm/czm the value
-// and z-face of plane z-1, vn the value of plane z+1 (registers).
-template <typename T, typename C, class F>
-__device__ __forceinline__ void faces(const TCell& c, const T* __restrict__ v, const C* __restrict__ cx,
-                                      const C* __restrict__ cy, int l, T vc, C cxc, C cyc, C czc,
-                                      T vm, C czm, T vn, F fold) {
-  // x (all lanes shuffle; inactive lanes hold zeros)
-  T vw = shfl_up1(vc);
-  C cxw = shfl_up1(cxc);
-  T ve = shfl_dn1(vc);
-  if (!c.act) return;
-  const int nx = c.nx;
-  if (c.lane == 0) {
-    if (c.x > 0) { vw = v[l - 1]; cxw = cx[l - 1]; }
-    else if (c.px && nx > 1) { vw = v[l + nx - 1]; cxw = cx[l + nx - 1]; }
-    else { vw = T(0); cxw = C(0); }
-  }
-  if (c.x + 1 < nx) { if (c.lane == 31) ve = v[l + 1]; }
-  else if (c.px && nx > 1) ve = v[l - (nx - 1)];
-  else ve = T(0);
-  fold(cxc, ve);
-  fold(cxw, vw);
-  // y
-  if (c.ny > 1) {
-    if (c.y + 1 < c.ny) fold(cyc, v[l + nx]);
-    else if (c.py) fold(cyc, v[l - (c.ny - 1) * nx]);
-    if (c.y > 0) fold(cy[l - nx], v[l - nx]);
-    else if (c.py) fold(cy[l + (c.ny - 1) * nx], v[l + (c.ny - 1) * nx]);
-  }
-  // z
-  if (c.nz > 1) {
-    fold(czc, vn);
-    fold(czm, vm);
+// West/east values and west face of chunk j at local cell l.
+template <typename T, typename C, class V>
+__device__ __forceinline__ void x_nbrs(const TCell& c, int j, const T (&vc)[kXC],
+                                       const C (&cxc)[kXC], int l, V v, const C* __restrict__ cx,
+                                       T& vw, C& cxw, T& ve) {
+  const T up = __shfl_up_sync(kFull, vc[j], 1);
+  const C cup = __shfl_up_sync(kFull, cxc[j], 1);
+  const T dn = __shfl_down_sync(kFull, vc[j], 1);
+  const T prev_last = __shfl_sync(kFull, vc[j > 0 ? j - 1 : 0], 31);
+  const C cprev_last = __shfl_sync(kFull, cxc[j > 0 ? j - 1 : 0], 31);
+  const T next_first = __shfl_sync(kFull, vc[j + 1 < kXC ? j + 1 : j], 0);
+  vw = T(0); cxw = C(0); ve = T(0);
+  if (!c.act(j)) return;
+  const int x = c.x(j), nx = c.nx;
+  if (c.lane > 0) { vw = up; cxw = cup; }
+  else if (j > 0) { vw = prev_last; cxw = cprev_last; }
+  else if (x > 0) { vw = v(l - 1); cxw = cx[l - 1]; }
+  else if (c.px && nx > 1) { vw = v(l + nx - 1); cxw = cx[l + nx - 1]; }
+  if (x + 1 < nx) {
+    if (c.lane < 31) ve = dn;
+    else if (j + 1 < kXC) ve = next_first;
+    else ve = v(l + 1);
+  } else if (c.px && nx > 1) {
+    ve = v(l - (nx - 1));
   }
 }
 
-// Value and z-face of plane z-1 for the first plane of a task.
-template <typename T, typename C>
-__device__ __forceinline__ void plane_below(const TCell& c, const T* __restrict__ v,
-                                            const C* __restrict__ cz, T& vm, C& czm) {
+// The y faces of cell l (chunk j active): fold(coef, value).
+template <typename T, typename C, class V, class F>
+__device__ __forceinline__ void y_faces(const TCell& c, int l, C cyc, V v, const C* __restrict__ cy,
+                                        F fold) {
+  if (c.ny < 2) return;
+  const int nx = c.nx;
+  if (c.y + 1 < c.ny) fold(cyc, v(l + nx));
+  else if (c.py) fold(cyc, v(l - (c.ny - 1) * nx));
+  if (c.y > 0) fold(cy[l - nx], v(l - nx));
+  else if (c.py) fold(cy[l + (c.ny - 1) * nx], v(l + (c.ny - 1) * nx));
+}
+
+// Value and z-face of plane z0-1 of chunk j (zeros at a non-periodic bottom face).
+template <typename T, typename C, class V>
+__device__ __forceinline__ void plane_below(const TCell& c, int j, V v, const C* __restrict__ cz,
+                                            T& vm, C& czm) {
   vm = T(0);
   czm = C(0);
-  if (!c.act || c.nz < 2) return;
-  if (c.z0 > 0) {
-    const int l = c.base + (c.z0 - 1) * c.nxy;
-    vm = v[l]; czm = cz[l];
-  } else if (c.pz) {
-    const int l = c.base + (c.nz - 1) * c.nxy;
-    vm = v[l]; czm = cz[l];
-  }
+  if (!c.act(j) || c.nz < 2) return;
+  int l;
+  if (c.z0 > 0) l = c.base(j) + (c.z0 - 1) * c.nxy;
+  else if (c.pz) l = c.base(j) + (c.nz - 1) * c.nxy;
+  else return;
+  vm = v(l);
+  czm = cz[l];
 }
 
-template <typename T>
-__device__ __forceinline__ T plane_above(const TCell& c, const T* __restrict__ v, int z) {
-  if (!c.act || c.nz < 2) return T(0);
-  if (z + 1 < c.nz) return v[c.base + (z + 1) * c.nxy];
-  if (c.pz) return v[c.base];
+template <typename T, class V>
+__device__ __forceinline__ T plane_above(const TCell& c, int j, V v, int z) {
+  if (!c.act(j) || c.nz < 2) return T(0);
+  if (z + 1 < c.nz) return v(c.base(j) + (z + 1) * c.nxy);
+  if (c.pz) return v(c.base(j));
   return T(0);
+}
+
+// FP32 block sum of one value into partial slot k of a task (one conversion per block).
+__device__ __forceinline__ void task_store_f(const DevArrays& A, int64_t task, int k, float v) {
+  __shared__ float red[kBlock / 32];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    v = lane < kBlock / 32 ? red[lane] : 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+    if (lane == 0) A.partials[task * kNR + k] = (double)v;
+  }
 }
 
 // ---- FP64 true residual ------------------------------------------------------------------------
@@ -175,53 +193,60 @@ __global__ void __launch_bounds__(kBlock) k_residual(DevArrays A) {
   const float isig = (float)(1.0 / s.sigma);
   // INIT: the residual of x0 + TINY (mod_evolve.f90:141) is r(x0) - TINY * H1
   const bool tiny = INIT && s.x0flag;
-  double xm, czm;
-  plane_below(c, X, cz, xm, czm);
-  double xc = c.act ? X[c.base + c.z0 * c.nxy] : 0.0;
+  auto xval = [&](int m) -> double { return X[m]; };
+  double xm[kXC], czm[kXC], xc[kXC];
+#pragma unroll
+  for (int j = 0; j < kXC; ++j) {
+    plane_below<double>(c, j, xval, cz, xm[j], czm[j]);
+    xc[j] = c.act(j) ? X[c.base(j) + c.z0 * c.nxy] : 0.0;
+  }
   double rr = 0.0, gg64 = 0.0;
   float gg = 0.f;
   for (int z = c.z0; z < c.z1; ++z) {
-    const int l = c.base + z * c.nxy;
-    const double xn = plane_above(c, X, z);
-    const double cxc = c.act ? cx[l] : 0.0, cyc = c.act ? cy[l] : 0.0, czc = c.act ? cz[l] : 0.0;
-    double acc = 0.0;
-    if (c.act) {
-      acc = fma(-diag[l], xc, b[l]);
-      if (tiny) acc = fma(-kTiny, rsum[l], acc);
+    double xn[kXC], cxc[kXC], acc[kXC];
+#pragma unroll
+    for (int j = 0; j < kXC; ++j) {
+      const int l = c.base(j) + z * c.nxy;
+      const bool a = c.act(j);
+      xn[j] = plane_above<double>(c, j, xval, z);
+      cxc[j] = a ? cx[l] : 0.0;
+      acc[j] = 0.0;
+      if (a) {
+        acc[j] = fma(-diag[l], xc[j], b[l]);
+        if (tiny) acc[j] = fma(-kTiny, rsum[l], acc[j]);
+      }
     }
-    faces(c, X, cx, cy, l, xc, cxc, cyc, czc, xm, czm, xn,
-          [&](double cf, double xv) { acc = fma(-cf, xv, acc); });
-    if (c.act) {
-      rr = fma(acc, acc, rr);
+#pragma unroll
+    for (int j = 0; j < kXC; ++j) {
+      const int l = c.base(j) + z * c.nxy;
+      double xw, cxw, xe;
+      x_nbrs(c, j, xc, cxc, l, xval, cx, xw, cxw, xe);
+      if (!c.act(j)) continue;
+      double a = acc[j];
+      a = fma(-cxc[j], xe, a);
+      a = fma(-cxw, xw, a);
+      y_faces<double>(c, l, cy[l], xval, cy, [&](double cf, double xv) { a = fma(-cf, xv, a); });
+      if (c.nz > 1) {
+        a = fma(-cz[l], xn[j], a);
+        a = fma(-czm[j], xm[j], a);
+      }
+      rr = fma(a, a, rr);
       if (sizeof(TR) == 4) {             // mixed: g in FP32, scaled by 1/sigma
-        const float g = -sinv32[l] * f64_to_f32_trunc(acc) * isig;
+        const float g = -sinv32[l] * f64_to_f32_trunc(a) * isig;
         R[l] = (TR)g;
         gg = fmaf(g, g, gg);
       } else {                           // FP64 path: sigma = 1
-        const double g = -sinv[l] * acc;
+        const double g = -sinv[l] * a;
         R[l] = (TR)g;
         gg64 = fma(g, g, gg64);
       }
+      czm[j] = cz[l];
     }
-    xm = xc; xc = xn; czm = czc;
+#pragma unroll
+    for (int j = 0; j < kXC; ++j) { xm[j] = xc[j]; xc[j] = xn[j]; }
   }
   if (sizeof(TR) == 4) {
-    const float f[1] = {gg};
-    __syncthreads();
-    {
-      __shared__ float red[kBlock / 32];
-      float t = f[0];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-      if (c.lane == 0) red[threadIdx.x >> 5] = t;
-      __syncthreads();
-      if (threadIdx.x < 32) {
-        t = c.lane < kBlock / 32 ? red[c.lane] : 0.f;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-        if (c.lane == 0) A.partials[task * kNR + 1] = (double)t;
-      }
-    }
+    task_store_f(A, task, 1, gg);
     const double v[1] = {rr};
     tile_store<1>(A, task, v);
   } else {
@@ -235,7 +260,7 @@ template <typename TY>
 __global__ void __launch_bounds__(kBlock) k_xupdate(DevArrays A) {
   const TCell c = task_cell(A, blockIdx.x);
   const InstScal& s = A.scal[c.inst];
-  if (!s.outer_active || s.inner_active || s.refine == 0 || !c.act) return;
+  if (!s.outer_active || s.inner_active || s.refine == 0) return;
   const int64_t off = c.off;
   const double* __restrict__ XR = A.tbuf[s.role[2]] + off;
   double* __restrict__ XW = A.tbuf[s.role[3]] + off;
@@ -245,70 +270,117 @@ __global__ void __launch_bounds__(kBlock) k_xupdate(DevArrays A) {
   const bool use_y = s.iter > 0;
   const bool tiny = s.tiny_pending != 0;
   const float sig = (float)s.sigma_prev;
-#pragma unroll 4
   for (int z = c.z0; z < c.z1; ++z) {
-    const int l = c.base + z * c.nxy;
-    double x = XR[l];
-    if (tiny) x = x + kTiny;
-    if (use_y) {
-      if (sizeof(TY) == 8) x = fma(sinv[l], (double)Y[l], x);   // sigma = 1 on the FP64 path
-      else x = x + f32_to_f64(sig * sinv32[l] * (float)Y[l]);
+#pragma unroll
+    for (int j = 0; j < kXC; ++j) {
+      if (!c.act(j)) continue;
+      const int l = c.base(j) + z * c.nxy;
+      double x = XR[l];
+      if (tiny) x = x + kTiny;
+      if (use_y) {
+        if (sizeof(TY) == 8) x = fma(sinv[l], (double)Y[l], x);   // sigma = 1 on the FP64 path
+        else x = x + f32_to_f64(sig * sinv32[l] * (float)Y[l]);
+      }
+      XW[l] = x;
     }
-    XW[l] = x;
   }
 }
 
 // ---- inner CG on Ah (type T) -------------------------------------------------------------------
-// k_cg_p:    p = r + beta p  (beta = 0 on the first iteration)
+// The direction p_k = r + beta p_(k-1) (p_0 = r) is written to the buffer of parity k; the
+// previous direction is read from the other buffer of the pair.
 template <typename T>
 __global__ void __launch_bounds__(kBlock) k_cg_p(DevArrays A) {
   const TCell c = task_cell(A, blockIdx.x);
   const InstScal& s = A.scal[c.inst];
-  if (!s.inner_active || !c.act) return;
+  if (!s.inner_active) return;
+  const int64_t k = s.iter;
+  const bool first = (k == 0);
   const T beta = (T)s.beta;
-  const bool first = (s.iter == 0);
   const T* __restrict__ R = Vec<T>::r(A) + c.off;
-  T* __restrict__ P = Vec<T>::p(A) + c.off;
+  const T* __restrict__ Po = Vec<T>::pb(A, k + 1) + c.off;
+  T* __restrict__ Pn = Vec<T>::pb(A, k) + c.off;
+#pragma unroll
+  for (int j = 0; j < kXC; ++j) {
+    if (!c.act(j)) continue;
 #pragma unroll 4
-  for (int z = c.z0; z < c.z1; ++z) {
-    const int l = c.base + z * c.nxy;
-    P[l] = first ? R[l] : fma(beta, P[l], R[l]);
+    for (int z = c.z0; z < c.z1; ++z) {
+      const int l = c.base(j) + z * c.nxy;
+      Pn[l] = first ? R[l] : fma(beta, Po[l], R[l]);
+    }
   }
 }
 
-// k_cg_spmv: q = Ah p, p.q
+// k_cg_spmv: q = Ah p_k and p_k.q.  One column per thread; the operands of plane z+1 (its
+// coefficients, y neighbours and plane z+2) are loaded while plane z is computed, so each
+// thread keeps two planes of loads in flight.
 template <typename T>
 __global__ void __launch_bounds__(kBlock) k_cg_spmv(DevArrays A) {
+  static_assert(kXC == 1, "one column per thread");
   const int64_t task = blockIdx.x;
   const TCell c = task_cell(A, task);
   const InstScal& s = A.scal[c.inst];
   if (!s.inner_active) return;
   const int64_t off = c.off;
-  const T* __restrict__ P = Vec<T>::p(A) + off;
+  const T* __restrict__ P = Vec<T>::pb(A, s.iter) + off;
   T* __restrict__ Q = Vec<T>::q(A) + off;
   const T* __restrict__ ax = Vec<T>::ax(A) + off;
   const T* __restrict__ ay = Vec<T>::ay(A) + off;
   const T* __restrict__ az = Vec<T>::az(A) + off;
+  const bool act = c.act(0);
+  const int nx = c.nx, ny = c.ny, nxy = c.nxy, base = c.base(0);
+  auto pv = [&](int m) -> T { return P[m]; };
+  // operands of one plane: own value, its faces, y neighbours (+ south face)
+  struct Plane { T p, axc, ayc, azc, pnn, ps, ays; };
+  auto load = [&](int z, Plane& o) {
+    o = Plane{T(0), T(0), T(0), T(0), T(0), T(0), T(0)};
+    if (!act || z >= c.nz) return;
+    const int l = base + z * nxy;
+    o.p = P[l]; o.axc = ax[l]; o.ayc = ay[l]; o.azc = az[l];
+    if (ny > 1) {
+      if (c.y + 1 < ny) o.pnn = P[l + nx];
+      else if (c.py) o.pnn = P[l - (ny - 1) * nx];
+      if (c.y > 0) { o.ps = P[l - nx]; o.ays = ay[l - nx]; }
+      else if (c.py) { o.ps = P[l + (ny - 1) * nx]; o.ays = ay[l + (ny - 1) * nx]; }
+    }
+  };
   T pm, azm;
-  plane_below(c, P, az, pm, azm);
-  T pc = c.act ? P[c.base + c.z0 * c.nxy] : T(0);
+  plane_below<T>(c, 0, pv, az, pm, azm);
+  Plane cur, nxt;
+  load(c.z0, cur);
   T pq = T(0);
   for (int z = c.z0; z < c.z1; ++z) {
-    const int l = c.base + z * c.nxy;
-    const T pn = plane_above(c, P, z);
-    const T axc = c.act ? ax[l] : T(0), ayc = c.act ? ay[l] : T(0), azc = c.act ? az[l] : T(0);
-    T acc = pc;
-    faces(c, P, ax, ay, l, pc, axc, ayc, azc, pm, azm, pn,
-          [&](T cf, T pv) { acc = fma(cf, pv, acc); });
-    if (c.act) {
-      Q[l] = acc;
-      pq = fma(pc, acc, pq);
+    // plane z+1 (wrapping to 0 on a periodic z axis) is both the next plane and the z+ value
+    if (z + 1 < c.nz) load(z + 1, nxt);
+    else {
+      nxt = Plane{T(0), T(0), T(0), T(0), T(0), T(0), T(0)};
+      if (act && c.pz && c.nz > 1) nxt.p = P[base];
     }
-    pm = pc; pc = pn; azm = azc;
+    const int l = base + z * nxy;
+    T pcv[kXC] = {cur.p};
+    T axv[kXC] = {cur.axc};
+    T pw, axw, pe;
+    x_nbrs(c, 0, pcv, axv, l, pv, ax, pw, axw, pe);
+    if (act) {
+      T acc = cur.p;
+      acc = fma(cur.axc, pe, acc);
+      acc = fma(axw, pw, acc);
+      if (ny > 1) {
+        acc = fma(cur.ayc, cur.pnn, acc);
+        acc = fma(cur.ays, cur.ps, acc);
+      }
+      if (c.nz > 1) {
+        acc = fma(cur.azc, nxt.p, acc);
+        acc = fma(azm, pm, acc);
+      }
+      Q[l] = acc;
+      pq = fma(cur.p, acc, pq);
+    }
+    pm = cur.p; azm = cur.azc;
+    cur = nxt;
   }
   if (sizeof(T) == 4) {
-    const float f[1] = {(float)pq};
-    tile_store_f<1>(A, task, f);
+    task_store_f(A, task, 0, (float)pq);
   } else {
     const double v[1] = {(double)pq};
     tile_store<1>(A, task, v);
@@ -329,15 +401,16 @@ __global__ void __launch_bounds__(kBlock) k_cg_upd(DevArrays A) {
   const int64_t off = c.off;
   T* __restrict__ Y = Vec<T>::y(A) + off;
   T* __restrict__ R = Vec<T>::r(A) + off;
-  const T* __restrict__ P = Vec<T>::p(A) + off;
+  const T* __restrict__ P = Vec<T>::pb(A, s.iter) + off;
   const T* __restrict__ Q = Vec<T>::q(A) + off;
   const double* __restrict__ diag = A.diag + off;
   T rr = T(0);
   double rw = 0.0;
-  if (c.act) {
-#pragma unroll 4
-    for (int z = c.z0; z < c.z1; ++z) {
-      const int l = c.base + z * c.nxy;
+  for (int z = c.z0; z < c.z1; ++z) {
+#pragma unroll
+    for (int j = 0; j < kXC; ++j) {
+      if (!c.act(j)) continue;
+      const int l = c.base(j) + z * c.nxy;
       const T pv = P[l];
       Y[l] = first ? alpha * pv : fma(alpha, pv, Y[l]);
       const T rv = fma(-alpha, Q[l], R[l]);
@@ -347,8 +420,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_upd(DevArrays A) {
     }
   }
   if (sizeof(T) == 4 && !weighted) {
-    const float f[1] = {(float)rr};
-    tile_store_f<1>(A, task, f);
+    task_store_f(A, task, 0, (float)rr);
   } else {
     const double v[2] = {(double)rr, rw};
     tile_store<2>(A, task, v);

@@ -178,12 +178,29 @@ int hf_solve(hf_ctx* ctx, const double* b, double* x, hf_stats* stats);
 int hf_assemble_coo(hf_ctx* ctx, int64_t instance, int64_t cap, int64_t* irow, int64_t* jcol,
                     double* val, int64_t* len, int64_t* count);
 
+/* ---- device-resident state and the discrete adjoint ------------------------------------------
+ * No reference counterpart: HeatFlow computes no gradients.  Single-grid contexts; every pointer
+ * is a device buffer of nx*ny*nz doubles in cell order.  With the forward step
+ * H x_k = S_k = a x_(k-1) + c x_(k-2) - Qdens_k - B (a = -rho c/dt - 2 tau' rho c, c = tau' rho c),
+ * the adjoint runs k = K..1:  H lambda_k = dJ/dx_k + a lambda_(k+1) + c lambda_(k+2)  (H = H^T). */
+int hf_set_state_device(hf_ctx* ctx, const double* temp_p, const double* temp_pp);
+int hf_get_state_device(hf_ctx* ctx, double* temp_p, double* temp_pp);
+/* Solve H x = b (x: initial guess in, solution out) with the context's options. */
+int hf_solve_device(hf_ctx* ctx, const double* b, double* x, hf_stats* stats);
+/* out = g + a*lam1 + c*lam2 (the adjoint right-hand side of one step). */
+int hf_adjoint_rhs(hf_ctx* ctx, const double* g, const double* lam1, const double* lam2, double* out);
+/* grad_logk += lambda^T (dS/dlog kappa - dH/dlog kappa x) over every face of every cell;
+ * grad_src += lambda^T dS/dP (P: each cell's heater power at step itime); grad_src may be NULL.
+ * Rejects Neumann (CG) faces and emissivity, whose terms are not differentiated. */
+int hf_adjoint_accumulate(hf_ctx* ctx, const double* lam, const double* x, int64_t itime,
+                          double* grad_logk, double* grad_src);
+
 /* ---- measurement (no reference counterpart: the reference times with cpu_time only) ------- */
 enum {
   HF_KERNEL_RHS = 0,         /* per-step right-hand side */
   HF_KERNEL_RESIDUAL = 1,    /* FP64 solution update + true residual sweep */
-  HF_KERNEL_CG_P = 2,        /* inner CG direction update (FP32 in mixed mode, else FP64) */
-  HF_KERNEL_CG_SPMV = 3,     /* inner CG SpMV + p.Ap */
+  HF_KERNEL_CG_P = 2,        /* inner CG direction update p = r + beta p */
+  HF_KERNEL_CG_SPMV = 3,     /* inner CG SpMV q = A p and p.q */
   HF_KERNEL_CG_UPDATE = 4,   /* inner CG solution/residual update + r.r */
   HF_KERNEL_XUPDATE = 5      /* FP64 solution update x += S^-1 y */
 };

@@ -1,0 +1,67 @@
+"""The discrete adjoint (hf_adjoint_rhs / hf_adjoint_accumulate / hf_solve_device behind
+torch.autograd.Function) against central finite differences and against the FP64 gradient.
+
+Workload: a 12^3 copy of the inverse problem (hidden smoothed log-kappa field, probes, 8 point
+sources, Cattaneo), 60 steps with checkpoints every 25 steps (segments 25, 25, 10)."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+FP64 = dict(precision="fp64", criterion="recursive", tol=1e-32)
+
+
+@pytest.fixture(scope="module")
+def setup(cuda_lib):
+    from heatflow_gb300.adjoint import AdjointModel, inverse_problem
+    template, probes, sources, hidden, amps = inverse_problem(n=12, nsteps=60, nprobes=16,
+                                                              nsources=8, seed=3)
+    model = AdjointModel(template, probes, sources, 60, ckpt_every=25, **FP64)
+    obs, _, hf = model.forward(hidden, amps)
+    hf.close()
+    N = template.ncells
+    lk0 = hidden + 0.3 * np.sin(np.arange(N) * 0.37)      # a guess away from the hidden field
+    a0 = amps * 0.7
+    return model, obs, lk0, a0
+
+
+def _adjoint_grad(model, obs, lk0, a0):
+    from heatflow_gb300.adjoint import ProbeMisfit
+    lk = torch.tensor(lk0, dtype=torch.float64, device="cuda", requires_grad=True)
+    a = torch.tensor(a0, dtype=torch.float64, device="cuda", requires_grad=True)
+    J = ProbeMisfit.apply(lk, a, model, obs)
+    J.backward()
+    return float(J), lk.grad.cpu().numpy(), a.grad.cpu().numpy()
+
+
+def test_adjoint_matches_central_fd(setup):
+    model, obs, lk0, a0 = setup
+    J, glk, ga = _adjoint_grad(model, obs, lk0, a0)
+    assert J > 0 and np.isfinite(glk).all() and np.isfinite(ga).all()
+    eps = 1e-6
+    cells = list(np.argsort(-np.abs(glk))[:6])
+    for i in cells:
+        lp, lm = lk0.copy(), lk0.copy()
+        lp[i] += eps
+        lm[i] -= eps
+        fd = (model.loss(lp, a0, obs) - model.loss(lm, a0, obs)) / (2 * eps)
+        assert abs(fd - glk[i]) <= 1e-6 * abs(glk[i]) + 1e-9 * np.abs(glk).max(), (i, fd, glk[i])
+    for s in range(len(a0)):
+        h = eps * a0[s]
+        ap, am = a0.copy(), a0.copy()
+        ap[s] += h
+        am[s] -= h
+        fd = (model.loss(lk0, ap, obs) - model.loss(lk0, am, obs)) / (2 * h)
+        assert abs(fd - ga[s]) <= 1e-6 * abs(ga[s]) + 1e-9 * np.abs(ga).max(), (s, fd, ga[s])
+
+
+def test_mixed_gradient_close_to_fp64(setup):
+    from heatflow_gb300.adjoint import AdjointModel
+    model, obs, lk0, a0 = setup
+    _, glk, ga = _adjoint_grad(model, obs, lk0, a0)
+    mixed = AdjointModel(model.template, model.probes.cpu().numpy(), model.sources_np, model.nsteps,
+                         ckpt_every=25, precision="mixed", criterion="true", tol=1e-12)
+    _, glk_m, ga_m = _adjoint_grad(mixed, obs, lk0, a0)
+    assert np.linalg.norm(glk_m - glk) <= 1e-6 * np.linalg.norm(glk)
+    assert np.linalg.norm(ga_m - ga) <= 1e-6 * np.linalg.norm(ga)
