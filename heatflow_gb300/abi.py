@@ -109,6 +109,9 @@ _SIGNATURES = {
     "hf_time_kernel": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp]),
     "hf_measure_fp_rates": (C.c_int, [_dp, _dp]),
     "hf_set_state_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "hf_residual_noalloc": (C.c_int, [C.c_int64, C.c_int64, C.c_int64, C.POINTER(C.c_int32),
+                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "hf_get_state_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "hf_solve_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(HfStats)]),
     "hf_adjoint_rhs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

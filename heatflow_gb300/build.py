@@ -25,6 +25,7 @@ UNITS = {
     "hf_solve.cu": [],
     "hf_abi.cu": ["-fmad=false"],
     "hf_probe.cu": [],
+    "hf_noalloc.cu": [],
 }
 
 

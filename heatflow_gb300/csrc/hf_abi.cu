@@ -29,6 +29,10 @@ static int set_err(int code, const std::string& msg) {
   return code;
 }
 
+namespace hf {
+void set_last_error(const std::string& msg) { g_err = msg; }
+}
+
 #define CU(call)                                                                         \
   do {                                                                                   \
     cudaError_t e_ = (call);                                                             \

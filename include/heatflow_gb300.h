@@ -212,6 +212,25 @@ int hf_time_kernel(hf_ctx* ctx, int kernel, int reps, double* ms_per_launch);
  * every SM, CUDA-event timed).  On GB300 the FP64 rate bounds the FP64 kernels of a step. */
 int hf_measure_fp_rates(double* fp64_tflops, double* fp32_tflops);
 
+/* ---- allocation-free residual ---------------------------------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device memory - hosts that
+ * own all device memory through a fixed arena and hand the library pre-allocated buffers, and
+ * loops that may not stall on the allocator (cudaMalloc can synchronise the device): r = b - H x and
+ * norms2 = {||r||^2, ||b||^2} for the geometric operator of hf_get_operator (diag and the face to
+ * the + neighbour per axis, periodic wrap on the last cell of a periodic axis).  Every pointer is
+ * a caller-owned device buffer (norms2: two doubles); stream is a cudaStream_t or NULL.  The call
+ * allocates nothing: its reduction scratch is a static device array of 256 KiB that every device
+ * loading the library holds until the process exits, which limits grids to
+ * HF_NOALLOC_MAX_CELLS cells (larger grids return HF_EARG).  The first call on a device looks up
+ * that array's device address (cudaGetSymbolAddress), so make it before any stream capture.
+ * Calls share the scratch and keep the last call's partial sums: calls whose kernels overlap on
+ * the GPU race and must be serialised by the caller.  Asynchronous: results are ready when the
+ * stream reaches them. */
+#define HF_NOALLOC_MAX_CELLS 16777216
+int hf_residual_noalloc(int64_t nx, int64_t ny, int64_t nz, const int32_t* periodic,
+                        const double* diag, const double* cx, const double* cy, const double* cz,
+                        const double* b, const double* x, double* r, double* norms2, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
