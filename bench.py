@@ -226,10 +226,12 @@ def timed_run(hf, torch, stream, itime0, steps):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("timed")
     e0.record(stream)
     st = hf.run(itime0, steps)
     e1.record(stream)
     e1.synchronize()
+    torch.cuda.nvtx.range_pop()
     return e0.elapsed_time(e1), st
 
 
