@@ -136,6 +136,7 @@ int validate_opts(const hf_solver_opts& o) {
     return set_err(HF_EARG, "the reference's recursive criterion is defined for the FP64 path");
   if (!(o.tol >= 0.0) || o.itmax < 1 || o.inner_itmax < 1 || o.max_refine < 1 || o.check_every < 1)
     return set_err(HF_EARG, "tol >= 0, itmax, inner_itmax, max_refine, check_every >= 1");
+  if (o.use_graph < 0 || o.use_graph > 2) return set_err(HF_EARG, "use_graph must be 0, 1 or 2");
   return HF_OK;
 }
 
@@ -213,10 +214,7 @@ int run_one_step(Ctx& c, int64_t itime) {
 // Capture one step as a CUDA graph: the solve loop is a WHILE node whose body selects, through a
 // SWITCH node, one inner CG iteration or one residual sweep; control kernels set the conditions
 // from the per-instance phase flags, so a step runs without any host round trip.
-int build_graph(Ctx& c) {
-  if (c.graph_exec && c.graph_precision == c.opts.precision && c.graph_criterion == c.opts.criterion)
-    return HF_OK;
-  drop_graph(c);
+int build_graph_cond(Ctx& c) {
   if (!c.d_ctrl) {
     int r = dalloc(c, &c.d_ctrl, 1);
     if (r) return r;
@@ -239,7 +237,7 @@ int build_graph(Ctx& c) {
     if (!chk(cudaGraphConditionalHandleCreate(&hw, g, 0, cudaGraphCondAssignDefault), "handle(while)")) break;
     if (!chk(cudaStreamBeginCaptureToGraph(cs, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed), "capture")) break;
     c.stream = cs;
-    chk(launch_graph_step_begin(c, c.d_ctrl), "step begin");
+    chk(launch_graph_step_begin(c, c.d_ctrl, 6), "step begin");
     chk(launch_rhs(c), "rhs");
     chk(launch_finalize(c, FIN_RHS, c.d_ctrl, hw, 1), "rhs finalize");
     chk(launch_residual(c, 0, c.d_ctrl, hw, 1), "residual init");
@@ -288,7 +286,7 @@ int build_graph(Ctx& c) {
       chk(cudaStreamEndCapture(cs2, &tmp), "end residual");
     }
     c.stream = cs;
-    chk(launch_graph_step_end(c, c.d_ctrl), "step end");
+    chk(launch_graph_step_end(c, c.d_ctrl, nullptr), "step end");
     cudaGraph_t outg = nullptr;
     chk(cudaStreamEndCapture(cs, &outg), "end capture");
     if (err.empty()) chk(cudaGraphInstantiate(&c.graph_exec, g, 0), "instantiate");
@@ -304,8 +302,61 @@ int build_graph(Ctx& c) {
     return set_err(HF_ECUDA, "graph capture: " + err);
   }
   c.graph = g;
+  return HF_OK;
+}
+
+// Capture one step with the persistent solve: step begin, RHS and its finalize, the cooperative
+// solve kernel (zeroing its control block first), step end.  Five kernels per step.
+int build_graph_persistent(Ctx& c) {
+  if (!c.d_ctrl) {
+    int r = dalloc(c, &c.d_ctrl, 1);
+    if (r) return r;
+    CU(cudaMemset(c.d_ctrl, 0, sizeof(CtrlState)));
+  }
+  if (solve_grid_blocks(c, c.opts.precision == HF_PREC_MIXED ? 1 : 0) < 1)
+    return set_err(HF_ECUDA, "no co-resident grid for the persistent solve kernel");
+  cudaStream_t cs = nullptr;
+  CU(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  cudaStream_t saved = c.stream;
+  cudaGraph_t g = nullptr;
+  std::string err;
+  auto chk = [&](cudaError_t e, const char* what) {
+    if (e != cudaSuccess && err.empty()) err = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaSuccess;
+  };
+  if (chk(cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed), "capture")) {
+    c.stream = cs;
+    chk(launch_graph_step_begin(c, c.d_ctrl, 5), "step begin");
+    chk(launch_rhs(c), "rhs");
+    chk(launch_finalize(c, FIN_RHS, nullptr, 0, 0), "rhs finalize");
+    chk(launch_solve(c), "persistent solve");
+    chk(launch_graph_step_end(c, c.d_ctrl, c.d_sctl), "step end");
+    chk(cudaStreamEndCapture(cs, &g), "end capture");
+    if (err.empty()) chk(cudaGraphInstantiate(&c.graph_exec, g, 0), "instantiate");
+  }
+  c.stream = saved;
+  cudaStreamDestroy(cs);
+  if (!err.empty()) {
+    if (c.graph_exec) cudaGraphExecDestroy(c.graph_exec);
+    c.graph_exec = nullptr;
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return set_err(HF_ECUDA, "graph capture: " + err);
+  }
+  c.graph = g;
+  return HF_OK;
+}
+
+int build_graph(Ctx& c) {
+  if (c.graph_exec && c.graph_precision == c.opts.precision &&
+      c.graph_criterion == c.opts.criterion && c.graph_mode == c.opts.use_graph)
+    return HF_OK;
+  drop_graph(c);
+  const int rc = c.opts.use_graph == 2 ? build_graph_cond(c) : build_graph_persistent(c);
+  if (rc) return rc;
   c.graph_precision = c.opts.precision;
   c.graph_criterion = c.opts.criterion;
+  c.graph_mode = c.opts.use_graph;
   return HF_OK;
 }
 
@@ -494,7 +545,11 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
   A.task_heat = d_task_heat;
   A.tasks = d_tasks;
   A.ntasks = c.ntasks;
-  ALLOC(A.partials, (size_t)c.ntasks * kNR);
+  ALLOC(A.partials, (size_t)c.ntasks * kNR * 2);
+  InstScal* d_scal2;
+  ALLOC(d_scal2, (size_t)count);
+  A.scal2 = d_scal2;
+  ALLOC(c.d_sctl, (size_t)1);
   ALLOC(A.counters, (size_t)count);
   ALLOC(c.d_bc, (size_t)count);
   A.inst = d_inst; A.scal = d_scal; A.tile_inst = d_tile_inst;
@@ -521,6 +576,8 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
 #define CK(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) return fail(set_err(HF_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_))); } while (0)
   CK(cudaMemsetAsync(A.counters, 0, sizeof(unsigned) * count, c.stream));
   CK(cudaMemsetAsync(d_scal, 0, sizeof(InstScal) * count, c.stream));
+  CK(cudaMemsetAsync(d_scal2, 0, sizeof(InstScal) * count, c.stream));
+  CK(cudaMemsetAsync(c.d_sctl, 0, sizeof(SolveCtl), c.stream));
   for (void* p : {(void*)A.diag, (void*)A.cx, (void*)A.cy, (void*)A.cz, (void*)c.asm_.kappa,
                   (void*)d_rho, (void*)d_hc, (void*)d_tau, (void*)A.rhoc, (void*)A.ccat,
                   (void*)A.bvec, (void*)A.tau_s, (void*)A.a64x, (void*)A.a64y, (void*)A.a64z,
@@ -764,6 +821,8 @@ int hf_run(hf_ctx* h, int64_t itime0, int64_t nsteps, hf_stats* stats) {
     for (int64_t k = 0; k < nsteps; ++k) CU(cudaGraphLaunch(c.graph_exec, c.stream));
     CU(cudaMemcpyAsync(&cs, c.d_ctrl, sizeof(cs), cudaMemcpyDeviceToHost, c.stream));
     CU(cudaStreamSynchronize(c.stream));
+    if (cs.guard_hit & 2)
+      return set_err(HF_EDEVICE, "persistent solve: a grid barrier wait reached its time limit");
     if (cs.guard_hit) return set_err(HF_EDEVICE, "captured solve loop reached its iteration bound");
     c.launches += cs.launches;
     done = nsteps;

@@ -40,6 +40,9 @@ struct Ctx {
   cudaGraphExec_t graph_exec = nullptr;
   cudaGraph_t graph = nullptr;
   CtrlState* d_ctrl = nullptr;
+  SolveCtl* d_sctl = nullptr;    // control block of the persistent solve kernel
+  int solve_blocks[2] = {0, 0};  // co-resident grid of the persistent solve (FP64, FP32)
+  int graph_mode = 0;            // use_graph value the graph was captured for
   int graph_precision = -1;     // options the graph was captured with
   int graph_criterion = -1;
   int64_t launches = 0;          // kernels launched on the device since creation

@@ -88,7 +88,7 @@ struct InstScal {
   int32_t status;       // bit k set: HF_ENAN_B + k raised
   int32_t devcheck;     // nonzero: a device-side consistency check failed
   int32_t tiny_pending; // x still needs the reference's +TINY (applied with the next update)
-  int32_t pad2;
+  int32_t phase;        // persistent solve: work of this instance in the current round (PH_*)
   int32_t role[4];      // temperature buffers: [0]=T^n, [1]=T^(n-1), [2]=x read, [3]=x write
   double sigma_prev;    // scale used by the previous residual sweep
   double last_err, last_relres;   // of the last finished step
@@ -105,6 +105,36 @@ struct CtrlState {
   int64_t launches;   // kernels the captured steps launched
 };
 
+// Phases of an instance inside the persistent solve kernel (one per grid-wide round).
+enum : int32_t {
+  PH_IDLE = 0,      // step finished (or failed): nothing to do
+  PH_START = 1,     // set by the step's begin: the next round forms the first residual
+  PH_RES_INIT = 2,  // r = S - H x0 (x0 + TINY), g, norms
+  PH_CG_P = 3,      // p = r + beta p                      (FP64 inner solve)
+  PH_CG_Q = 4,      // q = Ah p, p.q                        (FP64 inner solve)
+  PH_CG_PQ = 5,     // p = r + beta p and q = Ah p fused    (FP32 inner solve)
+  PH_CG_B = 6,      // y += alpha p, r -= alpha q, r.r
+  PH_XUPD = 7,      // x += sigma S^-1 y (+ TINY once)
+  PH_RES = 8        // true residual of the updated x
+};
+
+// Control block of one launch of the persistent solve kernel (zeroed before every launch).
+constexpr int kRoundLog = 64;                      // rounds whose end time is recorded
+struct SolveCtl {
+  unsigned count;          // blocks arrived at the current grid barrier
+  unsigned gen;            // barrier generation (release/acquire)
+  unsigned flag_acc;       // OR of the arriving blocks' "still active" flags
+  unsigned result[2];      // published OR, by barrier parity
+  unsigned next_task[2];   // dynamic task counters, by round parity
+  int32_t err;             // a barrier wait gave up (time limit): the launch was abandoned
+  int32_t guard_hit;       // the round bound was reached
+  int32_t pad;
+  int64_t rounds;          // rounds run
+  unsigned long long t_start;                 // %globaltimer at kernel start (ns)
+  unsigned long long t_round[kRoundLog];      // %globaltimer when round r's barrier opened
+  int32_t phase_log[kRoundLog];               // phase instance 0 ran in round r
+};
+
 // Options mirrored on the device.
 struct DevOpts {
   int32_t precision, criterion;
@@ -119,7 +149,8 @@ struct DevArrays {
   const InstDesc* inst;
   InstScal* scal;
   const int32_t* tile_inst;
-  double* partials;       // ntiles * kNR
+  double* partials;       // 2 * ntasks * kNR (the second half: odd rounds of the persistent solve)
+  InstScal* scal2;        // second copy of the scalars (odd rounds of the persistent solve)
   unsigned int* counters; // per instance, last-block detection
   DevOpts opts;
   // static
@@ -225,7 +256,14 @@ __device__ __forceinline__ void block_sum(double (&v)[NRV], double* smem /* [32*
 // block): on GB300 every FP64 warp instruction costs the slow FP64 pipe, so a shuffle tree in
 // all eight warps would cost more than the kernel's own arithmetic.
 template <int NRV>
+__device__ __forceinline__ void tile_store(double* dst, const double (&v)[NRV]);
+template <int NRV>
 __device__ __forceinline__ void tile_store(const DevArrays& A, int64_t tile, const double (&v)[NRV]) {
+  tile_store<NRV>(A.partials + tile * kNR, v);
+}
+// dst: the kNR partial slots of one task
+template <int NRV>
+__device__ __forceinline__ void tile_store(double* dst, const double (&v)[NRV]) {
   static_assert(NRV <= kNR, "reduction slots");
   __shared__ double stage[NRV][kBlock];
   __syncthreads();   // the previous tile of this block has finished reading the stage
@@ -240,7 +278,7 @@ __device__ __forceinline__ void tile_store(const DevArrays& A, int64_t tile, con
 #pragma unroll
       for (int w = 1; w < kBlock / 32; ++w) t += stage[k][lane + 32 * w];
       t = warp_sum(t);
-      if (lane == 0) A.partials[tile * kNR + k] = t;
+      if (lane == 0) dst[k] = t;
     }
   }
 }
@@ -330,10 +368,13 @@ cudaError_t launch_residual(Ctx& c, int mode, CtrlState* ctrl = nullptr,
 cudaError_t launch_inner_iteration(Ctx& c, int fp32, CtrlState* ctrl = nullptr,
                                    cudaGraphConditionalHandle hw = 0, int graph = 0);
 cudaError_t launch_step_end(Ctx& c);
+// Persistent solve: one cooperative launch runs the whole refinement loop of a step.
+cudaError_t launch_solve(Ctx& c);
+int solve_grid_blocks(Ctx& c, int fp32);
 cudaError_t launch_apply(Ctx& c, const double* x, double* y);
 cudaError_t launch_single(Ctx& c, int which);
-cudaError_t launch_graph_step_begin(Ctx& c, CtrlState* ctrl);
-cudaError_t launch_graph_step_end(Ctx& c, CtrlState* ctrl);
+cudaError_t launch_graph_step_begin(Ctx& c, CtrlState* ctrl, int launches_per_step);
+cudaError_t launch_graph_step_end(Ctx& c, CtrlState* ctrl, const SolveCtl* sctl);
 cudaError_t launch_ctrl_select(Ctx& c, CtrlState* ctrl, cudaGraphConditionalHandle hs,
                                cudaGraphConditionalHandle hw);
 // Finalize kernels: sum the tile partials of each instance and run the scalar epilogue of the

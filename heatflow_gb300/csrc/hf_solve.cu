@@ -60,6 +60,7 @@ __device__ __forceinline__ void begin_step(InstScal& s, int64_t itime) {
   s.x0flag = 0;
   s.tiny_pending = 0;
   s.err = 0.0;
+  s.phase = PH_START;
 }
 
 // Finished steps rotate the temperature roles: T^(n-1) <- T^n, T^n <- x (mod_evolve.f90:169-170).
@@ -152,7 +153,7 @@ __device__ __forceinline__ T plane_above(const TCell& c, int j, V v, int z) {
 }
 
 // FP32 block sum of one value into partial slot k of a task (one conversion per block).
-__device__ __forceinline__ void task_store_f(const DevArrays& A, int64_t task, int k, float v) {
+__device__ __forceinline__ void task_store_f(double* dst, int k, float v) {
   __shared__ float red[kBlock / 32];
   __syncthreads();
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -164,23 +165,64 @@ __device__ __forceinline__ void task_store_f(const DevArrays& A, int64_t task, i
     v = lane < kBlock / 32 ? red[lane] : 0.f;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
-    if (lane == 0) A.partials[task * kNR + k] = (double)v;
+    if (lane == 0) dst[k] = (double)v;
   }
 }
 
-// ---- FP64 true residual ------------------------------------------------------------------------
-// r = S - H x with x in the x-read buffer (INIT: x0 from the RHS kernel) or, after an update, in
-// the x-write buffer (the finalize then swaps the roles).  Writes g = -S^-1 r / sigma into the
-// inner residual (type TR).  FP64 work per cell: 7 FMA for S - Hx, 1 FMA for ||r||^2.
+// ---- task bodies ---------------------------------------------------------------------------------
+// Each body does one kernel's work for one task; the standalone kernels (host-polled loop, the
+// conditional-node graph, kernel timing) and the persistent solve kernel call the same bodies, so
+// every path computes the same bits.  Vectors that some phase of the persistent kernel writes
+// (temperature buffers, CG vectors) are read through plain pointers: within one launch they change
+// between rounds, so they must not be taken for read-only data.  The operator, S and the scalings
+// do not change during a solve and are read through const __restrict__ pointers.
+//
+// Loads are issued ahead of their use by hand (next plane of a stencil, four planes of an
+// element-wise pass), because the compiler may not move a load above a store to a vector it cannot
+// prove distinct.
+
+// x-neighbour loads of a column (offsets from the cell, or kNoNbr): lane 0 loads its west
+// neighbour, lane 31 its east neighbour, and a last column of a periodic axis its wrap; all other
+// x neighbours come from the adjacent lanes by shuffles.
+constexpr int kNoNbr = -2147483647 - 1;
+struct XEdge { int w, e; };
+__device__ __forceinline__ XEdge x_edges(const TCell& c) {
+  XEdge r{kNoNbr, kNoNbr};
+  if (!c.act(0)) return r;
+  const int x = c.x(0), nx = c.nx;
+  if (c.lane == 0) {
+    if (x > 0) r.w = -1;
+    else if (c.px && nx > 1) r.w = nx - 1;
+  }
+  if (x + 1 < nx) {
+    if (c.lane == 31) r.e = 1;
+  } else if (c.px && nx > 1) {
+    r.e = -(nx - 1);
+  }
+  return r;
+}
+// y-neighbour offsets (north = +y, south = -y) of an active column, or kNoNbr.
+__device__ __forceinline__ int y_north(const TCell& c) {
+  if (!c.act(0) || c.ny < 2) return kNoNbr;
+  if (c.y + 1 < c.ny) return c.nx;
+  return c.py ? -(c.ny - 1) * c.nx : kNoNbr;
+}
+__device__ __forceinline__ int y_south(const TCell& c) {
+  if (!c.act(0) || c.ny < 2) return kNoNbr;
+  if (c.y > 0) return -c.nx;
+  return c.py ? (c.ny - 1) * c.nx : kNoNbr;
+}
+
+// FP64 true residual of one task: r = S - H x with x in the x-read buffer (INIT: x0 from the RHS
+// kernel) or, after an update, in the x-write buffer (the epilogue then swaps the roles).  Writes
+// g = -S^-1 r / sigma into the inner residual (type TR).  FP64 work per cell: 7 FMA for S - Hx,
+// 1 FMA for ||r||^2.
 template <bool INIT, typename TR>
-__global__ void __launch_bounds__(kBlock) k_residual(DevArrays A) {
-  const int64_t task = blockIdx.x;
+__device__ __forceinline__ void res_task(const DevArrays& A, double* part, int64_t task,
+                                          const InstScal& s) {
   const TCell c = task_cell(A, task);
-  const InstScal& s = A.scal[c.inst];
-  if (!s.outer_active || s.inner_active) return;
-  if (INIT != (s.refine == 0)) return;
   const int64_t off = c.off;
-  const double* __restrict__ X = A.tbuf[INIT ? s.role[2] : s.role[3]] + off;
+  const double* X = A.tbuf[INIT ? s.role[2] : s.role[3]] + off;
   const double* __restrict__ diag = A.diag + off;
   const double* __restrict__ b = A.b + off;
   const double* __restrict__ cx = A.cx + off;
@@ -189,46 +231,47 @@ __global__ void __launch_bounds__(kBlock) k_residual(DevArrays A) {
   const double* __restrict__ rsum = A.rsum + off;
   const float* __restrict__ sinv32 = A.sinv32 + off;
   const double* __restrict__ sinv = A.sinv + off;
-  TR* __restrict__ R = Vec<TR>::r(A) + off;
+  TR* R = Vec<TR>::r(A) + off;
   const float isig = (float)(1.0 / s.sigma);
   // INIT: the residual of x0 + TINY (mod_evolve.f90:141) is r(x0) - TINY * H1
   const bool tiny = INIT && s.x0flag;
+  const bool act = c.act(0);
+  const int nz = c.nz, nxy = c.nxy, base = c.base(0);
+  const XEdge xe = x_edges(c);
+  const int yn = y_north(c), ys = y_south(c);
   auto xval = [&](int m) -> double { return X[m]; };
-  double xm[kXC], czm[kXC], xc[kXC];
-#pragma unroll
-  for (int j = 0; j < kXC; ++j) {
-    plane_below<double>(c, j, xval, cz, xm[j], czm[j]);
-    xc[j] = c.act(j) ? X[c.base(j) + c.z0 * c.nxy] : 0.0;
-  }
+  double xm, czm;
+  plane_below<double>(c, 0, xval, cz, xm, czm);
+  double xc = act ? X[base + c.z0 * nxy] : 0.0;
   double rr = 0.0, gg64 = 0.0;
   float gg = 0.f;
   for (int z = c.z0; z < c.z1; ++z) {
-    double xn[kXC], cxc[kXC], acc[kXC];
-#pragma unroll
-    for (int j = 0; j < kXC; ++j) {
-      const int l = c.base(j) + z * c.nxy;
-      const bool a = c.act(j);
-      xn[j] = plane_above<double>(c, j, xval, z);
-      cxc[j] = a ? cx[l] : 0.0;
-      acc[j] = 0.0;
-      if (a) {
-        acc[j] = fma(-diag[l], xc[j], b[l]);
-        if (tiny) acc[j] = fma(-kTiny, rsum[l], acc[j]);
-      }
+    const int l = base + z * nxy;
+    const double xn = plane_above<double>(c, 0, xval, z);
+    double cxc = 0.0, a = 0.0, xwl = 0.0, cxwl = 0.0, xel = 0.0;
+    double cyn = 0.0, xyn = 0.0, cys = 0.0, xys = 0.0, czc = 0.0;
+    if (act) {
+      cxc = cx[l];
+      a = fma(-diag[l], xc, b[l]);
+      if (tiny) a = fma(-kTiny, rsum[l], a);
+      if (xe.w != kNoNbr) { xwl = X[l + xe.w]; cxwl = cx[l + xe.w]; }
+      if (xe.e != kNoNbr) xel = X[l + xe.e];
+      if (yn != kNoNbr) { cyn = cy[l]; xyn = X[l + yn]; }
+      if (ys != kNoNbr) { cys = cy[l + ys]; xys = X[l + ys]; }
+      czc = cz[l];
     }
-#pragma unroll
-    for (int j = 0; j < kXC; ++j) {
-      const int l = c.base(j) + z * c.nxy;
-      double xw, cxw, xe;
-      x_nbrs(c, j, xc, cxc, l, xval, cx, xw, cxw, xe);
-      if (!c.act(j)) continue;
-      double a = acc[j];
-      a = fma(-cxc[j], xe, a);
+    const double up = __shfl_up_sync(kFull, xc, 1), cup = __shfl_up_sync(kFull, cxc, 1);
+    const double dn = __shfl_down_sync(kFull, xc, 1);
+    if (act) {
+      const double xw = c.lane > 0 ? up : xwl, cxw = c.lane > 0 ? cup : cxwl;
+      const double xeast = (c.x(0) + 1 < c.nx && c.lane < 31) ? dn : xel;
+      a = fma(-cxc, xeast, a);
       a = fma(-cxw, xw, a);
-      y_faces<double>(c, l, cy[l], xval, cy, [&](double cf, double xv) { a = fma(-cf, xv, a); });
-      if (c.nz > 1) {
-        a = fma(-cz[l], xn[j], a);
-        a = fma(-czm[j], xm[j], a);
+      if (yn != kNoNbr) a = fma(-cyn, xyn, a);
+      if (ys != kNoNbr) a = fma(-cys, xys, a);
+      if (nz > 1) {
+        a = fma(-czc, xn, a);
+        a = fma(-czm, xm, a);
       }
       rr = fma(a, a, rr);
       if (sizeof(TR) == 4) {             // mixed: g in FP32, scaled by 1/sigma
@@ -240,191 +283,278 @@ __global__ void __launch_bounds__(kBlock) k_residual(DevArrays A) {
         R[l] = (TR)g;
         gg64 = fma(g, g, gg64);
       }
-      czm[j] = cz[l];
     }
-#pragma unroll
-    for (int j = 0; j < kXC; ++j) { xm[j] = xc[j]; xc[j] = xn[j]; }
+    czm = czc;
+    xm = xc;
+    xc = xn;
   }
   if (sizeof(TR) == 4) {
-    task_store_f(A, task, 1, gg);
+    task_store_f(part + task * kNR, 1, gg);
     const double v[1] = {rr};
-    tile_store<1>(A, task, v);
+    tile_store<1>(part + task * kNR, v);
   } else {
     const double v[2] = {rr, gg64};
-    tile_store<2>(A, task, v);
+    tile_store<2>(part + task * kNR, v);
   }
 }
 
-// ---- solution update: x_new = x + sigma S^-1 y (+ TINY once) -----------------------------------
+// Solution update of one task: x_new = x + sigma S^-1 y (+ TINY once).
 template <typename TY>
-__global__ void __launch_bounds__(kBlock) k_xupdate(DevArrays A) {
-  const TCell c = task_cell(A, blockIdx.x);
-  const InstScal& s = A.scal[c.inst];
-  if (!s.outer_active || s.inner_active || s.refine == 0) return;
+__device__ __forceinline__ void xupd_task(const DevArrays& A, double* part, int64_t task,
+                                          const InstScal& s) {
+  const TCell c = task_cell(A, task);
+  if (!c.act(0)) return;
   const int64_t off = c.off;
-  const double* __restrict__ XR = A.tbuf[s.role[2]] + off;
-  double* __restrict__ XW = A.tbuf[s.role[3]] + off;
-  const TY* __restrict__ Y = Vec<TY>::y(A) + off;
+  const double* XR = A.tbuf[s.role[2]] + off;
+  double* XW = A.tbuf[s.role[3]] + off;
+  const TY* Y = Vec<TY>::y(A) + off;
   const double* __restrict__ sinv = A.sinv + off;
   const float* __restrict__ sinv32 = A.sinv32 + off;
   const bool use_y = s.iter > 0;
   const bool tiny = s.tiny_pending != 0;
   const float sig = (float)s.sigma_prev;
-  for (int z = c.z0; z < c.z1; ++z) {
+  const int nxy = c.nxy, base = c.base(0);
+  for (int z0 = c.z0; z0 < c.z1; z0 += 4) {
+    double xv[4];
+    TY yv[4];
 #pragma unroll
-    for (int j = 0; j < kXC; ++j) {
-      if (!c.act(j)) continue;
-      const int l = c.base(j) + z * c.nxy;
-      double x = XR[l];
+    for (int u = 0; u < 4; ++u) {
+      const int l = base + (z0 + u) * nxy;
+      xv[u] = 0.0; yv[u] = TY(0);
+      if (z0 + u < c.z1) {
+        xv[u] = XR[l];
+        if (use_y) yv[u] = Y[l];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (z0 + u >= c.z1) continue;
+      const int l = base + (z0 + u) * nxy;
+      double x = xv[u];
       if (tiny) x = x + kTiny;
       if (use_y) {
-        if (sizeof(TY) == 8) x = fma(sinv[l], (double)Y[l], x);   // sigma = 1 on the FP64 path
-        else x = x + f32_to_f64(sig * sinv32[l] * (float)Y[l]);
+        if (sizeof(TY) == 8) x = fma(sinv[l], (double)yv[u], x);   // sigma = 1 on the FP64 path
+        else x = x + f32_to_f64(sig * sinv32[l] * (float)yv[u]);
       }
       XW[l] = x;
     }
   }
 }
 
-// ---- inner CG on Ah (type T) -------------------------------------------------------------------
-// The direction p_k = r + beta p_(k-1) (p_0 = r) is written to the buffer of parity k; the
-// previous direction is read from the other buffer of the pair.
+// Direction update of one task: p_k = r + beta p_(k-1) (p_0 = r) into the buffer of parity k.
 template <typename T>
-__global__ void __launch_bounds__(kBlock) k_cg_p(DevArrays A) {
-  const TCell c = task_cell(A, blockIdx.x);
-  const InstScal& s = A.scal[c.inst];
-  if (!s.inner_active) return;
+__device__ __forceinline__ void cgp_task(const DevArrays& A, double* part, int64_t task,
+                                          const InstScal& s) {
+  const TCell c = task_cell(A, task);
+  if (!c.act(0)) return;
   const int64_t k = s.iter;
   const bool first = (k == 0);
   const T beta = (T)s.beta;
-  const T* __restrict__ R = Vec<T>::r(A) + c.off;
-  const T* __restrict__ Po = Vec<T>::pb(A, k + 1) + c.off;
-  T* __restrict__ Pn = Vec<T>::pb(A, k) + c.off;
+  const T* R = Vec<T>::r(A) + c.off;
+  const T* Po = Vec<T>::pb(A, k + 1) + c.off;
+  T* Pn = Vec<T>::pb(A, k) + c.off;
+  const int nxy = c.nxy, base = c.base(0);
+  for (int z0 = c.z0; z0 < c.z1; z0 += 4) {
+    T rv[4], pv[4];
 #pragma unroll
-  for (int j = 0; j < kXC; ++j) {
-    if (!c.act(j)) continue;
-#pragma unroll 4
-    for (int z = c.z0; z < c.z1; ++z) {
-      const int l = c.base(j) + z * c.nxy;
-      Pn[l] = first ? R[l] : fma(beta, Po[l], R[l]);
+    for (int u = 0; u < 4; ++u) {
+      const int l = base + (z0 + u) * nxy;
+      rv[u] = T(0); pv[u] = T(0);
+      if (z0 + u < c.z1) {
+        rv[u] = R[l];
+        if (!first) pv[u] = Po[l];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (z0 + u >= c.z1) continue;
+      Pn[base + (z0 + u) * nxy] = first ? rv[u] : fma(beta, pv[u], rv[u]);
     }
   }
 }
 
-// k_cg_spmv: q = Ah p_k and p_k.q.  One column per thread; the operands of plane z+1 (its
-// coefficients, y neighbours and plane z+2) are loaded while plane z is computed, so each
-// thread keeps two planes of loads in flight.
-template <typename T>
-__global__ void __launch_bounds__(kBlock) k_cg_spmv(DevArrays A) {
+// q = Ah p and p.q for one task.  FUSED: p is formed on the fly from r and the previous direction
+// (p = r + beta p_old, the value the direction update would store) and written out beside q, so
+// one pass replaces two.  One column per thread; the operands of plane z+1 (its coefficients, y
+// neighbours, x-edge neighbours and plane z+2) are loaded while plane z is computed.
+template <typename T, bool FUSED>
+__device__ __forceinline__ void spmv_task(const DevArrays& A, double* part, int64_t task,
+                                          const InstScal& s) {
   static_assert(kXC == 1, "one column per thread");
-  const int64_t task = blockIdx.x;
   const TCell c = task_cell(A, task);
-  const InstScal& s = A.scal[c.inst];
-  if (!s.inner_active) return;
   const int64_t off = c.off;
-  const T* __restrict__ P = Vec<T>::pb(A, s.iter) + off;
-  T* __restrict__ Q = Vec<T>::q(A) + off;
+  const int64_t k = s.iter;
+  const bool first = !FUSED || (k == 0);
+  const T beta = (T)s.beta;
+  const T* Src = FUSED ? Vec<T>::r(A) + off : Vec<T>::pb(A, k) + off;   // r, or p itself
+  const T* Po = Vec<T>::pb(A, k + 1) + off;
+  T* Pn = Vec<T>::pb(A, k) + off;
+  T* Q = Vec<T>::q(A) + off;
   const T* __restrict__ ax = Vec<T>::ax(A) + off;
   const T* __restrict__ ay = Vec<T>::ay(A) + off;
   const T* __restrict__ az = Vec<T>::az(A) + off;
   const bool act = c.act(0);
-  const int nx = c.nx, ny = c.ny, nxy = c.nxy, base = c.base(0);
-  auto pv = [&](int m) -> T { return P[m]; };
-  // operands of one plane: own value, its faces, y neighbours (+ south face)
-  struct Plane { T p, axc, ayc, azc, pnn, ps, ays; };
+  const int nx = c.nx, nz = c.nz, nxy = c.nxy, base = c.base(0);
+  const XEdge xe = x_edges(c);
+  const int yn = y_north(c), ys = y_south(c);
+  const bool east_shfl = act && (c.x(0) + 1 < nx) && c.lane < 31;
+  // raw operands of one direction value: p = first ? a : beta * b + a
+  struct RP { T a, b; };
+  auto ld = [&](int m) -> RP { return RP{Src[m], first ? T(0) : Po[m]}; };
+  auto pval = [&](const RP& v) -> T { return first ? v.a : fma(beta, v.b, v.a); };
+  struct Plane { RP own, n, s, w, e; T axc, ayc, azc, ays, axw; };
+  const RP z0v{T(0), T(0)};
   auto load = [&](int z, Plane& o) {
-    o = Plane{T(0), T(0), T(0), T(0), T(0), T(0), T(0)};
-    if (!act || z >= c.nz) return;
-    const int l = base + z * nxy;
-    o.p = P[l]; o.axc = ax[l]; o.ayc = ay[l]; o.azc = az[l];
-    if (ny > 1) {
-      if (c.y + 1 < ny) o.pnn = P[l + nx];
-      else if (c.py) o.pnn = P[l - (ny - 1) * nx];
-      if (c.y > 0) { o.ps = P[l - nx]; o.ays = ay[l - nx]; }
-      else if (c.py) { o.ps = P[l + (ny - 1) * nx]; o.ays = ay[l + (ny - 1) * nx]; }
+    o.own = z0v; o.n = z0v; o.s = z0v; o.w = z0v; o.e = z0v;
+    o.axc = T(0); o.ayc = T(0); o.azc = T(0); o.ays = T(0); o.axw = T(0);
+    if (!act) return;
+    if (z >= nz) {                      // above the top plane: the periodic wrap, or nothing
+      if (c.pz && nz > 1) o.own = ld(base);
+      return;
     }
+    const int l = base + z * nxy;
+    o.own = ld(l);
+    o.axc = ax[l]; o.ayc = ay[l]; o.azc = az[l];
+    if (yn != kNoNbr) o.n = ld(l + yn);
+    if (ys != kNoNbr) { o.s = ld(l + ys); o.ays = ay[l + ys]; }
+    if (xe.w != kNoNbr) { o.w = ld(l + xe.w); o.axw = ax[l + xe.w]; }
+    if (xe.e != kNoNbr) o.e = ld(l + xe.e);
   };
-  T pm, azm;
-  plane_below<T>(c, 0, pv, az, pm, azm);
+  // plane below the task (z0 - 1, or the periodic wrap to nz - 1)
+  T pm = T(0), azm = T(0);
+  if (act && nz > 1) {
+    int lb = -1;
+    if (c.z0 > 0) lb = base + (c.z0 - 1) * nxy;
+    else if (c.pz) lb = base + (nz - 1) * nxy;
+    if (lb >= 0) { pm = pval(ld(lb)); azm = az[lb]; }
+  }
   Plane cur, nxt;
   load(c.z0, cur);
   T pq = T(0);
   for (int z = c.z0; z < c.z1; ++z) {
-    // plane z+1 (wrapping to 0 on a periodic z axis) is both the next plane and the z+ value
-    if (z + 1 < c.nz) load(z + 1, nxt);
-    else {
-      nxt = Plane{T(0), T(0), T(0), T(0), T(0), T(0), T(0)};
-      if (act && c.pz && c.nz > 1) nxt.p = P[base];
-    }
+    if (z + 1 < nz) load(z + 1, nxt);
+    else load(nz, nxt);
     const int l = base + z * nxy;
-    T pcv[kXC] = {cur.p};
-    T axv[kXC] = {cur.axc};
-    T pw, axw, pe;
-    x_nbrs(c, 0, pcv, axv, l, pv, ax, pw, axw, pe);
+    const T pc = pval(cur.own);
+    const T up = __shfl_up_sync(kFull, pc, 1);
+    const T cup = __shfl_up_sync(kFull, cur.axc, 1);
+    const T dn = __shfl_down_sync(kFull, pc, 1);
     if (act) {
-      T acc = cur.p;
+      const T pw = c.lane > 0 ? up : pval(cur.w);
+      const T axw = c.lane > 0 ? cup : cur.axw;
+      const T pe = east_shfl ? dn : pval(cur.e);
+      T acc = pc;
       acc = fma(cur.axc, pe, acc);
       acc = fma(axw, pw, acc);
-      if (ny > 1) {
-        acc = fma(cur.ayc, cur.pnn, acc);
-        acc = fma(cur.ays, cur.ps, acc);
+      if (c.ny > 1) {
+        acc = fma(cur.ayc, pval(cur.n), acc);
+        acc = fma(cur.ays, pval(cur.s), acc);
       }
-      if (c.nz > 1) {
-        acc = fma(cur.azc, nxt.p, acc);
+      if (nz > 1) {
+        acc = fma(cur.azc, pval(nxt.own), acc);
         acc = fma(azm, pm, acc);
       }
+      if (FUSED) Pn[l] = pc;
       Q[l] = acc;
-      pq = fma(cur.p, acc, pq);
+      pq = fma(pc, acc, pq);
     }
-    pm = cur.p; azm = cur.azc;
+    pm = pc; azm = cur.azc;
     cur = nxt;
   }
   if (sizeof(T) == 4) {
-    task_store_f(A, task, 0, (float)pq);
+    task_store_f(part + task * kNR, 0, (float)pq);
   } else {
     const double v[1] = {(double)pq};
-    tile_store<1>(A, task, v);
+    tile_store<1>(part + task * kNR, v);
   }
 }
 
-// k_cg_upd: y += alpha p, r -= alpha q, r.r (and the unscaled ||r||^2 for the reference rule)
+// y += alpha p, r -= alpha q, r.r (and the unscaled ||r||^2 for the reference rule) of one task.
 template <typename T>
-__global__ void __launch_bounds__(kBlock) k_cg_upd(DevArrays A) {
-  const int64_t task = blockIdx.x;
+__device__ __forceinline__ void upd_task(const DevArrays& A, double* part, int64_t task,
+                                          const InstScal& s) {
   const TCell c = task_cell(A, task);
-  const InstScal& s = A.scal[c.inst];
-  if (!s.inner_active) return;
   const DevOpts& o = A.opts;
   const bool weighted = (o.criterion == HF_STOP_RECURSIVE);
   const T alpha = (T)s.alpha;
   const bool first = (s.iter == 0);
   const int64_t off = c.off;
-  T* __restrict__ Y = Vec<T>::y(A) + off;
-  T* __restrict__ R = Vec<T>::r(A) + off;
-  const T* __restrict__ P = Vec<T>::pb(A, s.iter) + off;
-  const T* __restrict__ Q = Vec<T>::q(A) + off;
+  T* Y = Vec<T>::y(A) + off;
+  T* R = Vec<T>::r(A) + off;
+  const T* P = Vec<T>::pb(A, s.iter) + off;
+  const T* Q = Vec<T>::q(A) + off;
   const double* __restrict__ diag = A.diag + off;
+  const bool act = c.act(0);
+  const int nxy = c.nxy, base = c.base(0);
   T rr = T(0);
   double rw = 0.0;
-  for (int z = c.z0; z < c.z1; ++z) {
+  if (act) {
+    for (int z0 = c.z0; z0 < c.z1; z0 += 4) {
+      T pv[4], qv[4], rv[4], yv[4];
 #pragma unroll
-    for (int j = 0; j < kXC; ++j) {
-      if (!c.act(j)) continue;
-      const int l = c.base(j) + z * c.nxy;
-      const T pv = P[l];
-      Y[l] = first ? alpha * pv : fma(alpha, pv, Y[l]);
-      const T rv = fma(-alpha, Q[l], R[l]);
-      R[l] = rv;
-      rr = fma(rv, rv, rr);
-      if (weighted) rw = fma(-diag[l] * (double)rv, (double)rv, rw);
+      for (int u = 0; u < 4; ++u) {
+        const int l = base + (z0 + u) * nxy;
+        pv[u] = T(0); qv[u] = T(0); rv[u] = T(0); yv[u] = T(0);
+        if (z0 + u < c.z1) {
+          pv[u] = P[l]; qv[u] = Q[l]; rv[u] = R[l];
+          if (!first) yv[u] = Y[l];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (z0 + u >= c.z1) continue;
+        const int l = base + (z0 + u) * nxy;
+        Y[l] = first ? alpha * pv[u] : fma(alpha, pv[u], yv[u]);
+        const T r = fma(-alpha, qv[u], rv[u]);
+        R[l] = r;
+        rr = fma(r, r, rr);
+        if (weighted) rw = fma(-diag[l] * (double)r, (double)r, rw);
+      }
     }
   }
   if (sizeof(T) == 4 && !weighted) {
-    task_store_f(A, task, 0, (float)rr);
+    task_store_f(part + task * kNR, 0, (float)rr);
   } else {
     const double v[2] = {(double)rr, rw};
-    tile_store<2>(A, task, v);
+    tile_store<2>(part + task * kNR, v);
   }
+}
+
+// ---- standalone kernels (host-polled loop, conditional-node graph, kernel timing) --------------
+template <bool INIT, typename TR>
+__global__ void __launch_bounds__(kBlock) k_residual(DevArrays A) {
+  const InstScal& s = A.scal[A.tasks[blockIdx.x].x];
+  if (!s.outer_active || s.inner_active) return;
+  if (INIT != (s.refine == 0)) return;
+  res_task<INIT, TR>(A, A.partials, blockIdx.x, s);
+}
+
+template <typename TY>
+__global__ void __launch_bounds__(kBlock) k_xupdate(DevArrays A) {
+  const InstScal& s = A.scal[A.tasks[blockIdx.x].x];
+  if (!s.outer_active || s.inner_active || s.refine == 0) return;
+  xupd_task<TY>(A, A.partials, blockIdx.x, s);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_cg_p(DevArrays A) {
+  const InstScal& s = A.scal[A.tasks[blockIdx.x].x];
+  if (!s.inner_active) return;
+  cgp_task<T>(A, A.partials, blockIdx.x, s);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_cg_spmv(DevArrays A) {
+  const InstScal& s = A.scal[A.tasks[blockIdx.x].x];
+  if (!s.inner_active) return;
+  spmv_task<T, false>(A, A.partials, blockIdx.x, s);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kBlock) k_cg_upd(DevArrays A) {
+  const InstScal& s = A.scal[A.tasks[blockIdx.x].x];
+  if (!s.inner_active) return;
+  upd_task<T>(A, A.partials, blockIdx.x, s);
 }
 
 // ---- finalize kernels: one block per instance sums the task partials in task order ----------
@@ -461,10 +591,7 @@ __device__ void epi_rhs_diag(const DevArrays& A, int inst, const double* tot) {
 
 // Epilogue of a residual sweep: convergence test and set-up of the next inner solve.
 template <bool INIT>
-__device__ void epi_residual(const DevArrays& A, int inst, const double* tot) {
-  InstScal& s = A.scal[inst];
-  const InstDesc& G = A.inst[inst];
-  const DevOpts& o = A.opts;
+__device__ void epi_residual_s(InstScal& s, const InstDesc& G, const DevOpts& o, const double* tot) {
   if (!INIT) {
     const int t = s.role[2]; s.role[2] = s.role[3]; s.role[3] = t;
     s.tiny_pending = 0;
@@ -520,8 +647,7 @@ __device__ void epi_residual(const DevArrays& A, int inst, const double* tot) {
 }
 
 
-__device__ void epi_spmv(const DevArrays& A, int inst, const double* tot) {
-  InstScal& s = A.scal[inst];
+__device__ void epi_spmv_s(InstScal& s, const double* tot) {
   s.pq = tot[0];
   if (tot[0] > 0.0 && isfinite(tot[0])) {
     s.alpha = s.rho / tot[0];
@@ -533,9 +659,7 @@ __device__ void epi_spmv(const DevArrays& A, int inst, const double* tot) {
 
 
 template <typename T>
-__device__ void epi_upd(const DevArrays& A, int inst, const double* tot) {
-  InstScal& s = A.scal[inst];
-  const DevOpts& o = A.opts;
+__device__ void epi_upd_s(InstScal& s, const DevOpts& o, const double* tot) {
   const bool weighted = (o.criterion == HF_STOP_RECURSIVE);
   const double rho_new = tot[0];
   s.beta = rho_new / s.rho;
@@ -562,6 +686,16 @@ __device__ void epi_upd(const DevArrays& A, int inst, const double* tot) {
   if (stop) s.inner_active = 0;
 }
 
+
+template <bool INIT>
+__device__ void epi_residual(const DevArrays& A, int inst, const double* tot) {
+  epi_residual_s<INIT>(A.scal[inst], A.inst[inst], A.opts, tot);
+}
+__device__ void epi_spmv(const DevArrays& A, int inst, const double* tot) { epi_spmv_s(A.scal[inst], tot); }
+template <typename T>
+__device__ void epi_upd(const DevArrays& A, int inst, const double* tot) {
+  epi_upd_s<T>(A.scal[inst], A.opts, tot);
+}
 
 // Whether instance s took part in the producing kernel (the producers' own entry tests).
 template <int KIND>
@@ -624,20 +758,24 @@ __global__ void __launch_bounds__(256) k_finalize(DevArrays A, CtrlState* ctrl,
 }
 
 // ---- captured step: control kernels of the conditional nodes -----------------------------------
-__global__ void k_graph_step_begin(DevArrays A, CtrlState* ctrl) {
+__global__ void k_graph_step_begin(DevArrays A, CtrlState* ctrl, int launches_per_step) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i == 0) {
     ctrl->loop_iter = 0;
-    ctrl->launches += 6;   // step begin, RHS + finalize, initial residual + finalize, step end
+    ctrl->launches += launches_per_step;   // the step's kernels outside the solve loop
   }
   if (i < A.ninst) begin_step(A.scal[i], ctrl->itime);
 }
 
-// One block: every instance rotates, then the step counter advances.
-__global__ void k_graph_step_end(DevArrays A, CtrlState* ctrl) {
+// One block: every instance rotates, then the step counter advances.  A persistent solve that
+// gave up (barrier time limit or round bound) is recorded in ctrl->guard_hit, which stays set.
+__global__ void k_graph_step_end(DevArrays A, CtrlState* ctrl, const SolveCtl* sctl) {
   for (int64_t i = threadIdx.x; i < A.ninst; i += blockDim.x) end_step(A.scal[i]);
   __syncthreads();
-  if (threadIdx.x == 0) ctrl->itime += 1;
+  if (threadIdx.x == 0) {
+    ctrl->itime += 1;
+    if (sctl && (sctl->err || sctl->guard_hit)) ctrl->guard_hit |= sctl->err ? 2 : 1;
+  }
 }
 
 // Branch of the solve loop body: 0 = one inner CG iteration, 1 = update + residual, 2 = nothing.
@@ -661,6 +799,258 @@ __global__ void k_ctrl_select(DevArrays A, CtrlState* ctrl, cudaGraphConditional
   ctrl->launches += 1 + (branch == 0u ? 5 : (branch == 1u ? 3 : 0));
   if (branch == 2u) cudaGraphSetConditional(hw, 0u);
   cudaGraphSetConditional(hs, branch);
+}
+
+// ---- persistent solve ------------------------------------------------------------------------
+// One cooperative launch runs a step's whole refinement loop.  Work proceeds in grid-wide rounds:
+// in round r every task does the work of its instance's current phase (PH_*) and writes its
+// partial sums to the round's partial buffer; a grid barrier closes the round.  At the start of
+// the next round, each block that picks up a task of an instance first runs that instance's
+// epilogue itself: it sums the instance's task partials of the previous round in task order (the
+// same order as the finalize kernels, so every block obtains the same bits) and updates the
+// scalars (alpha, beta, convergence, next phase) in shared memory.  Scalars and partials are
+// double-buffered by round parity, so the blocks that read round r's values never race with the
+// writes of round r + 1; only the block that picks up an instance's first task (its owner for the
+// round) stores the new scalars.  Tasks are handed out by an atomic counter per round, in
+// increasing order, so a block meets an instance's tasks in one run.  The kernel returns when a
+// barrier reports that no owner has work left.
+//
+// Termination: every barrier wait is bounded in time (kBarrierWaitNs); a block that gives up
+// records SolveCtl::err and returns, and the blocks still waiting see the flag and return too.
+// The number of rounds is bounded by `limit`.  Co-residency of all blocks, which the barrier
+// needs, is guaranteed by the cooperative launch (the grid never exceeds the occupancy bound).
+constexpr unsigned long long kBarrierWaitNs = 4000000000ull;
+
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Grid barrier that also ORs one flag per block.  Returns false if the wait gave up.
+__device__ bool grid_barrier_or(SolveCtl* ctl, unsigned nblocks, unsigned flag, int64_t round,
+                                unsigned& any) {
+  __shared__ unsigned s_any;
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const unsigned g = ld_acquire_u32(&ctl->gen);   // cannot advance before this block arrives
+    if (flag) atomicOr(&ctl->flag_acc, 1u);
+    __threadfence();
+    const unsigned arrived = atomicAdd(&ctl->count, 1u);
+    int ok = 1;
+    if (arrived == nblocks - 1) {
+      ctl->result[(g + 1) & 1] = atomicExch(&ctl->flag_acc, 0u);
+      ctl->next_task[(round + 1) & 1] = 0u;       // counter of the next round (last used at r-1)
+      if (round < kRoundLog) ctl->t_round[round] = gtimer();
+      ctl->rounds = round + 1;
+      ctl->count = 0u;
+      __threadfence();
+      st_release_u32(&ctl->gen, g + 1);
+    } else {
+      const unsigned long long t0 = gtimer();
+      unsigned polls = 0;
+      while (ld_acquire_u32(&ctl->gen) == g) {
+        if (*(volatile int*)&ctl->err) { ok = 0; break; }
+        if ((++polls & 255u) == 0u && (gtimer() - t0 > kBarrierWaitNs || polls > (1u << 27))) {
+          atomicExch(&ctl->err, 1);
+          ok = 0;
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+    s_any = ok ? *(volatile unsigned*)&ctl->result[(g + 1) & 1] : 0u;
+    s_ok = ok;
+  }
+  __syncthreads();
+  any = s_any;
+  return s_ok != 0;
+}
+
+template <typename T>
+__device__ __forceinline__ int32_t phase_after(const InstScal& s) {
+  if (!s.outer_active) return PH_IDLE;
+  if (s.inner_active) return sizeof(T) == 4 ? PH_CG_PQ : PH_CG_P;
+  return PH_XUPD;
+}
+
+// Epilogue of instance `inst` at the start of a round: previous scalars from `sin`, the previous
+// round's partials from `prev`; result in `sh` (all threads see it on return).  The owner block
+// (the one holding the instance's first task) stores it to `sout` and raises its active flag.
+template <typename T>
+__device__ void round_epilogue(const DevArrays& A, int inst, const InstScal* sin, InstScal* sout,
+                               const double* prev, int64_t task, InstScal& sh, double* red,
+                               int& s_flag) {
+  constexpr int kWords = (int)(sizeof(InstScal) / 8);
+  static_assert(sizeof(InstScal) % 8 == 0 && kWords <= kBlock, "scalar copy");
+  if ((int)threadIdx.x < kWords)
+    reinterpret_cast<unsigned long long*>(&sh)[threadIdx.x] =
+        __ldcg(reinterpret_cast<const unsigned long long*>(sin + inst) + threadIdx.x);
+  __syncthreads();
+  const int32_t ph = sh.phase;
+  const InstDesc& d = A.inst[inst];
+  const int nr = (ph == PH_RES_INIT || ph == PH_RES || ph == PH_CG_B) ? 2
+                 : ((ph == PH_CG_Q || ph == PH_CG_PQ) ? 1 : 0);
+  double acc[2] = {0.0, 0.0};
+  if (nr > 0) {
+    for (int64_t t = threadIdx.x; t < d.ntask; t += blockDim.x) {
+      acc[0] += __ldcg(&prev[(d.task0 + t) * kNR]);
+      acc[1] += __ldcg(&prev[(d.task0 + t) * kNR + 1]);
+    }
+    block_sum<2>(acc, red);
+  }
+  if (threadIdx.x == 0) {
+    switch (ph) {
+      case PH_START: sh.phase = sh.outer_active ? PH_RES_INIT : PH_IDLE; break;
+      case PH_RES_INIT:
+        epi_residual_s<true>(sh, d, A.opts, acc);
+        sh.phase = phase_after<T>(sh);
+        break;
+      case PH_RES:
+        epi_residual_s<false>(sh, d, A.opts, acc);
+        sh.phase = phase_after<T>(sh);
+        break;
+      case PH_CG_P: sh.phase = PH_CG_Q; break;
+      case PH_CG_Q:
+      case PH_CG_PQ:
+        epi_spmv_s(sh, acc);
+        sh.phase = sh.inner_active ? PH_CG_B : phase_after<T>(sh);
+        break;
+      case PH_CG_B:
+        epi_upd_s<T>(sh, A.opts, acc);
+        sh.phase = phase_after<T>(sh);
+        break;
+      case PH_XUPD: sh.phase = PH_RES; break;
+      default: sh.phase = PH_IDLE; break;
+    }
+    if (task == d.task0) {
+      sout[inst] = sh;
+      if (sh.phase != PH_IDLE) s_flag = 1;
+    }
+  }
+  __syncthreads();
+}
+
+template <typename T>
+__device__ __forceinline__ void round_task(const DevArrays& A, double* part, int64_t task,
+                                           const InstScal& s) {
+  switch (s.phase) {
+    case PH_RES_INIT: res_task<true, T>(A, part, task, s); break;
+    case PH_RES: res_task<false, T>(A, part, task, s); break;
+    case PH_CG_P: cgp_task<T>(A, part, task, s); break;
+    case PH_CG_Q: spmv_task<T, false>(A, part, task, s); break;
+    case PH_CG_PQ: spmv_task<T, true>(A, part, task, s); break;
+    case PH_CG_B: upd_task<T>(A, part, task, s); break;
+    case PH_XUPD: xupd_task<T>(A, part, task, s); break;
+    default: break;
+  }
+}
+
+// Blocks per SM: FP32 4 (64 registers), FP64 3 (its stencil needs ~85 registers).
+template <typename T>
+__global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 4 : 3)
+    k_solve(DevArrays A, SolveCtl* ctl, int64_t limit) {
+  __shared__ InstScal sh;
+  __shared__ double red[32 * 2];
+  __shared__ unsigned s_task;
+  __shared__ int s_flag;
+  const unsigned G = gridDim.x;
+  const unsigned nt = (unsigned)A.ntasks;
+  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->t_start = gtimer();
+  int64_t r = 0;
+  for (;; ++r) {
+    if (r >= limit) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) ctl->guard_hit = 1;
+      break;
+    }
+    double* part = A.partials + (r & 1) * (int64_t)nt * kNR;
+    const double* prev = A.partials + ((r + 1) & 1) * (int64_t)nt * kNR;
+    const InstScal* sin = (r & 1) ? A.scal2 : A.scal;
+    InstScal* sout = (r & 1) ? A.scal : A.scal2;
+    if (threadIdx.x == 0) {
+      s_flag = 0;
+      s_task = atomicAdd(&ctl->next_task[r & 1], 1u);
+    }
+    __syncthreads();
+    unsigned t = s_task;
+    int cur = -1;
+    while (t < nt) {
+      // the next task index is fetched now and consumed after this task (latency hidden)
+      unsigned nxt = 0u;
+      if (threadIdx.x == 0) nxt = atomicAdd(&ctl->next_task[r & 1], 1u);
+      const int inst = A.tasks[t].x;
+      if (inst != cur) {
+        cur = inst;
+        round_epilogue<T>(A, inst, sin, sout, prev, t, sh, red, s_flag);
+        if (inst == 0 && t == 0 && threadIdx.x == 0 && r < kRoundLog) ctl->phase_log[r] = sh.phase;
+      }
+      if (sh.phase != PH_IDLE) round_task<T>(A, part, t, sh);
+      __syncthreads();                               // sh and s_task are free
+      if (threadIdx.x == 0) s_task = nxt;
+      __syncthreads();
+      t = s_task;
+    }
+    unsigned any = 0;
+    if (!grid_barrier_or(ctl, G, (unsigned)s_flag, r, any)) return;
+    if (!any) break;
+  }
+  // the scalars of the last round live in the buffer of parity (r + 1): bring them to A.scal
+  if (((r + 1) & 1) == 1 && r < limit) {
+    for (int64_t i = blockIdx.x; i < A.ninst; i += G) {
+      if ((int)threadIdx.x < (int)(sizeof(InstScal) / 8))
+        reinterpret_cast<unsigned long long*>(A.scal + i)[threadIdx.x] =
+            __ldcg(reinterpret_cast<const unsigned long long*>(A.scal2 + i) + threadIdx.x);
+    }
+  }
+}
+
+// Largest co-resident grid of the persistent solve (cooperative launch bound), capped by tasks.
+int solve_grid_blocks(Ctx& c, int fp32) {
+  int& cached = c.solve_blocks[fp32 ? 1 : 0];
+  if (cached > 0) return cached;
+  int per_sm = 0, nsm = 0;
+  cudaError_t e = fp32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve<float>, kBlock, 0)
+                       : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve<double>, kBlock, 0);
+  if (e != cudaSuccess) return -1;
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c.device) != cudaSuccess) return -1;
+  int64_t g = (int64_t)per_sm * nsm;
+  if (g > c.ntasks) g = c.ntasks;
+  if (g < 1) return -1;
+  cached = (int)g;
+  return cached;
+}
+
+// Zero the control block, then launch the persistent solve cooperatively on the context stream.
+cudaError_t launch_solve(Ctx& c) {
+  const bool fp32 = c.opts.precision == HF_PREC_MIXED;
+  const int g = solve_grid_blocks(c, fp32 ? 1 : 0);
+  if (g < 1) return cudaErrorInvalidConfiguration;
+  cudaError_t e = cudaMemsetAsync(c.d_sctl, 0, sizeof(SolveCtl), c.stream);
+  if (e != cudaSuccess) return e;
+  const int64_t per = fp32 ? c.opts.inner_itmax : c.opts.itmax;
+  const int64_t limit = (int64_t)(c.opts.max_refine + 3) * (3 * per + 6) + 8;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)g);
+  cfg.blockDim = dim3(kBlock);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = c.stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  if (fp32) return cudaLaunchKernelEx(&cfg, k_solve<float>, c.A, c.d_sctl, limit);
+  return cudaLaunchKernelEx(&cfg, k_solve<double>, c.A, c.d_sctl, limit);
 }
 
 // ---- launchers ---------------------------------------------------------------------------------
@@ -711,12 +1101,13 @@ cudaError_t launch_inner_iteration(Ctx& c, int fp32, CtrlState* ctrl,
   return launch_finalize(c, FIN_UPD, ctrl, hw, graph);
 }
 
-cudaError_t launch_graph_step_begin(Ctx& c, CtrlState* ctrl) {
-  k_graph_step_begin<<<(unsigned)((c.ninst + 127) / 128), 128, 0, c.stream>>>(c.A, ctrl);
+cudaError_t launch_graph_step_begin(Ctx& c, CtrlState* ctrl, int launches_per_step) {
+  k_graph_step_begin<<<(unsigned)((c.ninst + 127) / 128), 128, 0, c.stream>>>(c.A, ctrl,
+                                                                               launches_per_step);
   return cudaGetLastError();
 }
-cudaError_t launch_graph_step_end(Ctx& c, CtrlState* ctrl) {
-  k_graph_step_end<<<1, 256, 0, c.stream>>>(c.A, ctrl);
+cudaError_t launch_graph_step_end(Ctx& c, CtrlState* ctrl, const SolveCtl* sctl) {
+  k_graph_step_end<<<1, 256, 0, c.stream>>>(c.A, ctrl, sctl);
   return cudaGetLastError();
 }
 cudaError_t launch_ctrl_select(Ctx& c, CtrlState* ctrl, cudaGraphConditionalHandle hs,

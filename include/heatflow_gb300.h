@@ -96,7 +96,10 @@ typedef struct hf_solver_opts {
   int32_t inner_itmax;  /* mixed: max FP32 CG iterations per inner solve */
   int32_t max_refine;   /* mixed: max FP64 refinement sweeps per step */
   int32_t check_every;  /* iterations launched between host convergence polls */
-  int32_t use_graph;    /* 1: hf_run captures the step loop in one CUDA graph */
+  int32_t use_graph;    /* hf_run's step: 0 = kernels launched and polled by the host;
+                           1 = a CUDA graph per step whose solve is one persistent cooperative
+                           kernel (grid-wide rounds, no host round trip);
+                           2 = a CUDA graph per step with conditional WHILE/SWITCH nodes */
 } hf_solver_opts;
 
 typedef struct hf_stats {

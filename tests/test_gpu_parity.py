@@ -177,11 +177,14 @@ def test_layered_slab_vs_oracle(cuda_lib, precision):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_batch_equals_single(cuda_lib, precision):
+@pytest.mark.parametrize("g", [0, 1])
+def test_batch_equals_single(cuda_lib, precision, g):
+    """A batch of uneven grids (host loop or one persistent launch per step) gives each grid's
+    own single-grid result bit for bit."""
     rng = np.random.default_rng(5)
     probs = [random_instance(rng, lo=5, hi=12) for _ in range(4)]
     kw = dict(precision=precision, criterion="true", tol=1e-10)
-    with HeatFlow(probs, **kw) as hf:
+    with HeatFlow(probs, use_graph=g, **kw) as hf:
         hf.initial_evolve()
         hf.run(1, 6)
         Tb, _ = hf.get_state()
@@ -250,28 +253,48 @@ def test_full_size_residual_property(cuda_lib, precision):
     dict(precision="mixed", criterion="true", tol=1e-10),
 ])
 def test_graph_equals_host_loop(cuda_lib, opts):
-    """The captured step (CUDA graph, conditional WHILE/SWITCH nodes, no host round trips)
-    runs the same kernels as the host-driven loop: identical fields and iteration counts."""
+    """Both captured steps -- the persistent cooperative solve kernel (use_graph=1) and the
+    conditional WHILE/SWITCH graph (use_graph=2) -- run the same task bodies and reductions as the
+    host-driven loop: identical fields and iteration counts on a batch of uneven grids."""
     rng = np.random.default_rng(11)
     probs = [point_source_cube(10)] + [random_instance(rng, lo=6, hi=14) for _ in range(3)]
     out = []
-    for g in (0, 1):
+    for g in (0, 1, 2):
         with HeatFlow(probs, use_graph=g, **opts) as hf:
             hf.initial_evolve()
             st = hf.run(1, 8)
             out.append((hf.get_state(), st))
-    (a, sa), (b, sb) = out
-    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
-    for k in ("iterations", "inner_iterations", "refinements", "unconverged"):
-        assert sa[k] == sb[k], k
-    assert sb["kernel_launches"] > 0
+    a, sa = out[0]
+    for b, sb in out[1:]:
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+        for k in ("iterations", "inner_iterations", "refinements", "unconverged"):
+            assert sa[k] == sb[k], k
+        assert sb["kernel_launches"] > 0
+    assert out[1][1]["kernel_launches"] == 5 * 8          # persistent: 5 kernels per step
 
 
-def test_graph_nan_stops(cuda_lib):
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_persistent_full_size_equals_host_loop(cuda_lib, precision):
+    """256^3 layered slab, 3 steps: the persistent solve (one cooperative launch per step over
+    4096 tasks) gives the host loop's fields bit for bit."""
+    prob = layered_slab(256)
+    out = []
+    for g in (0, 1):
+        with HeatFlow(prob, precision=precision, criterion="true", tol=1e-10, use_graph=g) as hf:
+            hf.initial_evolve()
+            st = hf.run(1, 3)
+            out.append((hf.get_state()[0], st))
+    assert np.array_equal(out[0][0], out[1][0])
+    assert out[0][1]["inner_iterations"] == out[1][1]["inner_iterations"]
+    assert out[1][1]["last_true_relres"] <= 1e-10
+
+
+@pytest.mark.parametrize("g", [1, 2])
+def test_graph_nan_stops(cuda_lib, g):
     prob = point_source_cube(4, icattaneo=0)
     tp, tpp = prob.initial_state()
     tp[3] = np.nan
-    with HeatFlow(prob, use_graph=1) as hf:
+    with HeatFlow(prob, use_graph=g) as hf:
         hf.set_state(tp, tpp)
         with pytest.raises(abi.HeatFlowError) as e:
             hf.run(1, 3)
