@@ -57,6 +57,7 @@ class HfSolverOpts(C.Structure):
         ("precision", C.c_int32), ("criterion", C.c_int32), ("tol", C.c_double),
         ("itmax", C.c_int64), ("inner_tol", C.c_double), ("inner_itmax", C.c_int32),
         ("max_refine", C.c_int32), ("check_every", C.c_int32), ("use_graph", C.c_int32),
+        ("task_depth", C.c_int32),
     ]
 
 
@@ -108,6 +109,8 @@ _SIGNATURES = {
     "hf_assemble_coo": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, _ip, _ip, _dp, _ip, _ip]),
     "hf_time_kernel": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp]),
     "hf_measure_fp_rates": (C.c_int, [_dp, _dp]),
+    "hf_solve_profile": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_int64),
+                                   C.POINTER(C.c_int32), _dp]),
     "hf_set_state_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "hf_residual_noalloc": (C.c_int, [C.c_int64, C.c_int64, C.c_int64, C.POINTER(C.c_int32),
                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -119,7 +122,12 @@ _SIGNATURES = {
                                         C.c_void_p]),
 }
 HF_KERNEL_RHS, HF_KERNEL_RESIDUAL, HF_KERNEL_CG_P, HF_KERNEL_CG_SPMV, HF_KERNEL_CG_UPDATE = 0, 1, 2, 3, 4
-HF_KERNEL_XUPDATE = 5
+HF_KERNEL_XUPDATE, HF_KERNEL_SOLVE, HF_KERNEL_CG_PQ = 5, 6, 7
+(HF_PHASE_IDLE, HF_PHASE_START, HF_PHASE_RES_INIT, HF_PHASE_CG_P, HF_PHASE_CG_Q, HF_PHASE_CG_PQ,
+ HF_PHASE_CG_B, HF_PHASE_XUPD, HF_PHASE_RES) = range(9)
+PHASE_NAMES = {HF_PHASE_IDLE: "idle", HF_PHASE_START: "start", HF_PHASE_RES_INIT: "res_init",
+               HF_PHASE_CG_P: "cg_p", HF_PHASE_CG_Q: "cg_q", HF_PHASE_CG_PQ: "cg_pq",
+               HF_PHASE_CG_B: "cg_b", HF_PHASE_XUPD: "xupd", HF_PHASE_RES: "res"}
 
 _lib = None
 

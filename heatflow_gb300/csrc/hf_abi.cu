@@ -76,6 +76,7 @@ void hf_default_opts(hf_solver_opts* o) {
   o->max_refine = 20;
   o->check_every = 2;
   o->use_graph = 0;
+  o->task_depth = 0;
 }
 
 }  // extern "C"
@@ -137,6 +138,8 @@ int validate_opts(const hf_solver_opts& o) {
   if (!(o.tol >= 0.0) || o.itmax < 1 || o.inner_itmax < 1 || o.max_refine < 1 || o.check_every < 1)
     return set_err(HF_EARG, "tol >= 0, itmax, inner_itmax, max_refine, check_every >= 1");
   if (o.use_graph < 0 || o.use_graph > 2) return set_err(HF_EARG, "use_graph must be 0, 1 or 2");
+  if (o.task_depth != 0 && (o.task_depth < kMinTaskDepth || o.task_depth > 1024))
+    return set_err(HF_EARG, "task_depth must be 0 (default) or 4..1024");
   return HF_OK;
 }
 
@@ -418,6 +421,40 @@ int download_padded(Ctx& c, T* dst, const T* src) {
   return HF_OK;
 }
 
+int effective_depth(const hf_solver_opts& o) { return o.task_depth > 0 ? o.task_depth : kZC; }
+
+// (Re)build the task table for a task depth: per instance, kTX x kTY column tiles x `depth`
+// planes, ordered (z, y, x); uploads the table and the instance descriptors, recomputes the
+// per-task heater flags and forgets what depended on the old table (captured graph, grid size).
+int build_tasks(Ctx& c, int depth) {
+  std::vector<int4> tasks;
+  for (int64_t i = 0; i < c.ninst; ++i) {
+    InstDesc& d = c.h_inst[i];
+    const int nbx = (d.nx + kTX - 1) / kTX, nby = (d.ny + kTY - 1) / kTY;
+    const int nbz = (d.nz + depth - 1) / depth;
+    d.task0 = (int64_t)tasks.size();
+    d.ntask = nbx * nby * nbz;
+    d.zc = depth;
+    for (int bz = 0; bz < nbz; ++bz)
+      for (int by = 0; by < nby; ++by)
+        for (int bx = 0; bx < nbx; ++bx)
+          tasks.push_back(make_int4((int)i, bx * kTX, by * kTY, bz * depth));
+  }
+  if ((int64_t)tasks.size() > c.ntasks_cap) return set_err(HF_EARG, "task depth below the minimum");
+  c.ntasks = (int64_t)tasks.size();
+  c.A.ntasks = c.ntasks;
+  CU(cudaMemcpyAsync(const_cast<int4*>(c.A.tasks), tasks.data(), sizeof(int4) * tasks.size(),
+                     cudaMemcpyHostToDevice, c.stream));
+  CU(cudaMemcpyAsync(const_cast<InstDesc*>(c.A.inst), c.h_inst.data(), sizeof(InstDesc) * c.ninst,
+                     cudaMemcpyHostToDevice, c.stream));
+  CU(launch_task_heat(c));
+  CU(cudaStreamSynchronize(c.stream));
+  c.depth = depth;
+  c.solve_blocks[0] = c.solve_blocks[1] = 0;
+  drop_graph(c);
+  return HF_OK;
+}
+
 int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* opts, hf_ctx** out) {
   if (!probs || count < 1 || !out) return set_err(HF_EARG, "null problem/out or count < 1");
   *out = nullptr;
@@ -514,19 +551,14 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
   }
   c.ncells = off;
   c.ntiles = tiles;
-  // tasks of the step kernels: kTX x kTY columns x kZC planes, ordered (z, y, x) per instance
-  std::vector<int4> tasks;
+  // task buffers are sized for the shallowest task depth; the table itself is built later
+  c.ntasks_cap = 0;
   for (int64_t i = 0; i < count; ++i) {
-    InstDesc& d = c.h_inst[i];
-    const int nbx = (d.nx + kTX - 1) / kTX, nby = (d.ny + kTY - 1) / kTY, nbz = (d.nz + kZC - 1) / kZC;
-    d.task0 = (int64_t)tasks.size();
-    d.ntask = nbx * nby * nbz;
-    for (int bz = 0; bz < nbz; ++bz)
-      for (int by = 0; by < nby; ++by)
-        for (int bx = 0; bx < nbx; ++bx)
-          tasks.push_back(make_int4((int)i, bx * kTX, by * kTY, bz * kZC));
+    const InstDesc& d = c.h_inst[i];
+    c.ntasks_cap += (int64_t)((d.nx + kTX - 1) / kTX) * ((d.ny + kTY - 1) / kTY) *
+                    ((d.nz + kMinTaskDepth - 1) / kMinTaskDepth);
   }
-  c.ntasks = (int64_t)tasks.size();
+  c.ntasks = c.ntasks_cap;
   const size_t N = (size_t)c.ncells;
   // ---- device memory
   DevArrays& A = c.A;
@@ -545,10 +577,7 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
   A.task_heat = d_task_heat;
   A.tasks = d_tasks;
   A.ntasks = c.ntasks;
-  ALLOC(A.partials, (size_t)c.ntasks * kNR * 2);
-  InstScal* d_scal2;
-  ALLOC(d_scal2, (size_t)count);
-  A.scal2 = d_scal2;
+  ALLOC(A.partials, (size_t)c.ntasks * kNR);
   ALLOC(c.d_sctl, (size_t)1);
   ALLOC(A.counters, (size_t)count);
   ALLOC(c.d_bc, (size_t)count);
@@ -576,7 +605,6 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
 #define CK(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) return fail(set_err(HF_ECUDA, std::string(#call) + ": " + cudaGetErrorString(e_))); } while (0)
   CK(cudaMemsetAsync(A.counters, 0, sizeof(unsigned) * count, c.stream));
   CK(cudaMemsetAsync(d_scal, 0, sizeof(InstScal) * count, c.stream));
-  CK(cudaMemsetAsync(d_scal2, 0, sizeof(InstScal) * count, c.stream));
   CK(cudaMemsetAsync(c.d_sctl, 0, sizeof(SolveCtl), c.stream));
   for (void* p : {(void*)A.diag, (void*)A.cx, (void*)A.cy, (void*)A.cz, (void*)c.asm_.kappa,
                   (void*)d_rho, (void*)d_hc, (void*)d_tau, (void*)A.rhoc, (void*)A.ccat,
@@ -594,21 +622,6 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
   CK(cudaMemcpyAsync(d_inst, c.h_inst.data(), sizeof(InstDesc) * count, cudaMemcpyHostToDevice, c.stream));
   CK(cudaMemcpyAsync(c.d_bc, c.h_bc.data(), sizeof(InstBC) * count, cudaMemcpyHostToDevice, c.stream));
   CK(cudaMemcpyAsync(d_tile_inst, tile_inst.data(), sizeof(int32_t) * tiles, cudaMemcpyHostToDevice, c.stream));
-  CK(cudaMemcpy(d_tasks, tasks.data(), sizeof(int4) * (size_t)c.ntasks, cudaMemcpyHostToDevice));
-  {   // tasks holding a heated cell (the RHS skips heater loads elsewhere)
-    std::vector<int8_t> th((size_t)c.ntasks, 0);
-    for (int64_t i = 0; i < count; ++i) {
-      const InstDesc& d = c.h_inst[i];
-      if (!probs[i].iheater) continue;
-      const int nbx = (d.nx + kTX - 1) / kTX, nby = (d.ny + kTY - 1) / kTY;
-      for (int64_t k = 0; k < d.n; ++k) {
-        if (probs[i].iheater[k] == 0) continue;
-        const int64_t ix = k % d.nx, iy = (k / d.nx) % d.ny, iz = k / ((int64_t)d.nx * d.ny);
-        th[(size_t)(d.task0 + ((iz / kZC) * nby + iy / kTY) * nbx + ix / kTX)] = 1;
-      }
-    }
-    CK(cudaMemcpy(d_task_heat, th.data(), (size_t)c.ntasks, cudaMemcpyHostToDevice));
-  }
   // per-cell inputs into the padded layout
   std::vector<int8_t> icase;
   for (int64_t i = 0; i < count; ++i) {
@@ -637,6 +650,10 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
       CK(cudaMemcpyAsync(A.icase + d.off, icase.data(), d.n, cudaMemcpyHostToDevice, c.stream));
       CK(cudaStreamSynchronize(c.stream));
     }
+  }
+  {
+    const int r = build_tasks(c, effective_depth(o));
+    if (r) return fail(r);
   }
   CK(launch_props(c, d_rho, d_hc, d_tau, d_em));
   CK(launch_assemble(c));
@@ -713,6 +730,7 @@ int hf_set_opts(hf_ctx* h, const hf_solver_opts* opts) {
   h->c.opts = *opts;
   h->c.A.opts = dev_opts(*opts);
   drop_graph(h->c);   // captured kernels hold the options by value
+  if (effective_depth(*opts) != h->c.depth) return build_tasks(h->c, effective_depth(*opts));
   return HF_OK;
 }
 
@@ -844,9 +862,71 @@ int hf_run(hf_ctx* h, int64_t itime0, int64_t nsteps, hf_stats* stats) {
   return first_error(c);
 }
 
-int hf_time_kernel(hf_ctx* h, int which, int reps, double* ms) {
-  if (!h || !ms || reps < 1 || which < HF_KERNEL_RHS || which > HF_KERNEL_XUPDATE)
+}  // extern "C"
+
+namespace {
+// Time the persistent solve alone: each repetition begins the next step and forms its RHS
+// (untimed), then times one solve with CUDA events on the context stream.  T^n and T^(n-1) are
+// not modified (the step's end, which rotates them, does not run); the scalars are restored.
+int time_solve(Ctx& c, int reps, double* ms) {
+  if (!c.state_set) return set_err(HF_ESTATE, "hf_set_state must be called first");
+  int rc = sync_scal(c);
+  if (rc) return rc;
+  std::vector<InstScal> saved(c.h_scal, c.h_scal + c.ninst);
+  const int64_t itime = saved[0].itime + 1;
+  cudaEvent_t e0, e1;
+  CU(cudaEventCreate(&e0));
+  CU(cudaEventCreate(&e1));
+  double total = 0.0;
+  for (int r = 0; r < reps; ++r) {
+    CU(launch_step_begin(c, itime, 0));
+    CU(launch_rhs(c));
+    CU(launch_finalize(c, FIN_RHS, nullptr, 0, 0));
+    CU(cudaEventRecord(e0, c.stream));
+    CU(launch_solve(c));
+    CU(cudaEventRecord(e1, c.stream));
+    CU(cudaEventSynchronize(e1));
+    float t = 0.f;
+    CU(cudaEventElapsedTime(&t, e0, e1));
+    total += t;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  SolveCtl sc;
+  CU(cudaMemcpy(&sc, c.d_sctl, sizeof(sc), cudaMemcpyDeviceToHost));
+  std::memcpy(c.h_scal, saved.data(), sizeof(InstScal) * c.ninst);
+  if ((rc = push_scal(c))) return rc;
+  if (sc.err) return set_err(HF_EDEVICE, "persistent solve: a grid barrier wait reached its time limit");
+  if (sc.guard_hit) return set_err(HF_EDEVICE, "persistent solve reached its round bound");
+  *ms = total / reps;
+  return HF_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int hf_solve_profile(hf_ctx* h, int64_t cap, int64_t* rounds, int32_t* phases, double* round_us) {
+  if (!h || !rounds || cap < 0 || (cap > 0 && (!phases || !round_us)))
     return set_err(HF_EARG, "bad arguments");
+  Ctx& c = h->c;
+  SolveCtl sc;
+  CU(cudaStreamSynchronize(c.stream));
+  CU(cudaMemcpy(&sc, c.d_sctl, sizeof(sc), cudaMemcpyDeviceToHost));
+  *rounds = sc.rounds;
+  const int64_t n = std::min<int64_t>(std::min<int64_t>(sc.rounds, cap), kRoundLog);
+  unsigned long long prev = sc.t_start;
+  for (int64_t r = 0; r < n; ++r) {
+    phases[r] = sc.phase_log[r];
+    round_us[r] = (double)(sc.t_round[r] - prev) * 1e-3;
+    prev = sc.t_round[r];
+  }
+  return HF_OK;
+}
+
+int hf_time_kernel(hf_ctx* h, int which, int reps, double* ms) {
+  if (!h || !ms || reps < 1 || which < HF_KERNEL_RHS || which > HF_KERNEL_CG_PQ)
+    return set_err(HF_EARG, "bad arguments");
+  if (which == HF_KERNEL_SOLVE) return time_solve(h->c, reps, ms);
   Ctx& c = h->c;
   if (!c.state_set) return set_err(HF_ESTATE, "hf_set_state must be called first");
   int rc = sync_scal(c);
@@ -855,9 +935,11 @@ int hf_time_kernel(hf_ctx* h, int which, int reps, double* ms) {
   std::vector<InstScal> phase = saved;
   for (auto& s : phase) {
     s.outer_active = 1;
-    s.inner_active = (which >= HF_KERNEL_CG_P && which <= HF_KERNEL_CG_UPDATE) ? 1 : 0;
+    const bool cg = (which >= HF_KERNEL_CG_P && which <= HF_KERNEL_CG_UPDATE) || which == HF_KERNEL_CG_PQ;
+    s.inner_active = cg ? 1 : 0;
     s.refine = 1;
-    s.iter = (which == HF_KERNEL_CG_P || which == HF_KERNEL_CG_UPDATE) ? 1 : (which == HF_KERNEL_RESIDUAL ? 1 : 0);
+    s.iter = (which == HF_KERNEL_CG_P || which == HF_KERNEL_CG_UPDATE || which == HF_KERNEL_CG_PQ ||
+              which == HF_KERNEL_RESIDUAL) ? 1 : 0;
     s.status = 0;
     s.rho = 1.0; s.gg0 = 1.0; s.beta = 0.5; s.alpha = 0.5; s.eta = 0.0;
     s.sigma = 1.0; s.sigma_prev = 1.0;

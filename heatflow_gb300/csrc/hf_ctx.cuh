@@ -25,6 +25,8 @@ struct Ctx {
   bool own_stream = false;
   int64_t ninst = 0, ncells = 0, ntiles = 0;
   int64_t ntasks = 0;            // blocks of the step kernels
+  int64_t ntasks_cap = 0;        // task buffers' capacity (shallowest task depth)
+  int depth = 0;                 // task depth of the current table
   std::vector<InstDesc> h_inst;
   std::vector<InstBC> h_bc;
   std::vector<int64_t> h_tile0;

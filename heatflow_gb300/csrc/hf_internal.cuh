@@ -31,9 +31,11 @@ constexpr int kCellsPerThread = 4;
 constexpr int kTile = kBlock * kCellsPerThread;   // cells per tile (one block per tile)
 constexpr int kNR = 8;
 // Step kernels work on tasks: a block of 32 x kTY threads owns kXC*32 x kTY columns of one
-// instance (one warp per row; lane L holds columns x0 + L + 32 j, j < kXC) and marches kZC planes
-// along z.  (kXC > 1 trades occupancy for per-thread parallelism; on GB300 kXC = 1 is faster.)
+// instance (one warp per row; lane L holds columns x0 + L + 32 j, j < kXC) and marches the task
+// depth (InstDesc::zc planes, an option; kZC by default) along z.  (kXC > 1 trades occupancy for
+// per-thread parallelism; on GB300 kXC = 1 is faster.)
 constexpr int kXC = 1, kTX = 32 * kXC, kTY = 8, kZC = 16;
+constexpr int kMinTaskDepth = 4;   // task buffers are sized for the shallowest task depth
 // InstScal::status bit: some S was NaN; the failing vector is found by the diagnosis kernel.
 constexpr int kStatusRhsNan = 1 << 16;                       // reduction slots per tile
 // Instances are laid out at multiples of kTile cells, so tile t covers cells
@@ -57,7 +59,7 @@ struct InstDesc {
   double mean_sinv;   // mean of 1/sqrt|H_II| (scaling of the FP32 inner right-hand side)
   int64_t task0;      // first task of the step kernels
   int32_t ntask;      // tasks of this instance
-  int32_t pad1;
+  int32_t zc;         // planes per task (the task depth)
 };
 
 // Per-instance mutable scalars (device memory).
@@ -107,15 +109,15 @@ struct CtrlState {
 
 // Phases of an instance inside the persistent solve kernel (one per grid-wide round).
 enum : int32_t {
-  PH_IDLE = 0,      // step finished (or failed): nothing to do
-  PH_START = 1,     // set by the step's begin: the next round forms the first residual
-  PH_RES_INIT = 2,  // r = S - H x0 (x0 + TINY), g, norms
-  PH_CG_P = 3,      // p = r + beta p                      (FP64 inner solve)
-  PH_CG_Q = 4,      // q = Ah p, p.q                        (FP64 inner solve)
-  PH_CG_PQ = 5,     // p = r + beta p and q = Ah p fused    (FP32 inner solve)
-  PH_CG_B = 6,      // y += alpha p, r -= alpha q, r.r
-  PH_XUPD = 7,      // x += sigma S^-1 y (+ TINY once)
-  PH_RES = 8        // true residual of the updated x
+  PH_IDLE = HF_PHASE_IDLE,          // step finished (or failed): nothing to do
+  PH_START = HF_PHASE_START,        // reserved
+  PH_RES_INIT = HF_PHASE_RES_INIT,  // r = S - H x0 (x0 + TINY), g, norms
+  PH_CG_P = HF_PHASE_CG_P,          // p = r + beta p                      (FP64 inner solve)
+  PH_CG_Q = HF_PHASE_CG_Q,          // q = Ah p, p.q                        (FP64 inner solve)
+  PH_CG_PQ = HF_PHASE_CG_PQ,        // p = r + beta p and q = Ah p fused    (FP32 inner solve)
+  PH_CG_B = HF_PHASE_CG_B,          // y += alpha p, r -= alpha q, r.r
+  PH_XUPD = HF_PHASE_XUPD,          // x += sigma S^-1 y (+ TINY once)
+  PH_RES = HF_PHASE_RES             // true residual of the updated x
 };
 
 // Control block of one launch of the persistent solve kernel (zeroed before every launch).
@@ -123,9 +125,7 @@ constexpr int kRoundLog = 64;                      // rounds whose end time is r
 struct SolveCtl {
   unsigned count;          // blocks arrived at the current grid barrier
   unsigned gen;            // barrier generation (release/acquire)
-  unsigned flag_acc;       // OR of the arriving blocks' "still active" flags
-  unsigned result[2];      // published OR, by barrier parity
-  unsigned next_task[2];   // dynamic task counters, by round parity
+  unsigned result[2];      // "some instance has work", published by barrier parity
   int32_t err;             // a barrier wait gave up (time limit): the launch was abandoned
   int32_t guard_hit;       // the round bound was reached
   int32_t pad;
@@ -149,8 +149,7 @@ struct DevArrays {
   const InstDesc* inst;
   InstScal* scal;
   const int32_t* tile_inst;
-  double* partials;       // 2 * ntasks * kNR (the second half: odd rounds of the persistent solve)
-  InstScal* scal2;        // second copy of the scalars (odd rounds of the persistent solve)
+  double* partials;       // ntasks * kNR partial sums, one fixed slot range per task
   unsigned int* counters; // per instance, last-block detection
   DevOpts opts;
   // static
@@ -331,7 +330,7 @@ __device__ __forceinline__ TCell task_cell(const DevArrays& A, int64_t task) {
   c.x0 = t.y;
   c.y = t.z + (int)(threadIdx.x >> 5);
   c.z0 = t.w;
-  c.z1 = min(t.w + kZC, d.nz);
+  c.z1 = min(t.w + d.zc, d.nz);
   return c;
 }
 
@@ -357,6 +356,7 @@ cudaError_t launch_coo(Ctx& c, int64_t instance, int64_t* d_counts, int64_t* d_i
                        int64_t* d_jcol, double* d_val, int64_t* d_pos, int phase);
 cudaError_t launch_step_begin(Ctx& c, int64_t itime, int first_of_run);
 cudaError_t launch_rhs(Ctx& c);
+cudaError_t launch_task_heat(Ctx& c);
 cudaError_t launch_rhs_parts(Ctx& c, double* B, double* Q, double* Qd, double* Sc);
 cudaError_t launch_rhs_diagnose(Ctx& c);
 cudaError_t launch_adj_rhs(Ctx& c, const double* g, const double* l1, const double* l2, double* out);

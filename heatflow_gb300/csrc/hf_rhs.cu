@@ -254,6 +254,24 @@ __global__ void k_adj_grad(DevArrays A, const InstBC* bcs, const double* kappa, 
   }
 }
 
+// Per task: does some cell hold a heater (any heater case != 0)?  The RHS skips the heater loads of
+// the other tasks.
+__global__ void k_task_heat(DevArrays A, int8_t* flag) {
+  const int64_t task = blockIdx.x;
+  const TCell c = task_cell(A, task);
+  int any = 0;
+  if (A.icase && c.act(0)) {
+    for (int z = c.z0; z < c.z1; ++z) any |= A.icase[c.off + c.base(0) + (int64_t)z * c.nxy] != 0;
+  }
+  any = __syncthreads_or(any);
+  if (threadIdx.x == 0) flag[task] = (int8_t)(any ? 1 : 0);
+}
+
+cudaError_t launch_task_heat(Ctx& c) {
+  k_task_heat<<<(unsigned)c.ntasks, kBlock, 0, c.stream>>>(c.A, const_cast<int8_t*>(c.A.task_heat));
+  return cudaGetLastError();
+}
+
 cudaError_t launch_adj_rhs(Ctx& c, const double* g, const double* l1, const double* l2, double* out) {
   k_adj_rhs<<<(unsigned)((c.ncells + 255) / 256), 256, 0, c.stream>>>(c.A, g, l1, l2, out);
   return cudaGetLastError();

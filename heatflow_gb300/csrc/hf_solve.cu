@@ -60,7 +60,7 @@ __device__ __forceinline__ void begin_step(InstScal& s, int64_t itime) {
   s.x0flag = 0;
   s.tiny_pending = 0;
   s.err = 0.0;
-  s.phase = PH_START;
+  s.phase = s.outer_active ? PH_RES_INIT : PH_IDLE;   // the persistent solve's first round
 }
 
 // Finished steps rotate the temperature roles: T^(n-1) <- T^n, T^n <- x (mod_evolve.f90:169-170).
@@ -315,15 +315,20 @@ __device__ __forceinline__ void xupd_task(const DevArrays& A, double* part, int6
   const float sig = (float)s.sigma_prev;
   const int nxy = c.nxy, base = c.base(0);
   for (int z0 = c.z0; z0 < c.z1; z0 += 4) {
-    double xv[4];
+    double xv[4], sv[4];
+    float sv32[4];
     TY yv[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int l = base + (z0 + u) * nxy;
-      xv[u] = 0.0; yv[u] = TY(0);
+      xv[u] = 0.0; yv[u] = TY(0); sv[u] = 0.0; sv32[u] = 0.f;
       if (z0 + u < c.z1) {
         xv[u] = XR[l];
-        if (use_y) yv[u] = Y[l];
+        if (use_y) {
+          yv[u] = Y[l];
+          if (sizeof(TY) == 8) sv[u] = sinv[l];
+          else sv32[u] = sinv32[l];
+        }
       }
     }
 #pragma unroll
@@ -333,8 +338,8 @@ __device__ __forceinline__ void xupd_task(const DevArrays& A, double* part, int6
       double x = xv[u];
       if (tiny) x = x + kTiny;
       if (use_y) {
-        if (sizeof(TY) == 8) x = fma(sinv[l], (double)yv[u], x);   // sigma = 1 on the FP64 path
-        else x = x + f32_to_f64(sig * sinv32[l] * (float)yv[u]);
+        if (sizeof(TY) == 8) x = fma(sv[u], (double)yv[u], x);   // sigma = 1 on the FP64 path
+        else x = x + f32_to_f64(sig * sv32[u] * (float)yv[u]);
       }
       XW[l] = x;
     }
@@ -520,6 +525,161 @@ __device__ __forceinline__ void upd_task(const DevArrays& A, double* part, int64
   }
 }
 
+// ---- FP32 p + SpMV on 16-byte vectors ---------------------------------------------------------
+// For grids whose rows hold a multiple of 4 cells (every row then starts 16-byte aligned; the
+// instances start at multiples of 1024 cells) each thread owns 4 consecutive x cells and works on
+// float4 vectors: a quarter of the scalar version's instructions per cell.  Block layout over a
+// 32 x 8 column tile: four z-groups of 64 threads, each marching its quarter of the task's planes;
+// in a group, thread w owns row w / 8 and cells x0 + 4 (w % 8) .. + 3, so a warp holds 4 rows of
+// 8 quads and the x neighbours across quads are shuffles.  Per plane a thread issues its ten
+// vector loads (own r, p_old, three faces; the y-neighbour rows; the next plane's r, p_old) at
+// once, which keeps ~40 KB per block in flight.  FUSED: p = r + beta p_old is formed on the fly and
+// stored beside q (the persistent solve's pass); otherwise p is read (the standalone SpMV).  The
+// per-cell arithmetic is the scalar version's; the p.q partial is summed per thread over its 4
+// cells plane by plane, the same way in both uses.
+__device__ __forceinline__ bool vec4_ok(const InstDesc& d) { return (d.nx & 3) == 0; }
+
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ void st4(float* p, const float4& v) { *reinterpret_cast<float4*>(p) = v; }
+__device__ __forceinline__ float f4(const float4& v, int i) {
+  return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
+}
+
+template <bool FUSED>
+__device__ __forceinline__ void spmv4_task(const DevArrays& A, double* part, int64_t task,
+                                           const InstScal& s) {
+  const int4 tk = A.tasks[task];
+  const InstDesc& d = A.inst[tk.x];
+  const int nx = d.nx, ny = d.ny, nz = d.nz, nxy = nx * ny;
+  const int64_t off = d.off;
+  const int tid = threadIdx.x, grp = tid >> 6, w = tid & 63, row = w >> 3, q = w & 7;
+  const int x = tk.y + 4 * q, y = tk.z + row;
+  const int z0 = tk.w, z1 = min(z0 + d.zc, nz);
+  const int per = (z1 - z0 + 3) >> 2;
+  const int za = min(z0 + grp * per, z1), zb = min(za + per, z1);
+  const bool act = x < nx && y < ny;
+  const int64_t k = s.iter;
+  const bool first = !FUSED || k == 0;
+  const float beta = (float)s.beta;
+  const float* Src = FUSED ? A.r32 + off : ((k & 1) ? A.p232 : A.p32) + off;
+  const float* Po = (((k + 1) & 1) ? A.p232 : A.p32) + off;
+  float* Pn = ((k & 1) ? A.p232 : A.p32) + off;
+  float* Q = A.q32 + off;
+  const float* __restrict__ ax = A.a32x + off;
+  const float* __restrict__ ay = A.a32y + off;
+  const float* __restrict__ az = A.a32z + off;
+  const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  // neighbour offsets (y rows, x edges, z wrap); has_* false: the face is absent (value 0)
+  bool hn = false, hs = false;
+  int dn = 0, ds = 0;
+  if (ny > 1) {
+    if (y + 1 < ny) { dn = nx; hn = true; } else if (d.py) { dn = -(ny - 1) * nx; hn = true; }
+    if (y > 0) { ds = -nx; hs = true; } else if (d.py) { ds = (ny - 1) * nx; hs = true; }
+  }
+  const bool wload = (q == 0 || x == 0);          // west of cell 0 is loaded, not shuffled
+  const bool eload = (q == 7 || x + 4 == nx);     // east of cell 3 is loaded, not shuffled
+  bool hw = false, he = false;
+  int dw = 0, de = 0;
+  if (x > 0) { dw = -1; hw = true; } else if (d.px && nx > 1) { dw = nx - 1; hw = true; }
+  if (x + 4 < nx) { de = 4; he = true; } else if (d.px && nx > 1) { de = 4 - nx; he = true; }
+  auto pv = [&](float a, float b) -> float { return first ? a : fmaf(beta, b, a); };
+  auto pv4 = [&](const float4& a, const float4& b) -> float4 {
+    return make_float4(pv(a.x, b.x), pv(a.y, b.y), pv(a.z, b.z), pv(a.w, b.w));
+  };
+  auto ldp = [&](int l, float4& r, float4& po) {
+    r = ld4(Src + l);
+    po = first ? zero4 : ld4(Po + l);
+  };
+  const int lxy = y * nx + x;
+  // plane below the group (za - 1, or the periodic wrap to nz - 1), and the group's first plane
+  float4 pm = zero4, azm = zero4, rc = zero4, poc = zero4;
+  if (act && za < zb) {
+    if (nz > 1) {
+      int lb = -1;
+      if (za > 0) lb = lxy + (za - 1) * nxy;
+      else if (d.pz) lb = lxy + (nz - 1) * nxy;
+      if (lb >= 0) {
+        float4 rb, pob;
+        ldp(lb, rb, pob);
+        pm = pv4(rb, pob);
+        azm = ld4(az + lb);
+      }
+    }
+    ldp(lxy + za * nxy, rc, poc);
+  }
+  float pq = 0.f;
+  for (int z = za; z < zb; ++z) {
+    const int l = lxy + z * nxy;
+    float4 ru = zero4, pou = zero4, axv = zero4, ayv = zero4, azv = zero4;
+    float4 rn = zero4, pon = zero4, rs = zero4, pos = zero4, aysv = zero4;
+    float rw = 0.f, pow_ = 0.f, axwl = 0.f, re = 0.f, poe = 0.f;
+    if (act) {
+      if (nz > 1) {
+        if (z + 1 < nz) ldp(l + nxy, ru, pou);
+        else if (d.pz) ldp(lxy, ru, pou);
+      }
+      axv = ld4(ax + l); ayv = ld4(ay + l); azv = ld4(az + l);
+      if (hn) ldp(l + dn, rn, pon);
+      if (hs) { ldp(l + ds, rs, pos); aysv = ld4(ay + l + ds); }
+      if (wload && hw) {
+        rw = Src[l + dw];
+        pow_ = first ? 0.f : Po[l + dw];
+        axwl = ax[l + dw];
+      }
+      if (eload && he) {
+        re = Src[l + de];
+        poe = first ? 0.f : Po[l + de];
+      }
+    }
+    const float4 p = pv4(rc, poc);
+    const float pw_sh = __shfl_up_sync(kFull, p.w, 1);
+    const float axw_sh = __shfl_up_sync(kFull, axv.w, 1);
+    const float pe_sh = __shfl_down_sync(kFull, p.x, 1);
+    if (act) {
+      const float pw0 = wload ? (hw ? pv(rw, pow_) : 0.f) : pw_sh;
+      const float axw0 = wload ? (hw ? axwl : 0.f) : axw_sh;
+      const float pe3 = eload ? (he ? pv(re, poe) : 0.f) : pe_sh;
+      const float4 pu = pv4(ru, pou), pn = pv4(rn, pon), ps = pv4(rs, pos);
+      float4 qv;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const float pc = f4(p, i);
+        const float pe = i < 3 ? f4(p, i + 1) : pe3;
+        const float pw = i > 0 ? f4(p, i - 1) : pw0;
+        const float axw = i > 0 ? f4(axv, i - 1) : axw0;
+        float acc = pc;
+        acc = fmaf(f4(axv, i), pe, acc);
+        acc = fmaf(axw, pw, acc);
+        if (ny > 1) {
+          acc = fmaf(f4(ayv, i), f4(pn, i), acc);
+          acc = fmaf(f4(aysv, i), f4(ps, i), acc);
+        }
+        if (nz > 1) {
+          acc = fmaf(f4(azv, i), f4(pu, i), acc);
+          acc = fmaf(f4(azm, i), f4(pm, i), acc);
+        }
+        pq = fmaf(pc, acc, pq);
+        if (i == 0) qv.x = acc; else if (i == 1) qv.y = acc; else if (i == 2) qv.z = acc; else qv.w = acc;
+      }
+      if (FUSED) st4(Pn + l, p);
+      st4(Q + l, qv);
+      pm = p;
+      azm = azv;
+      rc = ru;
+      poc = pou;
+    }
+  }
+  task_store_f(part + task * kNR, 0, pq);
+}
+
+// The FP32 p + SpMV pass of one task: vector form where the grid allows it.
+template <bool FUSED>
+__device__ __forceinline__ void pq_f32_task(const DevArrays& A, double* part, int64_t task,
+                                            const InstScal& s) {
+  if (vec4_ok(A.inst[A.tasks[task].x])) spmv4_task<FUSED>(A, part, task, s);
+  else spmv_task<float, FUSED>(A, part, task, s);
+}
+
 // ---- standalone kernels (host-polled loop, conditional-node graph, kernel timing) --------------
 template <bool INIT, typename TR>
 __global__ void __launch_bounds__(kBlock) k_residual(DevArrays A) {
@@ -547,7 +707,15 @@ template <typename T>
 __global__ void __launch_bounds__(kBlock) k_cg_spmv(DevArrays A) {
   const InstScal& s = A.scal[A.tasks[blockIdx.x].x];
   if (!s.inner_active) return;
-  spmv_task<T, false>(A, A.partials, blockIdx.x, s);
+  if (sizeof(T) == 4) pq_f32_task<false>(A, A.partials, blockIdx.x, s);
+  else spmv_task<T, false>(A, A.partials, blockIdx.x, s);
+}
+
+// The persistent solve's fused FP32 pass on its own (timing and profiling).
+__global__ void __launch_bounds__(kBlock) k_cg_pq_f32(DevArrays A) {
+  const InstScal& s = A.scal[A.tasks[blockIdx.x].x];
+  if (!s.inner_active) return;
+  pq_f32_task<true>(A, A.partials, blockIdx.x, s);
 }
 
 template <typename T>
@@ -555,6 +723,42 @@ __global__ void __launch_bounds__(kBlock) k_cg_upd(DevArrays A) {
   const InstScal& s = A.scal[A.tasks[blockIdx.x].x];
   if (!s.inner_active) return;
   upd_task<T>(A, A.partials, blockIdx.x, s);
+}
+
+// ---- summation of an instance's task partials ------------------------------------------------
+// The order depends only on the instance's task count, so every path (finalize kernels, the
+// persistent solve's barrier epilogue) and every batch composition obtains the same bits: above
+// kWarpSumMax tasks the whole block sums (thread-strided, then block_sum), otherwise warp 0 sums
+// (lane-strided, then a shuffle tree).  The result is valid in thread 0.  Partials are read
+// through L2 (written by other blocks of the same persistent launch).
+constexpr int kWarpSumMax = 512;
+template <int NRV>
+__device__ __forceinline__ void warp_instance_sum(const double* part, const InstDesc& d, int lane,
+                                                  double (&acc)[NRV]) {
+#pragma unroll
+  for (int k = 0; k < NRV; ++k) acc[k] = 0.0;
+  for (int64_t t = lane; t < d.ntask; t += 32) {
+#pragma unroll
+    for (int k = 0; k < NRV; ++k) acc[k] += __ldcg(&part[(d.task0 + t) * kNR + k]);
+  }
+#pragma unroll
+  for (int k = 0; k < NRV; ++k) acc[k] = warp_sum(acc[k]);
+}
+// Block-uniform call (all threads of the block).
+template <int NRV>
+__device__ __forceinline__ void instance_sum(const double* part, const InstDesc& d,
+                                             double (&acc)[NRV], double* red) {
+  if (d.ntask > kWarpSumMax) {
+#pragma unroll
+    for (int k = 0; k < NRV; ++k) acc[k] = 0.0;
+    for (int64_t t = threadIdx.x; t < d.ntask; t += blockDim.x) {
+#pragma unroll
+      for (int k = 0; k < NRV; ++k) acc[k] += __ldcg(&part[(d.task0 + t) * kNR + k]);
+    }
+    block_sum<NRV>(acc, red);
+  } else if (threadIdx.x < 32) {
+    warp_instance_sum<NRV>(part, d, (int)threadIdx.x, acc);
+  }
 }
 
 // ---- finalize kernels: one block per instance sums the task partials in task order ----------
@@ -570,6 +774,7 @@ __device__ void epi_rhs(const DevArrays& A, int inst, const double* tot) {
     s.status |= kStatusRhsNan;
     s.outer_active = 0;
     s.failed_step = s.itime;
+    s.phase = PH_IDLE;
     return;
   }
   // scale of the first FP32 residual: a power of two near rms(S)/rms(|H_II|^(1/2)) * 1e-6
@@ -717,14 +922,8 @@ __global__ void __launch_bounds__(256) k_finalize(DevArrays A, CtrlState* ctrl,
   const InstDesc& d = A.inst[inst];
   if (took_part<KIND>(A.scal[inst])) {
     double acc[NR];
-#pragma unroll
-    for (int k = 0; k < NR; ++k) acc[k] = 0.0;
-    for (int64_t t = threadIdx.x; t < d.ntask; t += blockDim.x) {
-#pragma unroll
-      for (int k = 0; k < NR; ++k) acc[k] += A.partials[(d.task0 + t) * kNR + k];
-    }
     __shared__ double red[32 * NR];
-    block_sum<NR>(acc, red);
+    instance_sum<NR>(A.partials, d, acc, red);
     if (threadIdx.x == 0) {
       switch (KIND) {
         case FIN_RHS: epi_rhs(A, inst, acc); break;
@@ -803,21 +1002,18 @@ __global__ void k_ctrl_select(DevArrays A, CtrlState* ctrl, cudaGraphConditional
 
 // ---- persistent solve ------------------------------------------------------------------------
 // One cooperative launch runs a step's whole refinement loop.  Work proceeds in grid-wide rounds:
-// in round r every task does the work of its instance's current phase (PH_*) and writes its
-// partial sums to the round's partial buffer; a grid barrier closes the round.  At the start of
-// the next round, each block that picks up a task of an instance first runs that instance's
-// epilogue itself: it sums the instance's task partials of the previous round in task order (the
-// same order as the finalize kernels, so every block obtains the same bits) and updates the
-// scalars (alpha, beta, convergence, next phase) in shared memory.  Scalars and partials are
-// double-buffered by round parity, so the blocks that read round r's values never race with the
-// writes of round r + 1; only the block that picks up an instance's first task (its owner for the
-// round) stores the new scalars.  Tasks are handed out by an atomic counter per round, in
-// increasing order, so a block meets an instance's tasks in one run.  The kernel returns when a
-// barrier reports that no owner has work left.
+// in round r every task does the work of its instance's current phase (PH_*), writing its partial
+// sums to its fixed slot; then every block arrives at a grid barrier.  The last block to arrive
+// runs the epilogue of every instance -- it sums each instance's task partials in the fixed order
+// of instance_sum (the order the finalize kernels use, so every path obtains the same bits) and
+// updates the instance's scalars (alpha, beta, convergence test, next phase) in device memory --
+// and only then opens the barrier.  Blocks read the scalars of the instances they work on through
+// L2 at the start of each round.  Tasks are assigned statically (task t to block t mod grid).
+// The kernel returns when the last epilogue reports that no instance has work left.
 //
-// Termination: every barrier wait is bounded in time (kBarrierWaitNs); a block that gives up
-// records SolveCtl::err and returns, and the blocks still waiting see the flag and return too.
-// The number of rounds is bounded by `limit`.  Co-residency of all blocks, which the barrier
+// Termination: every barrier wait is bounded in time (kBarrierWaitNs) and in polls; a block that
+// gives up records SolveCtl::err and returns, and the blocks still waiting see the flag and return
+// too.  The number of rounds is bounded by `limit`.  Co-residency of all blocks, which the barrier
 // needs, is guaranteed by the cooperative launch (the grid never exceeds the occupancy bound).
 constexpr unsigned long long kBarrierWaitNs = 4000000000ull;
 
@@ -835,42 +1031,130 @@ __device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-// Grid barrier that also ORs one flag per block.  Returns false if the wait gave up.
-__device__ bool grid_barrier_or(SolveCtl* ctl, unsigned nblocks, unsigned flag, int64_t round,
-                                unsigned& any) {
-  __shared__ unsigned s_any;
-  __shared__ int s_ok;
+template <typename T>
+__device__ __forceinline__ int32_t phase_after(const InstScal& s) {
+  if (!s.outer_active) return PH_IDLE;
+  if (s.inner_active) return sizeof(T) == 4 ? PH_CG_PQ : PH_CG_P;
+  return PH_XUPD;
+}
+__device__ __forceinline__ int phase_partials(int32_t ph) {
+  return (ph == PH_RES_INIT || ph == PH_RES || ph == PH_CG_B) ? 2
+         : ((ph == PH_CG_Q || ph == PH_CG_PQ) ? 1 : 0);
+}
+
+constexpr int kScalWords = (int)(sizeof(InstScal) / 8);
+static_assert(sizeof(InstScal) % 8 == 0 && kScalWords <= kBlock, "scalar copy");
+
+// Epilogue of one instance after a round (one thread): scalars read through L2, updated, stored.
+// Returns whether the instance has work in the next round.
+template <typename T>
+__device__ int instance_epilogue(const DevArrays& A, int64_t inst, const double (&acc)[2]) {
+  InstScal sc;
+  const unsigned long long* src = reinterpret_cast<const unsigned long long*>(A.scal + inst);
+  unsigned long long* w = reinterpret_cast<unsigned long long*>(&sc);
+  for (int k = 0; k < kScalWords; ++k) w[k] = __ldcg(src + k);
+  const InstDesc& d = A.inst[inst];
+  switch (sc.phase) {
+    case PH_RES_INIT:
+      epi_residual_s<true>(sc, d, A.opts, acc);
+      sc.phase = phase_after<T>(sc);
+      break;
+    case PH_RES:
+      epi_residual_s<false>(sc, d, A.opts, acc);
+      sc.phase = phase_after<T>(sc);
+      break;
+    case PH_CG_P: sc.phase = PH_CG_Q; break;
+    case PH_CG_Q:
+    case PH_CG_PQ:
+      epi_spmv_s(sc, acc);
+      sc.phase = sc.inner_active ? PH_CG_B : phase_after<T>(sc);
+      break;
+    case PH_CG_B:
+      epi_upd_s<T>(sc, A.opts, acc);
+      sc.phase = phase_after<T>(sc);
+      break;
+    case PH_XUPD: sc.phase = PH_RES; break;
+    default: sc.phase = PH_IDLE; break;
+  }
+  unsigned long long* dst = reinterpret_cast<unsigned long long*>(A.scal + inst);
+  for (int k = 0; k < kScalWords; ++k) dst[k] = w[k];
+  return sc.phase != PH_IDLE ? 1 : 0;
+}
+
+// Epilogues of all instances (the whole last-arriving block).  Large instances (block sums) one
+// after the other, small ones one per warp.  Returns (in every thread) whether any has work left.
+template <typename T>
+__device__ int all_epilogues(const DevArrays& A, double* red) {
+  int act = 0;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int64_t i = 0; i < A.ninst; ++i) {
+    const InstDesc& d = A.inst[i];
+    if (d.ntask <= kWarpSumMax) continue;
+    const int32_t ph = __ldcg(&A.scal[i].phase);
+    double acc[2] = {0.0, 0.0};
+    if (phase_partials(ph) > 0) instance_sum<2>(A.partials, d, acc, red);
+    if (threadIdx.x == 0) act |= instance_epilogue<T>(A, i, acc);
+    __syncthreads();
+  }
+  for (int64_t i = warp; i < A.ninst; i += kBlock / 32) {
+    const InstDesc& d = A.inst[i];
+    if (d.ntask > kWarpSumMax) continue;
+    const int32_t ph = __ldcg(&A.scal[i].phase);
+    double acc[2] = {0.0, 0.0};
+    if (phase_partials(ph) > 0) warp_instance_sum<2>(A.partials, d, lane, acc);
+    if (lane == 0) act |= instance_epilogue<T>(A, i, acc);
+  }
+  return __syncthreads_or(act);
+}
+
+// Grid barrier whose last arriving block runs all epilogues before opening it.  Returns false if
+// the wait gave up; `any` = some instance has work in the next round.
+template <typename T>
+__device__ bool grid_barrier_epilogue(const DevArrays& A, SolveCtl* ctl, unsigned nblocks,
+                                      int64_t round, double* red, unsigned& any) {
+  __shared__ unsigned s_gen, s_any;
+  __shared__ int s_last, s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     const unsigned g = ld_acquire_u32(&ctl->gen);   // cannot advance before this block arrives
-    if (flag) atomicOr(&ctl->flag_acc, 1u);
     __threadfence();
     const unsigned arrived = atomicAdd(&ctl->count, 1u);
-    int ok = 1;
-    if (arrived == nblocks - 1) {
-      ctl->result[(g + 1) & 1] = atomicExch(&ctl->flag_acc, 0u);
-      ctl->next_task[(round + 1) & 1] = 0u;       // counter of the next round (last used at r-1)
+    s_gen = g;
+    s_last = (arrived == nblocks - 1) ? 1 : 0;
+    if (s_last) __threadfence();                   // every block's partials are visible now
+  }
+  __syncthreads();
+  const unsigned g = s_gen;
+  if (s_last) {
+    if (threadIdx.x == 0 && round < kRoundLog) ctl->phase_log[round] = __ldcg(&A.scal[0].phase);
+    const int act = all_epilogues<T>(A, red);
+    if (threadIdx.x == 0) {
+      ctl->result[(g + 1) & 1] = act ? 1u : 0u;
       if (round < kRoundLog) ctl->t_round[round] = gtimer();
       ctl->rounds = round + 1;
       ctl->count = 0u;
       __threadfence();
       st_release_u32(&ctl->gen, g + 1);
-    } else {
-      const unsigned long long t0 = gtimer();
-      unsigned polls = 0;
-      while (ld_acquire_u32(&ctl->gen) == g) {
-        if (*(volatile int*)&ctl->err) { ok = 0; break; }
-        if ((++polls & 255u) == 0u && (gtimer() - t0 > kBarrierWaitNs || polls > (1u << 27))) {
-          atomicExch(&ctl->err, 1);
-          ok = 0;
-          break;
-        }
-        __nanosleep(32);
-      }
+      s_ok = 1;
     }
-    __threadfence();
-    s_any = ok ? *(volatile unsigned*)&ctl->result[(g + 1) & 1] : 0u;
+  } else if (threadIdx.x == 0) {
+    int ok = 1;
+    const unsigned long long t0 = gtimer();
+    unsigned polls = 0;
+    while (ld_acquire_u32(&ctl->gen) == g) {
+      if (*(volatile int*)&ctl->err) { ok = 0; break; }
+      if ((++polls & 255u) == 0u && (gtimer() - t0 > kBarrierWaitNs || polls > (1u << 27))) {
+        atomicExch(&ctl->err, 1);
+        ok = 0;
+        break;
+      }
+      __nanosleep(32);
+    }
     s_ok = ok;
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_any = s_ok ? *(volatile unsigned*)&ctl->result[(g + 1) & 1] : 0u;
   }
   __syncthreads();
   any = s_any;
@@ -878,72 +1162,12 @@ __device__ bool grid_barrier_or(SolveCtl* ctl, unsigned nblocks, unsigned flag, 
 }
 
 template <typename T>
-__device__ __forceinline__ int32_t phase_after(const InstScal& s) {
-  if (!s.outer_active) return PH_IDLE;
-  if (s.inner_active) return sizeof(T) == 4 ? PH_CG_PQ : PH_CG_P;
-  return PH_XUPD;
-}
-
-// Epilogue of instance `inst` at the start of a round: previous scalars from `sin`, the previous
-// round's partials from `prev`; result in `sh` (all threads see it on return).  The owner block
-// (the one holding the instance's first task) stores it to `sout` and raises its active flag.
-template <typename T>
-__device__ void round_epilogue(const DevArrays& A, int inst, const InstScal* sin, InstScal* sout,
-                               const double* prev, int64_t task, InstScal& sh, double* red,
-                               int& s_flag) {
-  constexpr int kWords = (int)(sizeof(InstScal) / 8);
-  static_assert(sizeof(InstScal) % 8 == 0 && kWords <= kBlock, "scalar copy");
-  if ((int)threadIdx.x < kWords)
-    reinterpret_cast<unsigned long long*>(&sh)[threadIdx.x] =
-        __ldcg(reinterpret_cast<const unsigned long long*>(sin + inst) + threadIdx.x);
-  __syncthreads();
-  const int32_t ph = sh.phase;
-  const InstDesc& d = A.inst[inst];
-  const int nr = (ph == PH_RES_INIT || ph == PH_RES || ph == PH_CG_B) ? 2
-                 : ((ph == PH_CG_Q || ph == PH_CG_PQ) ? 1 : 0);
-  double acc[2] = {0.0, 0.0};
-  if (nr > 0) {
-    for (int64_t t = threadIdx.x; t < d.ntask; t += blockDim.x) {
-      acc[0] += __ldcg(&prev[(d.task0 + t) * kNR]);
-      acc[1] += __ldcg(&prev[(d.task0 + t) * kNR + 1]);
-    }
-    block_sum<2>(acc, red);
-  }
-  if (threadIdx.x == 0) {
-    switch (ph) {
-      case PH_START: sh.phase = sh.outer_active ? PH_RES_INIT : PH_IDLE; break;
-      case PH_RES_INIT:
-        epi_residual_s<true>(sh, d, A.opts, acc);
-        sh.phase = phase_after<T>(sh);
-        break;
-      case PH_RES:
-        epi_residual_s<false>(sh, d, A.opts, acc);
-        sh.phase = phase_after<T>(sh);
-        break;
-      case PH_CG_P: sh.phase = PH_CG_Q; break;
-      case PH_CG_Q:
-      case PH_CG_PQ:
-        epi_spmv_s(sh, acc);
-        sh.phase = sh.inner_active ? PH_CG_B : phase_after<T>(sh);
-        break;
-      case PH_CG_B:
-        epi_upd_s<T>(sh, A.opts, acc);
-        sh.phase = phase_after<T>(sh);
-        break;
-      case PH_XUPD: sh.phase = PH_RES; break;
-      default: sh.phase = PH_IDLE; break;
-    }
-    if (task == d.task0) {
-      sout[inst] = sh;
-      if (sh.phase != PH_IDLE) s_flag = 1;
-    }
-  }
-  __syncthreads();
-}
-
-template <typename T>
 __device__ __forceinline__ void round_task(const DevArrays& A, double* part, int64_t task,
                                            const InstScal& s) {
+  if (sizeof(T) == 4 && s.phase == PH_CG_PQ) {
+    pq_f32_task<true>(A, part, task, s);
+    return;
+  }
   switch (s.phase) {
     case PH_RES_INIT: res_task<true, T>(A, part, task, s); break;
     case PH_RES: res_task<false, T>(A, part, task, s); break;
@@ -956,61 +1180,36 @@ __device__ __forceinline__ void round_task(const DevArrays& A, double* part, int
   }
 }
 
-// Blocks per SM: FP32 4 (64 registers), FP64 3 (its stencil needs ~85 registers).
+// Blocks per SM: 3 (85 registers: the FP64 stencil and the FP32 vector pass need about that).
 template <typename T>
-__global__ void __launch_bounds__(kBlock, sizeof(T) == 4 ? 4 : 3)
+__global__ void __launch_bounds__(kBlock, 3)
     k_solve(DevArrays A, SolveCtl* ctl, int64_t limit) {
   __shared__ InstScal sh;
   __shared__ double red[32 * 2];
-  __shared__ unsigned s_task;
-  __shared__ int s_flag;
   const unsigned G = gridDim.x;
   const unsigned nt = (unsigned)A.ntasks;
   if (blockIdx.x == 0 && threadIdx.x == 0) ctl->t_start = gtimer();
-  int64_t r = 0;
-  for (;; ++r) {
+  for (int64_t r = 0;; ++r) {
     if (r >= limit) {
       if (blockIdx.x == 0 && threadIdx.x == 0) ctl->guard_hit = 1;
-      break;
+      return;
     }
-    double* part = A.partials + (r & 1) * (int64_t)nt * kNR;
-    const double* prev = A.partials + ((r + 1) & 1) * (int64_t)nt * kNR;
-    const InstScal* sin = (r & 1) ? A.scal2 : A.scal;
-    InstScal* sout = (r & 1) ? A.scal : A.scal2;
-    if (threadIdx.x == 0) {
-      s_flag = 0;
-      s_task = atomicAdd(&ctl->next_task[r & 1], 1u);
-    }
-    __syncthreads();
-    unsigned t = s_task;
     int cur = -1;
-    while (t < nt) {
-      // the next task index is fetched now and consumed after this task (latency hidden)
-      unsigned nxt = 0u;
-      if (threadIdx.x == 0) nxt = atomicAdd(&ctl->next_task[r & 1], 1u);
+    for (unsigned t = blockIdx.x; t < nt; t += G) {
       const int inst = A.tasks[t].x;
-      if (inst != cur) {
+      if (inst != cur) {                     // this instance's scalars, through L2
+        __syncthreads();
+        if ((int)threadIdx.x < kScalWords)
+          reinterpret_cast<unsigned long long*>(&sh)[threadIdx.x] =
+              __ldcg(reinterpret_cast<const unsigned long long*>(A.scal + inst) + threadIdx.x);
+        __syncthreads();
         cur = inst;
-        round_epilogue<T>(A, inst, sin, sout, prev, t, sh, red, s_flag);
-        if (inst == 0 && t == 0 && threadIdx.x == 0 && r < kRoundLog) ctl->phase_log[r] = sh.phase;
       }
-      if (sh.phase != PH_IDLE) round_task<T>(A, part, t, sh);
-      __syncthreads();                               // sh and s_task are free
-      if (threadIdx.x == 0) s_task = nxt;
-      __syncthreads();
-      t = s_task;
+      if (sh.phase != PH_IDLE) round_task<T>(A, A.partials, t, sh);
     }
     unsigned any = 0;
-    if (!grid_barrier_or(ctl, G, (unsigned)s_flag, r, any)) return;
-    if (!any) break;
-  }
-  // the scalars of the last round live in the buffer of parity (r + 1): bring them to A.scal
-  if (((r + 1) & 1) == 1 && r < limit) {
-    for (int64_t i = blockIdx.x; i < A.ninst; i += G) {
-      if ((int)threadIdx.x < (int)(sizeof(InstScal) / 8))
-        reinterpret_cast<unsigned long long*>(A.scal + i)[threadIdx.x] =
-            __ldcg(reinterpret_cast<const unsigned long long*>(A.scal2 + i) + threadIdx.x);
-    }
+    if (!grid_barrier_epilogue<T>(A, ctl, G, r, red, any)) return;
+    if (!any) return;
   }
 }
 
@@ -1160,6 +1359,14 @@ cudaError_t launch_single(Ctx& c, int which) {
     case HF_KERNEL_CG_UPDATE:
       if (fp32) k_cg_upd<float><<<nb, kBlock, 0, c.stream>>>(c.A);
       else k_cg_upd<double><<<nb, kBlock, 0, c.stream>>>(c.A);
+      break;
+    case HF_KERNEL_CG_PQ:
+      if (fp32) {
+        k_cg_pq_f32<<<nb, kBlock, 0, c.stream>>>(c.A);
+      } else {
+        k_cg_p<double><<<nb, kBlock, 0, c.stream>>>(c.A);
+        k_cg_spmv<double><<<nb, kBlock, 0, c.stream>>>(c.A);
+      }
       break;
     default: return cudaErrorInvalidValue;
   }

@@ -40,7 +40,8 @@ def _d(a):
 
 
 def make_opts(precision="fp64", criterion="recursive", tol=None, itmax=50000, inner_tol=1e-4,
-              inner_itmax=200, max_refine=20, check_every=2, use_graph=0) -> abi.HfSolverOpts:
+              inner_itmax=200, max_refine=20, check_every=2, use_graph=0,
+              task_depth=0) -> abi.HfSolverOpts:
     lib = abi.load_library()
     o = abi.HfSolverOpts()
     lib.hf_default_opts(C.byref(o))
@@ -55,6 +56,7 @@ def make_opts(precision="fp64", criterion="recursive", tol=None, itmax=50000, in
     o.max_refine = max_refine
     o.check_every = check_every
     o.use_graph = use_graph
+    o.task_depth = task_depth
     return o
 
 
@@ -99,6 +101,16 @@ class HeatFlow:
         ms = C.c_double()
         abi.check(self.lib.hf_time_kernel(self.h, int(kernel), int(reps), C.byref(ms)), "hf_time_kernel")
         return ms.value
+
+    def solve_profile(self, cap: int = 64):
+        """Rounds of the last persistent solve: [(phase name, microseconds), ...] and the total
+        number of rounds (the per-round list stops at 64)."""
+        rounds = C.c_int64()
+        ph = (C.c_int32 * cap)()
+        us = (C.c_double * cap)()
+        abi.check(self.lib.hf_solve_profile(self.h, cap, C.byref(rounds), ph, us), "hf_solve_profile")
+        n = min(rounds.value, cap, 64)
+        return [(abi.PHASE_NAMES.get(ph[i], str(ph[i])), us[i]) for i in range(n)], rounds.value
 
     # ---- options
     def set_opts(self, **opts):

@@ -100,6 +100,7 @@ typedef struct hf_solver_opts {
                            1 = a CUDA graph per step whose solve is one persistent cooperative
                            kernel (grid-wide rounds, no host round trip);
                            2 = a CUDA graph per step with conditional WHILE/SWITCH nodes */
+  int32_t task_depth;   /* z-planes per task of the step kernels (0: 16; otherwise 4..1024) */
 } hf_solver_opts;
 
 typedef struct hf_stats {
@@ -205,7 +206,11 @@ enum {
   HF_KERNEL_CG_P = 2,        /* inner CG direction update p = r + beta p */
   HF_KERNEL_CG_SPMV = 3,     /* inner CG SpMV q = A p and p.q */
   HF_KERNEL_CG_UPDATE = 4,   /* inner CG solution/residual update + r.r */
-  HF_KERNEL_XUPDATE = 5      /* FP64 solution update x += S^-1 y */
+  HF_KERNEL_XUPDATE = 5,     /* FP64 solution update x += S^-1 y */
+  HF_KERNEL_SOLVE = 6,       /* the persistent solve kernel: one whole solve of the next step's
+                                system (the step's RHS runs before each timed launch) */
+  HF_KERNEL_CG_PQ = 7        /* the fused direction update + SpMV pass of the persistent solve's
+                                FP32 inner CG, launched on its own (FP64: CG_P then CG_SPMV) */
 };
 /* Launch one kernel `reps` times on the current state, each bracketed by CUDA events on the
  * context's stream, and return its mean duration in milliseconds.  Solver scalars are restored
@@ -214,6 +219,24 @@ int hf_time_kernel(hf_ctx* ctx, int kernel, int reps, double* ms_per_launch);
 /* FP64 and FP32 FMA throughput of the current device in TFLOP/s (independent FMA chains over
  * every SM, CUDA-event timed).  On GB300 the FP64 rate bounds the FP64 kernels of a step. */
 int hf_measure_fp_rates(double* fp64_tflops, double* fp32_tflops);
+
+/* Phases of the persistent solve kernel, one per grid-wide round. */
+enum {
+  HF_PHASE_IDLE = 0,      /* nothing left (step finished) */
+  HF_PHASE_START = 1,     /* reserved */
+  HF_PHASE_RES_INIT = 2,  /* first true residual r = S - H x0 */
+  HF_PHASE_CG_P = 3,      /* FP64 inner CG: p = r + beta p */
+  HF_PHASE_CG_Q = 4,      /* FP64 inner CG: q = Ah p, p.q */
+  HF_PHASE_CG_PQ = 5,     /* FP32 inner CG: p = r + beta p and q = Ah p in one pass */
+  HF_PHASE_CG_B = 6,      /* inner CG: y += alpha p, r -= alpha q, r.r */
+  HF_PHASE_XUPD = 7,      /* x += sigma S^-1 y */
+  HF_PHASE_RES = 8        /* true residual of the updated x */
+};
+/* Round profile of the context's last persistent solve (use_graph = 1, or hf_time_kernel with
+ * HF_KERNEL_SOLVE).  No counterpart in the reference.  *rounds = grid-wide rounds run; for the
+ * first min(rounds, cap, 64) rounds, phases[r] = the phase instance 0 ran and round_us[r] = the
+ * round's length in microseconds (device %globaltimer; round 0 counts from the kernel's start). */
+int hf_solve_profile(hf_ctx* ctx, int64_t cap, int64_t* rounds, int32_t* phases, double* round_us);
 
 /* ---- allocation-free residual ---------------------------------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device memory - hosts that
