@@ -672,6 +672,205 @@ __device__ __forceinline__ void spmv4_task(const DevArrays& A, double* part, int
   task_store_f(part + task * kNR, 0, pq);
 }
 
+// ---- element-wise passes on 4-cell vectors (rows of 4k cells) --------------------------------
+// Same thread layout as spmv4_task (four z-groups of 64 threads, 4 consecutive x cells per
+// thread); FP32 vectors are one 16-byte access, FP64 vectors two.  Two planes of loads are issued
+// before they are used.  Reductions are summed per thread plane by plane, cells in x order.
+template <typename T> struct V4 { T v[4]; };
+__device__ __forceinline__ V4<float> ldv4(const float* p) {
+  const float4 t = *reinterpret_cast<const float4*>(p);
+  return V4<float>{{t.x, t.y, t.z, t.w}};
+}
+__device__ __forceinline__ V4<double> ldv4(const double* p) {
+  const double2 a = reinterpret_cast<const double2*>(p)[0], b = reinterpret_cast<const double2*>(p)[1];
+  return V4<double>{{a.x, a.y, b.x, b.y}};
+}
+__device__ __forceinline__ void stv4(float* p, const V4<float>& v) {
+  *reinterpret_cast<float4*>(p) = make_float4(v.v[0], v.v[1], v.v[2], v.v[3]);
+}
+__device__ __forceinline__ void stv4(double* p, const V4<double>& v) {
+  reinterpret_cast<double2*>(p)[0] = make_double2(v.v[0], v.v[1]);
+  reinterpret_cast<double2*>(p)[1] = make_double2(v.v[2], v.v[3]);
+}
+
+struct Quad {
+  int64_t off;
+  int nxy, lxy, za, zb;
+  bool act;
+};
+__device__ __forceinline__ Quad quad_cell(const DevArrays& A, int64_t task) {
+  const int4 tk = A.tasks[task];
+  const InstDesc& d = A.inst[tk.x];
+  const int tid = threadIdx.x, grp = tid >> 6, w = tid & 63;
+  const int x = tk.y + 4 * (w & 7), y = tk.z + (w >> 3);
+  const int z1 = min(tk.w + d.zc, d.nz);
+  const int per = (z1 - tk.w + 3) >> 2;
+  Quad c;
+  c.off = d.off;
+  c.nxy = d.nx * d.ny;
+  c.lxy = y * d.nx + x;
+  c.za = min(tk.w + grp * per, z1);
+  c.zb = min(c.za + per, z1);
+  c.act = x < d.nx && y < d.ny;
+  return c;
+}
+
+template <typename T>
+__device__ __forceinline__ void upd4_task(const DevArrays& A, double* part, int64_t task,
+                                          const InstScal& s) {
+  const Quad c = quad_cell(A, task);
+  const bool weighted = (A.opts.criterion == HF_STOP_RECURSIVE);
+  const T alpha = (T)s.alpha;
+  const bool first = (s.iter == 0);
+  T* Y = Vec<T>::y(A) + c.off;
+  T* R = Vec<T>::r(A) + c.off;
+  const T* P = Vec<T>::pb(A, s.iter) + c.off;
+  const T* Q = Vec<T>::q(A) + c.off;
+  const double* __restrict__ diag = A.diag + c.off;
+  T rr = T(0);
+  double rw = 0.0;
+  if (c.act) {
+    for (int z = c.za; z < c.zb; z += 2) {
+      const bool two = z + 1 < c.zb;
+      const int l0 = c.lxy + z * c.nxy, l1 = l0 + c.nxy;
+      V4<T> p0 = ldv4(P + l0), q0 = ldv4(Q + l0), r0 = ldv4(R + l0), y0{}, p1{}, q1{}, r1{}, y1{};
+      if (!first) y0 = ldv4(Y + l0);
+      if (two) {
+        p1 = ldv4(P + l1); q1 = ldv4(Q + l1); r1 = ldv4(R + l1);
+        if (!first) y1 = ldv4(Y + l1);
+      }
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        if (h == 1 && !two) break;
+        const int l = h ? l1 : l0;
+        const V4<T>& pv = h ? p1 : p0;
+        const V4<T>& qv = h ? q1 : q0;
+        const V4<T>& rv = h ? r1 : r0;
+        const V4<T>& yv = h ? y1 : y0;
+        V4<T> yo, ro;
+        V4<double> dg{};
+        if (weighted) dg = ldv4(diag + l);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          yo.v[i] = first ? alpha * pv.v[i] : fma(alpha, pv.v[i], yv.v[i]);
+          const T r = fma(-alpha, qv.v[i], rv.v[i]);
+          ro.v[i] = r;
+          rr = fma(r, r, rr);
+          if (weighted) rw = fma(-dg.v[i] * (double)r, (double)r, rw);
+        }
+        stv4(Y + l, yo);
+        stv4(R + l, ro);
+      }
+    }
+  }
+  if (sizeof(T) == 4 && !weighted) {
+    task_store_f(part + task * kNR, 0, (float)rr);
+  } else {
+    const double v[2] = {(double)rr, rw};
+    tile_store<2>(part + task * kNR, v);
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void cgp4_task(const DevArrays& A, double* part, int64_t task,
+                                          const InstScal& s) {
+  const Quad c = quad_cell(A, task);
+  if (!c.act) return;
+  const int64_t k = s.iter;
+  const bool first = (k == 0);
+  const T beta = (T)s.beta;
+  const T* R = Vec<T>::r(A) + c.off;
+  const T* Po = Vec<T>::pb(A, k + 1) + c.off;
+  T* Pn = Vec<T>::pb(A, k) + c.off;
+  for (int z = c.za; z < c.zb; z += 2) {
+    const bool two = z + 1 < c.zb;
+    const int l0 = c.lxy + z * c.nxy, l1 = l0 + c.nxy;
+    V4<T> r0 = ldv4(R + l0), o0{}, r1{}, o1{};
+    if (!first) o0 = ldv4(Po + l0);
+    if (two) {
+      r1 = ldv4(R + l1);
+      if (!first) o1 = ldv4(Po + l1);
+    }
+    V4<T> n0, n1;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      n0.v[i] = first ? r0.v[i] : fma(beta, o0.v[i], r0.v[i]);
+      n1.v[i] = first ? r1.v[i] : fma(beta, o1.v[i], r1.v[i]);
+    }
+    stv4(Pn + l0, n0);
+    if (two) stv4(Pn + l1, n1);
+  }
+}
+
+template <typename TY>
+__device__ __forceinline__ void xupd4_task(const DevArrays& A, double* part, int64_t task,
+                                           const InstScal& s) {
+  const Quad c = quad_cell(A, task);
+  if (!c.act) return;
+  const double* XR = A.tbuf[s.role[2]] + c.off;
+  double* XW = A.tbuf[s.role[3]] + c.off;
+  const TY* Y = Vec<TY>::y(A) + c.off;
+  const double* __restrict__ sinv = A.sinv + c.off;
+  const float* __restrict__ sinv32 = A.sinv32 + c.off;
+  const bool use_y = s.iter > 0;
+  const bool tiny = s.tiny_pending != 0;
+  const float sig = (float)s.sigma_prev;
+  for (int z = c.za; z < c.zb; z += 2) {
+    const bool two = z + 1 < c.zb;
+    const int l0 = c.lxy + z * c.nxy, l1 = l0 + c.nxy;
+    V4<double> x0 = ldv4(XR + l0), x1{}, s0{}, s1{};
+    V4<TY> y0{}, y1{};
+    V4<float> f0{}, f1{};
+    if (use_y) {
+      y0 = ldv4(Y + l0);
+      if (sizeof(TY) == 8) s0 = ldv4(sinv + l0); else f0 = ldv4(sinv32 + l0);
+    }
+    if (two) {
+      x1 = ldv4(XR + l1);
+      if (use_y) {
+        y1 = ldv4(Y + l1);
+        if (sizeof(TY) == 8) s1 = ldv4(sinv + l1); else f1 = ldv4(sinv32 + l1);
+      }
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      if (h == 1 && !two) break;
+      V4<double> xv = h ? x1 : x0;
+      const V4<TY>& yv = h ? y1 : y0;
+      const V4<double>& sv = h ? s1 : s0;
+      const V4<float>& fv = h ? f1 : f0;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        double x = xv.v[i];
+        if (tiny) x = x + kTiny;
+        if (use_y) {
+          if (sizeof(TY) == 8) x = fma(sv.v[i], (double)yv.v[i], x);   // sigma = 1 on the FP64 path
+          else x = x + f32_to_f64(sig * fv.v[i] * (float)yv.v[i]);
+        }
+        xv.v[i] = x;
+      }
+      stv4(XW + (h ? l1 : l0), xv);
+    }
+  }
+}
+
+// Dispatch between the vector and the scalar form of a pass (same choice on every path).
+template <typename T>
+__device__ __forceinline__ void upd_any(const DevArrays& A, double* part, int64_t task, const InstScal& s) {
+  if (vec4_ok(A.inst[A.tasks[task].x])) upd4_task<T>(A, part, task, s);
+  else upd_task<T>(A, part, task, s);
+}
+template <typename T>
+__device__ __forceinline__ void cgp_any(const DevArrays& A, double* part, int64_t task, const InstScal& s) {
+  if (vec4_ok(A.inst[A.tasks[task].x])) cgp4_task<T>(A, part, task, s);
+  else cgp_task<T>(A, part, task, s);
+}
+template <typename TY>
+__device__ __forceinline__ void xupd_any(const DevArrays& A, double* part, int64_t task, const InstScal& s) {
+  if (vec4_ok(A.inst[A.tasks[task].x])) xupd4_task<TY>(A, part, task, s);
+  else xupd_task<TY>(A, part, task, s);
+}
+
 // The FP32 p + SpMV pass of one task: vector form where the grid allows it.
 template <bool FUSED>
 __device__ __forceinline__ void pq_f32_task(const DevArrays& A, double* part, int64_t task,
@@ -693,14 +892,14 @@ template <typename TY>
 __global__ void __launch_bounds__(kBlock) k_xupdate(DevArrays A) {
   const InstScal& s = A.scal[A.tasks[blockIdx.x].x];
   if (!s.outer_active || s.inner_active || s.refine == 0) return;
-  xupd_task<TY>(A, A.partials, blockIdx.x, s);
+  xupd_any<TY>(A, A.partials, blockIdx.x, s);
 }
 
 template <typename T>
 __global__ void __launch_bounds__(kBlock) k_cg_p(DevArrays A) {
   const InstScal& s = A.scal[A.tasks[blockIdx.x].x];
   if (!s.inner_active) return;
-  cgp_task<T>(A, A.partials, blockIdx.x, s);
+  cgp_any<T>(A, A.partials, blockIdx.x, s);
 }
 
 template <typename T>
@@ -722,7 +921,7 @@ template <typename T>
 __global__ void __launch_bounds__(kBlock) k_cg_upd(DevArrays A) {
   const InstScal& s = A.scal[A.tasks[blockIdx.x].x];
   if (!s.inner_active) return;
-  upd_task<T>(A, A.partials, blockIdx.x, s);
+  upd_any<T>(A, A.partials, blockIdx.x, s);
 }
 
 // ---- summation of an instance's task partials ------------------------------------------------
@@ -1171,11 +1370,11 @@ __device__ __forceinline__ void round_task(const DevArrays& A, double* part, int
   switch (s.phase) {
     case PH_RES_INIT: res_task<true, T>(A, part, task, s); break;
     case PH_RES: res_task<false, T>(A, part, task, s); break;
-    case PH_CG_P: cgp_task<T>(A, part, task, s); break;
+    case PH_CG_P: cgp_any<T>(A, part, task, s); break;
     case PH_CG_Q: spmv_task<T, false>(A, part, task, s); break;
     case PH_CG_PQ: spmv_task<T, true>(A, part, task, s); break;
-    case PH_CG_B: upd_task<T>(A, part, task, s); break;
-    case PH_XUPD: xupd_task<T>(A, part, task, s); break;
+    case PH_CG_B: upd_any<T>(A, part, task, s); break;
+    case PH_XUPD: xupd_any<T>(A, part, task, s); break;
     default: break;
   }
 }
