@@ -43,10 +43,12 @@ BYTES_PER_CELL = {
     "rhs": 6 * 8 + 1 + 2 * 8,
     # mixed: x, diag, cx, cy, cz, S (8 B) + 1/sqrt|H_II| (4 B) read; g (4 B) written
     "residual_mixed": 6 * 8 + 4 + 4,
-    # FP64: the same with g written in FP64
-    "residual_fp64": 6 * 8 + 4 + 8,
+    # FP64: x, diag, cx, cy, cz, S, 1/sqrt|H_II| (8 B) read; g (8 B) written
+    "residual_fp64": 7 * 8 + 8,
     # direction update: r, p_old read, p written; SpMV: p, ax, ay, az read, q written
     "cg_p_fp32": 3 * 4, "cg_spmv_fp32": 5 * 4, "cg_update_fp32": 6 * 4,
+    # fused direction update + SpMV: r, p_old, ax, ay, az read, p, q written
+    "cg_pq_fp32": 7 * 4,
     # x read (8) + y (4) + sinv (4) read, x written (8)
     "xupdate_mixed": 8 + 4 + 4 + 8,
     # x, y, sinv read and x written (8 B each)
@@ -57,6 +59,41 @@ BYTES_PER_CELL = {
 # residual does 7 FMA for S - Hx and 1 FMA for ||r||^2; the RHS 2 mul (rho c T/dt), 1 FMA + 1 mul
 # (S_cat), 1 add, 2 add + 1 sub (x0 and its test), 1 FMA (||S||^2).
 FP64_FLOPS_PER_CELL = {"residual_mixed": 16, "residual_fp64": 18, "rhs": 12}
+
+# Algorithmic bytes per cell of each round of the persistent solve kernel (k_solve), by phase:
+# (bytes, bytes of the first inner iteration / of an update without a correction).  The first
+# residual also reads H*1 (the x0 + TINY rule applies on this workload: far-field cells do not
+# move, so x0 - T < TINY somewhere every step).
+PHASE_BYTES = {
+    "mixed": {"res_init": (64, 64), "res": (56, 56), "cg_pq": (28, 24), "cg_b": (24, 20),
+              "xupd": (24, 16)},
+    "fp64": {"res_init": (72, 72), "res": (64, 64), "cg_p": (24, 16), "cg_q": (40, 40),
+             "cg_b": (48, 40), "xupd": (32, 16)},
+}
+
+
+def solve_bytes_per_cell(rounds, precision):
+    """Algorithmic bytes per cell of one persistent-solve launch from its round phases."""
+    table = PHASE_BYTES[precision]
+    total, first_cg, first_b, have_y = 0, True, True, False
+    for ph, _ in rounds:
+        full, alt = table.get(ph, (0, 0))
+        if ph in ("res_init", "res"):
+            total += full
+            first_cg = first_b = True
+            have_y = False
+        elif ph in ("cg_pq", "cg_p"):
+            total += alt if first_cg else full
+            first_cg = False
+        elif ph == "cg_q":
+            total += full
+        elif ph == "cg_b":
+            total += alt if first_b else full
+            first_b = False
+            have_y = True
+        elif ph == "xupd":
+            total += full if have_y else alt
+    return total
 
 
 def parse():
@@ -287,35 +324,48 @@ def main():
     cell_iters = N * (st["inner_iterations"] + st["iterations"] + st["refinements"])
     cell_iters_per_s = world * cell_iters / (ms / 1000.0)
 
-    # ---- kernel roofline: each kernel timed alone with CUDA events on the library's stream
-    kernels = {"rhs": abi.HF_KERNEL_RHS, "residual_mixed": abi.HF_KERNEL_RESIDUAL,
-               "xupdate_mixed": abi.HF_KERNEL_XUPDATE, "cg_p_fp32": abi.HF_KERNEL_CG_P,
-               "cg_spmv_fp32": abi.HF_KERNEL_CG_SPMV,
-               "cg_update_fp32": abi.HF_KERNEL_CG_UPDATE}
-    kms = {name: hf.time_kernel(k, reps=20) for name, k in kernels.items()}
-    per_step_launches = {
-        "rhs": 1.0, "residual_mixed": st["refinements"] / K,
-        "xupdate_mixed": max(st["refinements"] / K - 1.0, 0.0),
-        "cg_p_fp32": st["inner_iterations"] / K, "cg_spmv_fp32": st["inner_iterations"] / K,
-        "cg_update_fp32": st["inner_iterations"] / K,
-    }
-    share = {k: kms[k] * per_step_launches[k] for k in kms}
-    dominant = max(share, key=share.get)
+    # ---- kernel roofline.  The dominant kernel is the persistent solve (k_solve: the whole
+    # refinement loop of a step in one cooperative launch); it and the RHS kernel are timed alone
+    # with CUDA events on the library's stream.  The solve's algorithmic bytes come from the phase
+    # of every grid-wide round of the timed launches (the kernel's own round log).
     peak, peak_kind = measured_peak()
+    prec = "mixed"
+    solve_ms = hf.time_kernel(abi.HF_KERNEL_SOLVE, reps=10)
+    rounds, nrounds = hf.solve_profile()
+    solve_bpc = solve_bytes_per_cell(rounds, prec)
+    rhs_ms = hf.time_kernel(abi.HF_KERNEL_RHS, reps=10)
+    phases = {}
+    for ph, us in rounds:
+        e = phases.setdefault(ph, {"rounds": 0, "us": 0.0})
+        e["rounds"] += 1
+        e["us"] += us
+    for ph, e in phases.items():
+        full, alt = PHASE_BYTES[prec].get(ph, (0, 0))
+        e["us_per_round"] = e["us"] / e["rounds"]
+        e["GB/s_upper"] = full * N / (e["us_per_round"] * 1e-6) / 1e9 if full else None
+    kernels = {"cg_p_fp32": abi.HF_KERNEL_CG_P, "cg_spmv_fp32": abi.HF_KERNEL_CG_SPMV,
+               "cg_pq_fp32": abi.HF_KERNEL_CG_PQ, "cg_update_fp32": abi.HF_KERNEL_CG_UPDATE,
+               "xupdate_mixed": abi.HF_KERNEL_XUPDATE, "residual_mixed": abi.HF_KERNEL_RESIDUAL}
+    kms = {name: hf.time_kernel(k, reps=10) for name, k in kernels.items()}
+    kms["rhs"] = rhs_ms
     f64 = C.c_double()
     f32 = C.c_double()
     rc = abi.load_library().hf_measure_fp_rates(C.byref(f64), C.byref(f32))
     fp_rates = {"fp64_tflops": f64.value, "fp32_tflops": f32.value} if rc == 0 else None
-    bpc = BYTES_PER_CELL[dominant]
-    achieved = bpc * N / (kms[dominant] / 1000.0) / 1e9
-    traffic = ncu_traffic().get(dominant)
-    roofline = {"kernel": dominant, "bound": "hbm", "achieved": achieved, "peak": peak,
-                "unit": "GB/s", "frac": achieved / peak, "peak_kind": f"of {peak_kind}",
+    achieved = solve_bpc * N / (solve_ms / 1000.0) / 1e9
+    traffic = ncu_traffic().get("solve_mixed")
+    roofline = {"kernel": "k_solve<float> (persistent cooperative solve, one launch per step)",
+                "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_kind": f"of {peak_kind}",
                 "traffic": traffic * N if traffic else None,
-                "algorithmic_bytes_per_launch": bpc * N,
+                "algorithmic_bytes_per_launch": solve_bpc * N, "ms_per_launch": solve_ms,
+                "rounds_per_launch": nrounds, "share_of_step": solve_ms / (ms / K),
+                "phases": phases,
                 "kernels": {k: {"ms": kms[k], "GB/s": BYTES_PER_CELL[k] * N / (kms[k] / 1000.0) / 1e9,
-                                "frac": BYTES_PER_CELL[k] * N / (kms[k] / 1000.0) / 1e9 / peak,
-                                "launches_per_step": per_step_launches[k]} for k in kms}}
+                                "frac": BYTES_PER_CELL[k] * N / (kms[k] / 1000.0) / 1e9 / peak}
+                            for k in kms},
+                "note": "phases' GB/s_upper assume every round of that phase moved its full bytes; "
+                        "standalone kernels are timed repeatedly on the same data (partly L2-resident)"}
     if fp_rates:
         roofline["fp64"] = {
             k: {"achieved_tflops": FP64_FLOPS_PER_CELL[k] * N / (kms[k] / 1000.0) / 1e12,
@@ -335,6 +385,8 @@ def main():
         barrier()
         ms64, st64 = timed_run(h2, torch, stream, W + 1, K)
         ms64 = max_over_ranks(ms64)
+        solve64 = h2.time_kernel(abi.HF_KERNEL_SOLVE, 10)
+        r64, n64 = h2.solve_profile()
         k64 = {"residual_fp64": h2.time_kernel(abi.HF_KERNEL_RESIDUAL, 10),
                "xupdate_fp64": h2.time_kernel(abi.HF_KERNEL_XUPDATE, 10),
                "cg_spmv_fp64": h2.time_kernel(abi.HF_KERNEL_CG_SPMV, 10),
@@ -344,6 +396,8 @@ def main():
                 "iterations_per_step": st64["iterations"] / K,
                 "refinements_per_step": st64["refinements"] / K,
                 "last_true_relres": st64["last_true_relres"],
+                "solve": {"ms": solve64, "rounds": n64,
+                          "GB/s": solve_bytes_per_cell(r64, "fp64") * N / (solve64 / 1000.0) / 1e9},
                 "kernels": {k: {"ms": v, "GB/s": BYTES_PER_CELL[k] * N / (v / 1000.0) / 1e9}
                             for k, v in k64.items()}}
         h2.close()
