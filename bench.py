@@ -353,11 +353,13 @@ def main():
     rc = abi.load_library().hf_measure_fp_rates(C.byref(f64), C.byref(f32))
     fp_rates = {"fp64_tflops": f64.value, "fp32_tflops": f32.value} if rc == 0 else None
     achieved = solve_bpc * N / (solve_ms / 1000.0) / 1e9
-    traffic = ncu_traffic().get("solve_mixed")
+    ratio = ncu_traffic().get("solve_mixed_ratio")     # DRAM bytes per algorithmic byte (ncu)
     roofline = {"kernel": "k_solve<float> (persistent cooperative solve, one launch per step)",
                 "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_kind": f"of {peak_kind}",
-                "traffic": traffic * N if traffic else None,
+                "traffic": ratio * solve_bpc * N if ratio else None,
+                "traffic_source": "ncu DRAM read+write of an 11-round k_solve launch at 256^3 per "
+                                  "algorithmic byte, times this launch's algorithmic bytes",
                 "algorithmic_bytes_per_launch": solve_bpc * N, "ms_per_launch": solve_ms,
                 "rounds_per_launch": nrounds, "share_of_step": solve_ms / (ms / K),
                 "phases": phases,
