@@ -1233,7 +1233,7 @@ __device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
 template <typename T>
 __device__ __forceinline__ int32_t phase_after(const InstScal& s) {
   if (!s.outer_active) return PH_IDLE;
-  if (s.inner_active) return sizeof(T) == 4 ? PH_CG_PQ : PH_CG_P;
+  if (s.inner_active) return PH_CG_P;   // the fused FP32 pass (PH_CG_PQ) measured slower
   return PH_XUPD;
 }
 __device__ __forceinline__ int phase_partials(int32_t ph) {
@@ -1363,8 +1363,9 @@ __device__ bool grid_barrier_epilogue(const DevArrays& A, SolveCtl* ctl, unsigne
 template <typename T>
 __device__ __forceinline__ void round_task(const DevArrays& A, double* part, int64_t task,
                                            const InstScal& s) {
-  if (sizeof(T) == 4 && s.phase == PH_CG_PQ) {
-    pq_f32_task<true>(A, part, task, s);
+  if (sizeof(T) == 4 && (s.phase == PH_CG_PQ || s.phase == PH_CG_Q)) {
+    if (s.phase == PH_CG_PQ) pq_f32_task<true>(A, part, task, s);
+    else pq_f32_task<false>(A, part, task, s);
     return;
   }
   switch (s.phase) {
