@@ -108,6 +108,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the default task depth and inner tolerance")
     ap.add_argument("--host-loop", action="store_true",
                     help="drive the solve loop from the host instead of the captured graph")
     ap.add_argument("--cpu-seconds", type=float, default=90.0,
@@ -315,6 +317,13 @@ def main():
     hf.initial_evolve()
     if W:
         hf.run(1, W)
+    tuned = {}
+    if not args.no_autotune:        # task depth and inner tolerance, timed on this problem
+        t0 = time.perf_counter()
+        cand = hf.autotune(itime0=W + 1, steps=3)
+        best = next(r for r in cand if r["chosen"])
+        tuned["mixed"] = {"task_depth": best["task_depth"], "inner_tol": best["inner_tol"],
+                          "candidates": len(cand), "seconds": time.perf_counter() - t0}
     barrier()
     with ClockSampler(torch.cuda.current_device()) as clk:
         ms, st = timed_run(hf, torch, stream, W + 1, K)
@@ -384,6 +393,10 @@ def main():
         h2.initial_evolve()
         if W:
             h2.run(1, W)
+        if not args.no_autotune:
+            cand = h2.autotune(itime0=W + 1, steps=3)
+            best = next(r for r in cand if r["chosen"])
+            tuned["fp64"] = {"task_depth": best["task_depth"], "candidates": len(cand)}
         barrier()
         ms64, st64 = timed_run(h2, torch, stream, W + 1, K)
         ms64 = max_over_ranks(ms64)
@@ -439,7 +452,7 @@ def main():
             "metric": METRIC, "value": steps_per_s, "unit": UNIT, "n_gpus": world, "steps": K,
             "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
-            "config": workload_config(args, prob),
+            "config": dict(workload_config(args, prob), autotuned=tuned),
             "cell_iters_per_s": cell_iters_per_s,
             "iterations_per_step": {"fp32_cg": st["inner_iterations"] / K,
                                     "fp64_refinement_sweeps": st["refinements"] / K},

@@ -61,6 +61,11 @@ class HfSolverOpts(C.Structure):
     ]
 
 
+class HfTuneResult(C.Structure):
+    _fields_ = [("task_depth", C.c_int32), ("chosen", C.c_int32), ("inner_tol", C.c_double),
+                ("ms_per_step", C.c_double)]
+
+
 class HfStats(C.Structure):
     _fields_ = [
         ("steps", C.c_int64), ("iterations", C.c_int64), ("inner_iterations", C.c_int64),
@@ -111,6 +116,8 @@ _SIGNATURES = {
     "hf_measure_fp_rates": (C.c_int, [_dp, _dp]),
     "hf_solve_profile": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_int64),
                                    C.POINTER(C.c_int32), _dp]),
+    "hf_autotune": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.POINTER(HfTuneResult), C.c_int32,
+                              C.POINTER(C.c_int32)]),
     "hf_set_state_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "hf_residual_noalloc": (C.c_int, [C.c_int64, C.c_int64, C.c_int64, C.POINTER(C.c_int32),
                                       C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,

@@ -819,9 +819,21 @@ int hf_step(hf_ctx* h, int64_t itime, hf_stats* stats) {
   return hf_run(h, itime, 1, stats);
 }
 
+}  // extern "C"
+namespace {
+int run_steps(Ctx& c, int64_t itime0, int64_t nsteps, hf_stats* stats);
+}
+extern "C" {
+
 int hf_run(hf_ctx* h, int64_t itime0, int64_t nsteps, hf_stats* stats) {
   if (!h || nsteps < 0) return set_err(HF_EARG, "null context or nsteps < 0");
-  Ctx& c = h->c;
+  return run_steps(h->c, itime0, nsteps, stats);
+}
+
+}  // extern "C"
+
+namespace {
+int run_steps(Ctx& c, int64_t itime0, int64_t nsteps, hf_stats* stats) {
   if (!c.state_set) return set_err(HF_ESTATE, "hf_set_state must be called before stepping");
   int rc = sync_scal(c);
   if (rc) return rc;
@@ -860,6 +872,94 @@ int hf_run(hf_ctx* h, int64_t itime0, int64_t nsteps, hf_stats* stats) {
   fill_stats(c, stats, done, before);
   if (stats) stats->kernel_launches = c.launches - launches0;
   return first_error(c);
+}
+
+// Saved temperature state and scalars of all instances (autotuner).
+struct Snapshot {
+  double* t = nullptr;                  // [T^n | T^(n-1)] of every instance, cells in order
+  std::vector<InstScal> scal;
+};
+int snapshot_take(Ctx& c, Snapshot& sn) {
+  int rc = sync_scal(c);
+  if (rc) return rc;
+  sn.scal.assign(c.h_scal, c.h_scal + c.ninst);
+  CU(cudaMalloc((void**)&sn.t, sizeof(double) * 2 * (size_t)c.ncells));
+  for (int64_t i = 0; i < c.ninst; ++i) {
+    const InstDesc& d = c.h_inst[i];
+    for (int k = 0; k < 2; ++k)
+      CU(cudaMemcpyAsync(sn.t + k * c.ncells + d.off, c.A.tbuf[sn.scal[i].role[k]] + d.off,
+                         8 * (size_t)d.n, cudaMemcpyDeviceToDevice, c.stream));
+  }
+  CU(cudaStreamSynchronize(c.stream));
+  return HF_OK;
+}
+int snapshot_restore(Ctx& c, const Snapshot& sn) {
+  for (int64_t i = 0; i < c.ninst; ++i) {
+    const InstDesc& d = c.h_inst[i];
+    for (int k = 0; k < 2; ++k)
+      CU(cudaMemcpyAsync(c.A.tbuf[sn.scal[i].role[k]] + d.off, sn.t + k * c.ncells + d.off,
+                         8 * (size_t)d.n, cudaMemcpyDeviceToDevice, c.stream));
+  }
+  std::memcpy(c.h_scal, sn.scal.data(), sizeof(InstScal) * c.ninst);
+  return push_scal(c);
+}
+}  // namespace
+
+extern "C" {
+
+int hf_autotune(hf_ctx* h, int64_t itime0, int32_t steps, hf_tune_result* results, int32_t cap,
+                int32_t* n_results) {
+  if (!h || steps < 1 || cap < 0 || (cap > 0 && !results)) return set_err(HF_EARG, "bad arguments");
+  Ctx& c = h->c;
+  if (!c.state_set) return set_err(HF_ESTATE, "hf_set_state must be called first");
+  Snapshot sn;
+  int rc = snapshot_take(c, sn);
+  if (rc) { cudaFree(sn.t); return rc; }
+  const hf_solver_opts base = c.opts;
+  const bool mixed = base.precision == HF_PREC_MIXED;
+  const int depths[3] = {8, 16, 32};
+  const double tols[3] = {1e-4, 1e-5, 1e-6};
+  const int ntol = mixed ? 3 : 1;
+  std::vector<hf_tune_result> all;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  auto finish = [&](int code) {
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    cudaFree(sn.t);
+    return code;
+  };
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+    return finish(set_err(HF_ECUDA, "cudaEventCreate failed"));
+  for (int di = 0; di < 3; ++di) {
+    for (int ti = 0; ti < ntol; ++ti) {
+      hf_solver_opts o = base;
+      o.task_depth = depths[di];
+      if (mixed) o.inner_tol = tols[ti];
+      if ((rc = hf_set_opts(h, &o))) return finish(rc);
+      if ((rc = snapshot_restore(c, sn))) return finish(rc);
+      if ((rc = run_steps(c, itime0, 1, nullptr))) return finish(rc);     // warm-up (and capture)
+      if ((rc = snapshot_restore(c, sn))) return finish(rc);
+      if (cudaEventRecord(e0, c.stream) != cudaSuccess) return finish(set_err(HF_ECUDA, "event"));
+      if ((rc = run_steps(c, itime0, steps, nullptr))) return finish(rc);
+      if (cudaEventRecord(e1, c.stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess)
+        return finish(set_err(HF_ECUDA, "event"));
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      all.push_back(hf_tune_result{depths[di], 0, o.inner_tol, (double)ms / steps});
+    }
+  }
+  size_t best = 0;
+  for (size_t k = 1; k < all.size(); ++k)
+    if (all[k].ms_per_step < all[best].ms_per_step) best = k;
+  all[best].chosen = 1;
+  hf_solver_opts o = base;
+  o.task_depth = all[best].task_depth;
+  if (mixed) o.inner_tol = all[best].inner_tol;
+  if ((rc = hf_set_opts(h, &o))) return finish(rc);
+  if ((rc = snapshot_restore(c, sn))) return finish(rc);
+  if (n_results) *n_results = (int32_t)std::min<size_t>(all.size(), (size_t)cap);
+  for (size_t k = 0; k < all.size() && (int32_t)k < cap; ++k) results[k] = all[k];
+  return finish(HF_OK);
 }
 
 }  // extern "C"

@@ -112,6 +112,20 @@ class HeatFlow:
         n = min(rounds.value, cap, 64)
         return [(abi.PHASE_NAMES.get(ph[i], str(ph[i])), us[i]) for i in range(n)], rounds.value
 
+    def autotune(self, itime0: int = 1, steps: int = 3):
+        """Choose the task depth (and, mixed, the inner tolerance) by timing `steps` steps of this
+        problem per candidate; state and statistics are unchanged.  Returns the candidates."""
+        res = (abi.HfTuneResult * 16)()
+        n = C.c_int32()
+        abi.check(self.lib.hf_autotune(self.h, int(itime0), int(steps), res, 16, C.byref(n)),
+                  "hf_autotune")
+        out = [dict(task_depth=r.task_depth, inner_tol=r.inner_tol, ms_per_step=r.ms_per_step,
+                    chosen=bool(r.chosen)) for r in res[:n.value]]
+        best = next(r for r in out if r["chosen"])
+        self.opts.task_depth = best["task_depth"]
+        self.opts.inner_tol = best["inner_tol"]
+        return out
+
     # ---- options
     def set_opts(self, **opts):
         self.opts = make_opts(**opts)

@@ -238,6 +238,23 @@ enum {
  * round's length in microseconds (device %globaltimer; round 0 counts from the kernel's start). */
 int hf_solve_profile(hf_ctx* ctx, int64_t cap, int64_t* rounds, int32_t* phases, double* round_us);
 
+/* ---- autotuner ------------------------------------------------------------------------------
+ * No counterpart in the reference.  Chooses the stencil task shape (z-planes per 32 x 8 column
+ * tile: 8, 16 or 32) and, on the mixed path, the inner FP32 tolerance (1e-4, 1e-5, 1e-6) for this
+ * context's own grids: for every candidate it restores the current state, runs one untimed step
+ * and then `steps` steps from step `itime0` timed with CUDA events through the context's step loop
+ * (use_graph as set), and keeps the fastest.  On return the options hold the choice and the state,
+ * the scalars and the statistics are those of the call (the tuning steps leave no trace).
+ * results (may be NULL): up to cap candidates with their measured time per step. */
+typedef struct hf_tune_result {
+  int32_t task_depth;
+  int32_t chosen;        /* 1 for the candidate kept */
+  double inner_tol;
+  double ms_per_step;
+} hf_tune_result;
+int hf_autotune(hf_ctx* ctx, int64_t itime0, int32_t steps, hf_tune_result* results, int32_t cap,
+                int32_t* n_results);
+
 /* ---- allocation-free residual ---------------------------------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device memory - hosts that
  * own all device memory through a fixed arena and hand the library pre-allocated buffers, and

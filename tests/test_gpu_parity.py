@@ -299,3 +299,31 @@ def test_graph_nan_stops(cuda_lib, g):
         with pytest.raises(abi.HeatFlowError) as e:
             hf.run(1, 3)
         assert e.value.code == abi.HF_ENAN_S
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_autotune_leaves_state_and_picks_a_candidate(cuda_lib, precision):
+    """The autotuner times every candidate from the same state and restores it: the state and the
+    step statistics are unchanged, and stepping afterwards equals a fresh context created with the
+    chosen options."""
+    rng = np.random.default_rng(3)
+    probs = [point_source_cube(12), random_instance(rng, lo=8, hi=20)]
+    kw = dict(precision=precision, criterion="true", tol=1e-10, use_graph=1)
+    with HeatFlow(probs, **kw) as hf:
+        hf.initial_evolve()
+        hf.run(1, 2)
+        before = hf.get_state()
+        res = hf.autotune(itime0=3, steps=2)
+        assert len(res) == (9 if precision == "mixed" else 3)
+        assert sum(r["chosen"] for r in res) == 1 and all(r["ms_per_step"] > 0 for r in res)
+        best = next(r for r in res if r["chosen"])
+        after = hf.get_state()
+        assert np.array_equal(before[0], after[0]) and np.array_equal(before[1], after[1])
+        st = hf.run(3, 3)
+        T = hf.get_state()[0]
+    with HeatFlow(probs, task_depth=best["task_depth"], inner_tol=best["inner_tol"], **kw) as h2:
+        h2.set_state(*before)
+        st2 = h2.run(3, 3)
+        T2 = h2.get_state()[0]
+    assert np.array_equal(T, T2)
+    assert st["inner_iterations"] == st2["inner_iterations"]
