@@ -124,6 +124,22 @@ def dist_info():
     return rank, world, local
 
 
+def reduce_max(v, dist=None, device="cuda"):
+    """Max of a per-rank timing over all ranks (identity without a process group)."""
+    if dist is None:
+        return v
+    import torch
+    t = torch.tensor([v], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_rate(world, steps, ms_max):
+    """Whole-job rate of `world` independent replicas, each advancing `steps` steps, timed by the
+    slowest rank (weak scaling: the per-rank work is fixed)."""
+    return world * steps / (ms_max / 1000.0)
+
+
 def measured_peak():
     path = os.path.join(HERE, "MEASURED_PEAKS.json")
     if os.path.exists(path):
@@ -299,11 +315,7 @@ def main():
         torch.cuda.synchronize()
 
     def max_over_ranks(v):
-        if dist is None:
-            return v
-        t = torch.tensor([v], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return reduce_max(v, dist, "cuda")
 
     prob = layered_slab(args.n, icattaneo=0 if args.fourier else 1)
     N = prob.ncells
@@ -329,7 +341,7 @@ def main():
         ms, st = timed_run(hf, torch, stream, W + 1, K)
     ms = max_over_ranks(ms)
     clocks = clk.summary()
-    steps_per_s = world * K / (ms / 1000.0)
+    steps_per_s = aggregate_rate(world, K, ms)
     cell_iters = N * (st["inner_iterations"] + st["iterations"] + st["refinements"])
     cell_iters_per_s = world * cell_iters / (ms / 1000.0)
 
@@ -407,7 +419,7 @@ def main():
                "cg_spmv_fp64": h2.time_kernel(abi.HF_KERNEL_CG_SPMV, 10),
                "cg_update_fp64": h2.time_kernel(abi.HF_KERNEL_CG_UPDATE, 10),
                "cg_p_fp64": h2.time_kernel(abi.HF_KERNEL_CG_P, 10)}
-        fp64 = {"steps_per_s": world * K / (ms64 / 1000.0), "ms_per_step": ms64 / K,
+        fp64 = {"steps_per_s": aggregate_rate(world, K, ms64), "ms_per_step": ms64 / K,
                 "iterations_per_step": st64["iterations"] / K,
                 "refinements_per_step": st64["refinements"] / K,
                 "last_true_relres": st64["last_true_relres"],
