@@ -432,22 +432,23 @@ def main():
     # ---- end to end through the C ABI with host buffers
     e2e = None
     if not args.no_e2e:
-        h3 = HeatFlow(prob, precision="mixed", criterion="true", tol=args.tol, use_graph=graph)
+        kw3 = {}
+        if "mixed" in tuned:
+            kw3 = dict(task_depth=tuned["mixed"]["task_depth"], inner_tol=tuned["mixed"]["inner_tol"])
+        h3 = HeatFlow(prob, precision="mixed", criterion="true", tol=args.tol, use_graph=graph, **kw3)
         h3.set_stream(stream.cuda_stream)
         tp = torch.full((N,), prob.t_system, dtype=torch.float64).pin_memory().numpy()
         tpp = torch.full((N,), prob.t_system, dtype=torch.float64).pin_memory().numpy()
         for k in range(W):
             h3.set_state(tp, tpp)
             h3.simulate(k + 1)
-            tp[:], tpp[:] = h3.get_state()
+            h3.get_state(out=(tp, tpp))
         barrier()
         t0 = time.perf_counter()
-        for k in range(K):
+        for k in range(K):                 # inputs in and results out through pinned buffers
             h3.set_state(tp, tpp)
             h3.simulate(W + 1 + k)
-            a, b = h3.get_state()
-            tp[:] = a
-            tpp[:] = b
+            h3.get_state(out=(tp, tpp))
         torch.cuda.synchronize()
         e2e_s = max_over_ranks(time.perf_counter() - t0)
         e2e = {"value": world * K / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * N,

@@ -143,9 +143,16 @@ class HeatFlow:
         t = np.concatenate([np.full(p.ncells, p.t_system) for p in self.problems])
         self.set_state(t, t)
 
-    def get_state(self):
-        tp = np.empty(self.n)
-        tpp = np.empty(self.n)
+    def get_state(self, out=None):
+        """(T^n, T^(n-1)) in cell order; `out` = two contiguous float64 arrays to fill (e.g.
+        pinned host buffers, which the copies then reach without staging)."""
+        if out is None:
+            tp, tpp = np.empty(self.n), np.empty(self.n)
+        else:
+            tp, tpp = out
+            assert tp.dtype == np.float64 and tpp.dtype == np.float64
+            assert tp.flags.c_contiguous and tpp.flags.c_contiguous
+            assert tp.size == self.n and tpp.size == self.n
         abi.check(self.lib.hf_get_state(self.h, _d(tp), _d(tpp)), "hf_get_state")
         return tp, tpp
 
