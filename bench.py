@@ -65,8 +65,8 @@ FP64_FLOPS_PER_CELL = {"residual_mixed": 16, "residual_fp64": 18, "rhs": 12}
 # residual also reads H*1 (the x0 + TINY rule applies on this workload: far-field cells do not
 # move, so x0 - T < TINY somewhere every step).
 PHASE_BYTES = {
-    "mixed": {"res_init": (64, 64), "res": (56, 56), "cg_pq": (28, 24), "cg_b": (24, 20),
-              "xupd": (24, 16)},
+    "mixed": {"res_init": (64, 64), "res": (56, 56), "cg_p": (12, 8), "cg_q": (20, 20),
+              "cg_pq": (28, 24), "cg_b": (24, 20), "xupd": (24, 16)},
     "fp64": {"res_init": (72, 72), "res": (64, 64), "cg_p": (24, 16), "cg_q": (40, 40),
              "cg_b": (48, 40), "xupd": (32, 16)},
 }
@@ -271,9 +271,11 @@ def workload_config(args, prob):
                     f"{'Fourier' if args.fourier else 'Cattaneo'}, top-face Gaussian heating",
         "cells": prob.ncells, "dx_m": 1e-9, "dt_s": 1e-13, "rel_res": args.tol,
         "layers": "z-alternating every 16 cells, kappa 149 / 0.2",
-        "l2": "inputs larger than L2: ~3.7 GB resident per grid, no flush needed",
+        "l2": f"inputs larger than L2: ~{prob.ncells * 230 / 1e9:.1f} GB resident per grid "
+              f"(L2 129 MB), no flush needed",
         "parallelism": f"replicas x{args.gpus}",
-        "step_loop": "host-polled" if args.host_loop else "CUDA graph per step (conditional WHILE/SWITCH)",
+        "step_loop": "host-polled kernels" if args.host_loop else
+                     "CUDA graph per step: RHS + one persistent cooperative solve kernel",
     }
 
 
