@@ -40,12 +40,140 @@ __device__ __forceinline__ double heat_case(int cs, double P, double tau, int64_
   }
 }
 
+// The per-cell work of the step RHS (shared by the scalar and the vector forms): heater, S_cat,
+// S and the initial guess of cell l; returns S and sets x0 and the x0 - T < TINY flag.
+struct RhsCtx {
+  bool heater, has_power, has_em, case5, cat, steady;
+  int qmode;
+  double inv_dt, vol, hvol, power_in, tb4, dt2;
+  int64_t itime;
+};
+// Heat density of cell l (the heater branch, out of line so the common heater-free tasks keep
+// a small register footprint).
+__device__ __noinline__ double rhs_qdens(const DevArrays& A, const InstDesc& d, const RhsCtx& r,
+                                         int64_t off, int l, double tp) {
+  double q = 0.0, qd = 0.0;
+  {
+    const int cs = A.icase[off + l];
+    if (cs > 0 && cs < 7) {
+      const double P = r.has_power ? A.power[off + l] : r.power_in;
+      const double tau = r.case5 ? A.tau_s[off + l] * r.dt2 : 0.0;
+      q = heat_case(cs, P, tau, r.itime, d);
+    }
+    if (r.has_em) q = q - A.emc[off + l] * (pow(tp, 4.0) - r.tb4);
+    if (!dbl_is_zero(q)) {
+      if (r.qmode == HF_QDENS_CELL_VOLUME) qd = q / r.vol;
+      else if (r.hvol > 0.0) qd = q / r.hvol;
+    }
+  }
+  return qd;
+}
+
+template <bool HEAT>
+__device__ __forceinline__ double rhs_cell(const DevArrays& A, const InstDesc& d, const RhsCtx& r,
+                                           int64_t off, int l, double tp, double tpp, double rhoc,
+                                           double ccat, double B, double& x0, int& flag) {
+  const double qd = HEAT ? rhs_qdens(A, d, r, off, l, tp) : 0.0;
+  double S;
+  if (!r.steady) {
+    S = -r.inv_dt * tp * rhoc;
+    if (!dbl_is_zero(qd)) S = S - qd;
+    if (!dbl_is_zero(B)) S = S - B;
+    if (r.cat) S = S + fma(-2.0, tp, tpp) * ccat;   // (tpp - 2 tp) * ccat: 2 tp is exact
+  } else {
+    S = -qd;
+    if (!dbl_is_zero(B)) S = S - B;
+  }
+  x0 = tp + (tp - tpp);
+  flag |= dbl_lt_pos(x0 - tp, kTiny) ? 1 : 0;
+  return S;
+}
+
+// Vector form for rows of 4k cells: each thread owns 4 consecutive x cells of a quarter of the
+// task's planes (the layout of the solver's vector passes), so every thread has 4 independent
+// cells of FP64 work in flight: the pass is bound by the FP64 pipe, and one cell per thread left
+// it partly idle.  ||S||^2 is summed per thread plane by plane, cells in x order.
+__device__ __forceinline__ void rhs4_task(const DevArrays& A, int64_t task, const InstDesc& d,
+                                          const InstScal& s, const RhsCtx& r) {
+  const int4 tk = A.tasks[task];
+  const int tid = threadIdx.x, grp = tid >> 6, w = tid & 63;
+  const int x = tk.y + 4 * (w & 7), y = tk.z + (w >> 3);
+  const int z1 = min(tk.w + d.zc, d.nz);
+  const int per = (z1 - tk.w + 3) >> 2;
+  const int za = min(tk.w + grp * per, z1), zb = min(za + per, z1);
+  const bool act = x < d.nx && y < d.ny;
+  const int64_t off = d.off;
+  const int nxy = d.nx * d.ny, lxy = y * d.nx + x;
+  const double* Tp = A.tbuf[s.role[0]] + off;
+  const double* Tpp = A.tbuf[s.role[1]] + off;
+  double* X = A.tbuf[s.role[2]] + off;
+  const double* __restrict__ rhoc = A.rhoc + off;
+  const double* __restrict__ ccat = A.ccat + off;
+  const double* __restrict__ bvec = A.bvec + off;
+  double* bout = A.b + off;
+  double bb = 0.0;
+  int flag = 0;
+  if (act) {
+    for (int z = za; z < zb; ++z) {
+      const int l = lxy + z * nxy;
+      const double2* tp2 = reinterpret_cast<const double2*>(Tp + l);
+      const double2* tq2 = reinterpret_cast<const double2*>(Tpp + l);
+      const double2* rc2 = reinterpret_cast<const double2*>(rhoc + l);
+      const double2* cc2 = reinterpret_cast<const double2*>(ccat + l);
+      const double2* bv2 = reinterpret_cast<const double2*>(bvec + l);
+      const double2 t0 = tp2[0], t1 = tp2[1], u0 = tq2[0], u1 = tq2[1];
+      const double2 h0 = rc2[0], h1 = rc2[1], c0 = cc2[0], c1 = cc2[1], b0 = bv2[0], b1 = bv2[1];
+      const double tp[4] = {t0.x, t0.y, t1.x, t1.y}, tpp[4] = {u0.x, u0.y, u1.x, u1.y};
+      const double rh[4] = {h0.x, h0.y, h1.x, h1.y}, cc[4] = {c0.x, c0.y, c1.x, c1.y};
+      const double bv[4] = {b0.x, b0.y, b1.x, b1.y};
+      double S[4], x0[4];
+      if (r.heater) {
+        for (int i = 0; i < 4; ++i)
+          S[i] = rhs_cell<true>(A, d, r, off, l + i, tp[i], tpp[i], rh[i], cc[i], bv[i], x0[i], flag);
+      } else {
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          S[i] = rhs_cell<false>(A, d, r, off, l + i, tp[i], tpp[i], rh[i], cc[i], bv[i], x0[i], flag);
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i) bb = fma(S[i], S[i], bb);
+      reinterpret_cast<double2*>(bout + l)[0] = make_double2(S[0], S[1]);
+      reinterpret_cast<double2*>(bout + l)[1] = make_double2(S[2], S[3]);
+      reinterpret_cast<double2*>(X + l)[0] = make_double2(x0[0], x0[1]);
+      reinterpret_cast<double2*>(X + l)[1] = make_double2(x0[2], x0[3]);
+    }
+  }
+  const int any_flag = __syncthreads_or(flag);
+  if (threadIdx.x == 0) A.partials[task * kNR + 1] = any_flag ? 1.0 : 0.0;
+  const double v[1] = {bb};
+  tile_store<1>(A, task, v);
+}
+
 // One block per task.  PARTS: also write B, Q, Qdens and S_cat (parity probe hf_get_rhs).
 // DIAG: count NaNs per vector (failure path only).
 template <bool PARTS, bool DIAG>
-__global__ void __launch_bounds__(kBlock) k_rhs(DevArrays A, double* oB, double* oQ, double* oQd,
+__global__ void __launch_bounds__(kBlock, 4) k_rhs(DevArrays A, double* oB, double* oQ, double* oQd,
                                                 double* oSc) {
   const int64_t task = blockIdx.x;
+  if (!PARTS && !DIAG) {          // the step's pass: vector form where the rows allow it
+    const int inst = A.tasks[task].x;
+    const InstDesc& d = A.inst[inst];
+    const InstScal& s = A.scal[inst];
+    if ((d.nx & 3) == 0) {
+      if (!s.outer_active) return;
+      RhsCtx r;
+      r.heater = d.heater && (d.has_em || A.task_heat[task]);
+      r.has_power = d.has_power; r.has_em = d.has_em; r.case5 = d.has_case5;
+      r.cat = d.icattaneo == 1; r.steady = d.isteady != 0;
+      r.qmode = d.qdens_mode;
+      r.inv_dt = d.inv_dt; r.vol = d.volume; r.hvol = d.heated_volume; r.power_in = d.power_in;
+      r.tb4 = d.has_em ? pow(d.t_bath, 4.0) : 0.0;
+      r.dt2 = d.has_case5 ? pow(d.time_step, 2.0) : 0.0;
+      r.itime = s.itime;
+      rhs4_task(A, task, d, s, r);
+      return;
+    }
+  }
   const TCell c = task_cell(A, task);
   const InstDesc& d = A.inst[c.inst];
   InstScal& s = A.scal[c.inst];
