@@ -108,6 +108,15 @@ void drop_graph(Ctx& c) {
 
 void free_all(Ctx& c) {
   drop_graph(c);
+  if (c.copy_stream) cudaStreamSynchronize(c.copy_stream);
+  for (auto& sl : c.sub) {
+    if (sl.dev) cudaFree(sl.dev);
+    if (sl.gathered) cudaEventDestroy(sl.gathered);
+    if (sl.copied) cudaEventDestroy(sl.copied);
+    sl = Ctx::SubSlot{};
+  }
+  if (c.copy_stream) cudaStreamDestroy(c.copy_stream);
+  c.copy_stream = nullptr;
   for (void* p : c.allocs) cudaFree(p);
   c.allocs.clear();
   if (c.h_scal) cudaFreeHost(c.h_scal);
@@ -906,6 +915,59 @@ int snapshot_restore(Ctx& c, const Snapshot& sn) {
 }  // namespace
 
 extern "C" {
+
+int hf_subbox_async(hf_ctx* h, int64_t inst, const int64_t* lo, const int64_t* hi, int which,
+                    double* host, int64_t* ticket) {
+  if (!h || !lo || !hi || !host || !ticket || (which != 0 && which != 1))
+    return set_err(HF_EARG, "bad arguments");
+  Ctx& c = h->c;
+  if (inst < 0 || inst >= c.ninst) return set_err(HF_EARG, "instance out of range");
+  const InstDesc& d = c.h_inst[inst];
+  const int64_t dims[3] = {d.nx, d.ny, d.nz};
+  int64_t n = 1;
+  for (int k = 0; k < 3; ++k) {
+    if (lo[k] < 0 || hi[k] < lo[k] || hi[k] >= dims[k]) return set_err(HF_EARG, "box outside the grid");
+    n *= hi[k] - lo[k] + 1;
+  }
+  if (!c.state_set) return set_err(HF_ESTATE, "hf_set_state must be called first");
+  if (!c.copy_stream) CU(cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking));
+  Ctx::SubSlot& sl = c.sub[c.next_ticket % Ctx::kSubSlots];
+  if (!sl.gathered) {
+    CU(cudaEventCreateWithFlags(&sl.gathered, cudaEventDisableTiming));
+    CU(cudaEventCreateWithFlags(&sl.copied, cudaEventDisableTiming));
+  }
+  if (sl.cap < (size_t)n) {                    // grow the slot (after its previous copy)
+    if (sl.dev) {
+      CU(cudaEventSynchronize(sl.copied));
+      CU(cudaFree(sl.dev));
+      sl.dev = nullptr;
+    }
+    CU(cudaMalloc((void**)&sl.dev, sizeof(double) * (size_t)n));
+    sl.cap = (size_t)n;
+  } else if (sl.ticket >= 0) {
+    CU(cudaStreamWaitEvent(c.stream, sl.copied, 0));   // the slot's previous copy has finished
+  }
+  CU(launch_subbox_gather(c, inst, lo, hi, which, sl.dev));
+  CU(cudaEventRecord(sl.gathered, c.stream));
+  CU(cudaStreamWaitEvent(c.copy_stream, sl.gathered, 0));
+  CU(cudaMemcpyAsync(host, sl.dev, sizeof(double) * (size_t)n, cudaMemcpyDeviceToHost, c.copy_stream));
+  CU(cudaEventRecord(sl.copied, c.copy_stream));
+  sl.ticket = c.next_ticket;
+  *ticket = c.next_ticket++;
+  c.launches += 1;
+  return HF_OK;
+}
+
+int hf_subbox_wait(hf_ctx* h, int64_t ticket) {
+  if (!h || ticket < 0) return set_err(HF_EARG, "bad arguments");
+  Ctx& c = h->c;
+  if (ticket >= c.next_ticket) return set_err(HF_EARG, "unknown ticket");
+  // a slot's event covers its latest copy; copies on the copy stream complete in order, so a
+  // reused slot's event also covers every earlier ticket of that slot
+  Ctx::SubSlot& sl = c.sub[ticket % Ctx::kSubSlots];
+  if (sl.copied) CU(cudaEventSynchronize(sl.copied));
+  return HF_OK;
+}
 
 int hf_autotune(hf_ctx* h, int64_t itime0, int32_t steps, hf_tune_result* results, int32_t cap,
                 int32_t* n_results) {

@@ -48,6 +48,17 @@ struct Ctx {
   int graph_precision = -1;     // options the graph was captured with
   int graph_criterion = -1;
   int64_t launches = 0;          // kernels launched on the device since creation
+  // sub-box snapshots: staging slots copied to the host on a second stream
+  struct SubSlot {
+    double* dev = nullptr;
+    size_t cap = 0;                // doubles
+    cudaEvent_t gathered = nullptr, copied = nullptr;
+    int64_t ticket = -1;
+  };
+  static constexpr int kSubSlots = 4;
+  SubSlot sub[kSubSlots];
+  cudaStream_t copy_stream = nullptr;
+  int64_t next_ticket = 0;
 };
 
 }  // namespace hf

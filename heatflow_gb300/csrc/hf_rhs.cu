@@ -400,6 +400,30 @@ cudaError_t launch_task_heat(Ctx& c) {
   return cudaGetLastError();
 }
 
+// Pack the box lo..hi of one temperature field of instance `inst` (its current role, read on the
+// device, so this works inside a stream of captured steps) into dst, x fastest.
+__global__ void k_subbox_gather(DevArrays A, int inst, int which, int x0, int y0, int z0, int bx,
+                                int by, int bz, double* dst) {
+  const InstDesc& d = A.inst[inst];
+  const double* T = A.tbuf[A.scal[inst].role[which]] + d.off;
+  const int64_t n = (int64_t)bx * by * bz;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int ix = (int)(i % bx), iy = (int)((i / bx) % by), iz = (int)(i / ((int64_t)bx * by));
+    dst[i] = T[(int64_t)(z0 + iz) * d.nx * d.ny + (int64_t)(y0 + iy) * d.nx + (x0 + ix)];
+  }
+}
+
+cudaError_t launch_subbox_gather(Ctx& c, int64_t inst, const int64_t* lo, const int64_t* hi,
+                                 int which, double* dst) {
+  const int bx = (int)(hi[0] - lo[0] + 1), by = (int)(hi[1] - lo[1] + 1), bz = (int)(hi[2] - lo[2] + 1);
+  const int64_t n = (int64_t)bx * by * bz;
+  const unsigned nb = (unsigned)std::min<int64_t>((n + 255) / 256, 4096);
+  k_subbox_gather<<<nb, 256, 0, c.stream>>>(c.A, (int)inst, which, (int)lo[0], (int)lo[1], (int)lo[2],
+                                            bx, by, bz, dst);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_adj_rhs(Ctx& c, const double* g, const double* l1, const double* l2, double* out) {
   k_adj_rhs<<<(unsigned)((c.ncells + 255) / 256), 256, 0, c.stream>>>(c.A, g, l1, l2, out);
   return cudaGetLastError();

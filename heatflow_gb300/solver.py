@@ -112,6 +112,24 @@ class HeatFlow:
         n = min(rounds.value, cap, 64)
         return [(abi.PHASE_NAMES.get(ph[i], str(ph[i])), us[i]) for i in range(n)], rounds.value
 
+    def subbox_async(self, lo, hi, which: int = 1, out=None, instance: int = 0):
+        """Start copying the box lo..hi (0-based, inclusive, (x, y, z)) of T^(n-1) (which=1, the
+        field the reference logs) or T^n (which=0) into `out` (float64, x fastest; pinned for
+        overlap) behind the queued steps.  Returns (ticket, out); `subbox_wait(ticket)` waits."""
+        lo = (C.c_int64 * 3)(*[int(v) for v in lo])
+        hi = (C.c_int64 * 3)(*[int(v) for v in hi])
+        n = int(np.prod([hi[k] - lo[k] + 1 for k in range(3)]))
+        if out is None:
+            out = np.empty(n)
+        assert out.dtype == np.float64 and out.flags.c_contiguous and out.size == n
+        t = C.c_int64()
+        abi.check(self.lib.hf_subbox_async(self.h, int(instance), lo, hi, int(which), _d(out),
+                                           C.byref(t)), "hf_subbox_async")
+        return t.value, out
+
+    def subbox_wait(self, ticket: int):
+        abi.check(self.lib.hf_subbox_wait(self.h, int(ticket)), "hf_subbox_wait")
+
     def autotune(self, itime0: int = 1, steps: int = 3):
         """Choose the task depth (and, mixed, the inner tolerance) by timing `steps` steps of this
         problem per candidate; state and statistics are unchanged.  Returns the candidates."""

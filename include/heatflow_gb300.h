@@ -238,6 +238,20 @@ enum {
  * round's length in microseconds (device %globaltimer; round 0 counts from the kernel's start). */
 int hf_solve_profile(hf_ctx* ctx, int64_t cap, int64_t* rounds, int32_t* phases, double* round_us);
 
+/* ---- sub-box snapshots overlapped with stepping --------------------------------------------
+ * The reference logs a sub-box of the field after a step (data_write, mod_output.f90:57-66,
+ * :92-113: Temp_pp, i.e. T^(n-1) after the state rotation, for start_i..end_i on each axis).
+ * hf_subbox_async enqueues, on the context stream after the work already queued, a gather of the
+ * box lo..hi (0-based, inclusive; packed x fastest, then y, then z) of instance `inst`'s field
+ * `which` (0: T^n, 1: T^(n-1)) into a device staging slot, and a copy of that slot to `host` on a
+ * separate copy stream; it returns at once with a ticket, so the following steps run while the
+ * copy engine moves the data (with a pinned `host` buffer; a pageable one makes the calling thread
+ * wait for the copy).  Four staging slots rotate; reusing a slot waits on the device for its
+ * previous copy.  hf_subbox_wait blocks until the copy of `ticket` has landed in `host`. */
+int hf_subbox_async(hf_ctx* ctx, int64_t inst, const int64_t* lo, const int64_t* hi, int which,
+                    double* host, int64_t* ticket);
+int hf_subbox_wait(hf_ctx* ctx, int64_t ticket);
+
 /* ---- autotuner ------------------------------------------------------------------------------
  * No counterpart in the reference.  Chooses the stencil task shape (z-planes per 32 x 8 column
  * tile: 8, 16 or 32) and, on the mixed path, the inner FP32 tolerance (1e-4, 1e-5, 1e-6) for this
