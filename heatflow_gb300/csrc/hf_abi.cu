@@ -1192,6 +1192,31 @@ int hf_get_rhs(hf_ctx* h, int64_t itime, double* B, double* Q, double* Qd, doubl
   return HF_OK;
 }
 
+}  // extern "C"
+
+namespace {
+// The solve of hf_solve / hf_solve_device after the scalars were set up: one persistent launch
+// (use_graph = 1) or the host-polled kernels.
+int device_solve(Ctx& c) {
+  if (c.opts.use_graph == 1) {
+    if (solve_grid_blocks(c, c.opts.precision == HF_PREC_MIXED ? 1 : 0) < 1)
+      return set_err(HF_ECUDA, "no co-resident grid for the persistent solve kernel");
+    CU(launch_solve(c));
+    SolveCtl sc;
+    CU(cudaMemcpyAsync(&sc, c.d_sctl, sizeof(sc), cudaMemcpyDeviceToHost, c.stream));
+    CU(cudaStreamSynchronize(c.stream));
+    c.launches += 1;
+    if (sc.err) return set_err(HF_EDEVICE, "persistent solve: a grid barrier wait reached its time limit");
+    if (sc.guard_hit) return set_err(HF_EDEVICE, "persistent solve reached its round bound");
+    return HF_OK;
+  }
+  CU(launch_residual(c, 0));
+  return solve_loop(c);
+}
+}  // namespace
+
+extern "C" {
+
 int hf_solve(hf_ctx* h, const double* b, double* x, hf_stats* stats) {
   if (!h || !b || !x) return set_err(HF_EARG, "null argument");
   Ctx& c = h->c;
@@ -1217,9 +1242,9 @@ int hf_solve(hf_ctx* h, const double* b, double* x, hf_stats* stats) {
   double rms = std::sqrt(bb / (double)d.n) * d.mean_sinv * 1e-6;
   s.sigma = (c.opts.precision == HF_PREC_MIXED && rms > 0.0 && std::isfinite(rms))
                 ? std::exp2(std::rint(std::log2(rms))) : 1.0;
+  s.phase = PH_RES_INIT;
   if ((rc = push_scal(c))) return rc;
-  CU(launch_residual(c, 0));
-  if ((rc = solve_loop(c))) return rc;
+  if ((rc = device_solve(c))) return rc;
   if ((rc = sync_scal(c))) return rc;
   CU(cudaMemcpyAsync(x, c.A.tbuf[c.h_scal[0].role[2]] + d.off, 8 * d.n, cudaMemcpyDeviceToHost, c.stream));
   CU(cudaStreamSynchronize(c.stream));
@@ -1274,12 +1299,12 @@ int hf_solve_device(hf_ctx* h, const double* b, double* x, hf_stats* stats) {
   s.x0flag = 0;
   s.tiny_pending = 0;
   s.status = 0;
+  s.phase = PH_RES_INIT;
   if ((rc = push_scal(c))) return rc;
   CU(cudaMemcpyAsync(c.A.b + d.off, b, 8 * d.n, cudaMemcpyDeviceToDevice, c.stream));
   CU(cudaMemcpyAsync(c.A.tbuf[s.role[2]] + d.off, x, 8 * d.n, cudaMemcpyDeviceToDevice, c.stream));
   CU(launch_sumsq(c, c.A.b + d.off, d.n));
-  CU(launch_residual(c, 0));
-  if ((rc = solve_loop(c))) return rc;
+  if ((rc = device_solve(c))) return rc;
   if ((rc = sync_scal(c))) return rc;
   CU(cudaMemcpyAsync(x, c.A.tbuf[c.h_scal[0].role[2]] + d.off, 8 * d.n, cudaMemcpyDeviceToDevice, c.stream));
   CU(cudaStreamSynchronize(c.stream));

@@ -65,3 +65,19 @@ def test_mixed_gradient_close_to_fp64(setup):
     _, glk_m, ga_m = _adjoint_grad(mixed, obs, lk0, a0)
     assert np.linalg.norm(glk_m - glk) <= 1e-6 * np.linalg.norm(glk)
     assert np.linalg.norm(ga_m - ga) <= 1e-6 * np.linalg.norm(ga)
+
+
+def test_persistent_solves_give_the_same_gradient(setup):
+    """The forward steps and the adjoint solves through the persistent solve kernel
+    (use_graph=1) give the host-polled path's gradient bit for bit."""
+    from heatflow_gb300.adjoint import AdjointModel
+    model, obs, lk0, a0 = setup
+    kw = dict(precision="mixed", criterion="true", tol=1e-12)
+    grads = []
+    for g in (0, 1):
+        m = AdjointModel(model.template, model.probes.cpu().numpy(), model.sources_np,
+                         model.nsteps, ckpt_every=25, use_graph=g, **kw)
+        grads.append(_adjoint_grad(m, obs, lk0, a0))
+    (J0, l0, s0), (J1, l1, s1) = grads
+    assert J0 == J1
+    assert np.array_equal(l0, l1) and np.array_equal(s0, s1)
