@@ -89,8 +89,12 @@ class AdjointModel:
         self._set(hf, tp, tpp)
         ckpts = {0: (tp.clone(), tpp.clone())}
         series = torch.empty(self.nsteps, self.probes.numel(), dtype=torch.float64, device="cuda")
+        self.forward_stats = {"iterations": 0, "inner_iterations": 0, "refinements": 0,
+                              "unconverged": 0}
         for k in range(1, self.nsteps + 1):
-            hf.simulate(k)
+            st = hf.simulate(k)
+            for key in self.forward_stats:
+                self.forward_stats[key] += st[key]
             self._get(hf, tp, tpp)
             series[k - 1] = tp[self.probes]
             if k % self.ckpt_every == 0 and k < self.nsteps:
@@ -169,7 +173,7 @@ def smooth_log_kappa(shape, length: float = 8.0, std: float = 0.5, mean: float =
     ky = np.fft.fftfreq(ny)[None, :, None]
     kx = np.fft.rfftfreq(nx)[None, None, :]
     f *= np.exp(-2.0 * (np.pi * length) ** 2 * (kx ** 2 + ky ** 2 + kz ** 2))
-    s = np.fft.irfftn(f, s=(nz, ny, nx))
+    s = np.fft.irfftn(f, s=(nz, ny, nx), axes=(0, 1, 2))
     s = (s - s.mean()) / (s.std() + 1e-300) * std + mean
     return s.reshape(-1)
 
@@ -194,3 +198,60 @@ def inverse_problem(n: int = 64, nsteps: int = 300, nprobes: int = 64, nsources:
                        time_step=dt, icattaneo=1, qdens_mode=abi.HF_QDENS_CELL_VOLUME,
                        kappa_bound=(50.0,) * 6, t_bath_face=(300.0,) * 6, t_bath=300.0)
     return template, probes, sources, hidden, amps
+
+
+def _main(argv=None):
+    """Time one loss + gradient evaluation of the inverse problem (forward steps with
+    checkpoints, backward adjoint solves), FP64 and mixed, and print one JSON line per path."""
+    import argparse
+    import json
+    import time
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--n", type=int, default=64)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--probes", type=int, default=64)
+    ap.add_argument("--sources", type=int, default=8)
+    ap.add_argument("--ckpt", type=int, default=25)
+    ap.add_argument("--use-graph", type=int, default=1)
+    a = ap.parse_args(argv)
+    # untimed warm-up on a small copy: the first use of each torch operation on the device may
+    # compile its kernel (PTX JIT), which is not part of the workload
+    wt, wp, ws, wh, wa = inverse_problem(8, 4, 4, 2)
+    for prec in ("fp64", "mixed"):
+        wm = AdjointModel(wt, wp, ws, 4, 2, precision=prec, criterion="true", tol=1e-10,
+                          use_graph=a.use_graph)
+        wobs, _, whf = wm.forward(wh, wa)
+        whf.close()
+        lw = torch.tensor(wh, dtype=torch.float64, device="cuda", requires_grad=True)
+        aw = torch.tensor(wa, dtype=torch.float64, device="cuda", requires_grad=True)
+        ProbeMisfit.apply(lw, aw, wm, wobs).backward()
+        float(lw.grad.norm())
+    template, probes, sources, hidden, amps = inverse_problem(a.n, a.steps, a.probes, a.sources)
+    obs_model = AdjointModel(template, probes, sources, a.steps, a.ckpt, precision="fp64",
+                             criterion="true", tol=1e-12, use_graph=a.use_graph)
+    obs, _, hf = obs_model.forward(hidden, amps)
+    hf.close()
+    lk0 = smooth_log_kappa((a.n, a.n, a.n), seed=1)
+    for prec, tol in (("fp64", 1e-12), ("mixed", 1e-10)):
+        model = AdjointModel(template, probes, sources, a.steps, a.ckpt, precision=prec,
+                             criterion="true", tol=tol, use_graph=a.use_graph)
+        lk = torch.tensor(lk0, dtype=torch.float64, device="cuda", requires_grad=True)
+        am = torch.tensor(amps * 0.7, dtype=torch.float64, device="cuda", requires_grad=True)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        J = ProbeMisfit.apply(lk, am, model, obs)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        J.backward()
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        print(json.dumps({"workload": f"adjoint inverse problem {a.n}^3, {a.steps} Cattaneo steps, "
+                                      f"{a.probes} probes, {a.sources} sources, checkpoints every {a.ckpt}",
+                          "precision": prec, "loss": float(J.detach()),
+                          "forward_s": t1 - t0, "backward_s": t2 - t1,
+                          "forward_solver": model.forward_stats,
+                          "gradient_norm": float(lk.grad.norm())}), flush=True)
+
+
+if __name__ == "__main__":
+    _main()
