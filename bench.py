@@ -334,7 +334,7 @@ def main():
     tuned = {}
     if not args.no_autotune:        # task depth and inner tolerance, timed on this problem
         t0 = time.perf_counter()
-        cand = hf.autotune(itime0=W + 1, steps=3)
+        cand = hf.autotune(itime0=W + 1, steps=6)
         best = next(r for r in cand if r["chosen"])
         tuned["mixed"] = {"task_depth": best["task_depth"], "inner_tol": best["inner_tol"],
                           "candidates": len(cand), "seconds": time.perf_counter() - t0}
@@ -408,7 +408,7 @@ def main():
         if W:
             h2.run(1, W)
         if not args.no_autotune:
-            cand = h2.autotune(itime0=W + 1, steps=3)
+            cand = h2.autotune(itime0=W + 1, steps=6)
             best = next(r for r in cand if r["chosen"])
             tuned["fp64"] = {"task_depth": best["task_depth"], "candidates": len(cand)}
         barrier()

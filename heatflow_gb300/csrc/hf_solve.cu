@@ -1425,6 +1425,10 @@ int solve_grid_blocks(Ctx& c, int fp32) {
   int64_t g = (int64_t)per_sm * nsm;
   if (g > c.ntasks) g = c.ntasks;
   if (g < 1) return -1;
+  // every round lasts as long as the busiest block: with r = ceil(tasks / grid) tasks on some
+  // block, a grid of ceil(tasks / r) blocks has the same r and no partly idle blocks
+  const int64_t r = (c.ntasks + g - 1) / g;
+  g = (c.ntasks + r - 1) / r;
   cached = (int)g;
   return cached;
 }
