@@ -282,31 +282,6 @@ __device__ __forceinline__ void tile_store(double* dst, const double (&v)[NRV]) 
   }
 }
 
-// FP32 partials: block sum in FP32, one conversion to FP64 per tile.
-template <int NRV>
-__device__ __forceinline__ void tile_store_f(const DevArrays& A, int64_t tile, const float (&v)[NRV]) {
-  __shared__ float red[NRV][kBlock / 32];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  __syncthreads();   // the previous tile of this block has finished reading red
-#pragma unroll
-  for (int k = 0; k < NRV; ++k) {
-    float t = v[k];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-    if (lane == 0) red[k][warp] = t;
-  }
-  __syncthreads();
-  if (warp == 0) {
-#pragma unroll
-    for (int k = 0; k < NRV; ++k) {
-      float t = lane < kBlock / 32 ? red[k][lane] : 0.f;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-      if (lane == 0) A.partials[tile * kNR + k] = (double)t;
-    }
-  }
-}
-
 // The columns of a task that this thread owns.
 struct TCell {
   int inst;
@@ -331,21 +306,6 @@ __device__ __forceinline__ TCell task_cell(const DevArrays& A, int64_t task) {
   c.y = t.z + (int)(threadIdx.x >> 5);
   c.z0 = t.w;
   c.z1 = min(t.w + d.zc, d.nz);
-  return c;
-}
-
-// Coordinates of local cell l in an instance.
-struct Coord {
-  int32_t x, y, z;
-};
-__device__ __forceinline__ Coord coord_of(const InstDesc& d, int32_t l) {
-  Coord c;
-  uint32_t ul = (uint32_t)l;
-  uint32_t row = ul / (uint32_t)d.nx;
-  c.x = (int32_t)(ul - row * (uint32_t)d.nx);
-  uint32_t pl = row / (uint32_t)d.ny;
-  c.y = (int32_t)(row - pl * (uint32_t)d.ny);
-  c.z = (int32_t)pl;
   return c;
 }
 

@@ -84,50 +84,10 @@ __global__ void k_step_end(DevArrays A) {
 }
 
 // ---- neighbour access for the columns of a task ------------------------------------------------
-// x neighbours come from the lanes of the same warp (shuffles; across chunk boundaries from the
-// first/last lane of the next/previous chunk); lanes at a task edge, periodic wraps and the y
-// neighbours are loaded; the z neighbours roll through registers as the block marches along z.
-// Inactive lanes hold zeros, so every lane can take part in the shuffles.
+// x neighbours come from the lanes of the same warp (shuffles); lanes at a task edge, periodic
+// wraps and the y neighbours are loaded; the z neighbours roll through registers as the block
+// marches along z.  Inactive lanes hold zeros, so every lane can take part in the shuffles.
 constexpr unsigned kFull = 0xffffffffu;
-
-// West/east values and west face of chunk j at local cell l.
-template <typename T, typename C, class V>
-__device__ __forceinline__ void x_nbrs(const TCell& c, int j, const T (&vc)[kXC],
-                                       const C (&cxc)[kXC], int l, V v, const C* __restrict__ cx,
-                                       T& vw, C& cxw, T& ve) {
-  const T up = __shfl_up_sync(kFull, vc[j], 1);
-  const C cup = __shfl_up_sync(kFull, cxc[j], 1);
-  const T dn = __shfl_down_sync(kFull, vc[j], 1);
-  const T prev_last = __shfl_sync(kFull, vc[j > 0 ? j - 1 : 0], 31);
-  const C cprev_last = __shfl_sync(kFull, cxc[j > 0 ? j - 1 : 0], 31);
-  const T next_first = __shfl_sync(kFull, vc[j + 1 < kXC ? j + 1 : j], 0);
-  vw = T(0); cxw = C(0); ve = T(0);
-  if (!c.act(j)) return;
-  const int x = c.x(j), nx = c.nx;
-  if (c.lane > 0) { vw = up; cxw = cup; }
-  else if (j > 0) { vw = prev_last; cxw = cprev_last; }
-  else if (x > 0) { vw = v(l - 1); cxw = cx[l - 1]; }
-  else if (c.px && nx > 1) { vw = v(l + nx - 1); cxw = cx[l + nx - 1]; }
-  if (x + 1 < nx) {
-    if (c.lane < 31) ve = dn;
-    else if (j + 1 < kXC) ve = next_first;
-    else ve = v(l + 1);
-  } else if (c.px && nx > 1) {
-    ve = v(l - (nx - 1));
-  }
-}
-
-// The y faces of cell l (chunk j active): fold(coef, value).
-template <typename T, typename C, class V, class F>
-__device__ __forceinline__ void y_faces(const TCell& c, int l, C cyc, V v, const C* __restrict__ cy,
-                                        F fold) {
-  if (c.ny < 2) return;
-  const int nx = c.nx;
-  if (c.y + 1 < c.ny) fold(cyc, v(l + nx));
-  else if (c.py) fold(cyc, v(l - (c.ny - 1) * nx));
-  if (c.y > 0) fold(cy[l - nx], v(l - nx));
-  else if (c.py) fold(cy[l + (c.ny - 1) * nx], v(l + (c.ny - 1) * nx));
-}
 
 // Value and z-face of plane z0-1 of chunk j (zeros at a non-periodic bottom face).
 template <typename T, typename C, class V>
