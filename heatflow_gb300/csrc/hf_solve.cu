@@ -1354,8 +1354,12 @@ __global__ void __launch_bounds__(kBlock, 3)
       if (blockIdx.x == 0 && threadIdx.x == 0) ctl->guard_hit = 1;
       return;
     }
+    // odd rounds walk the tasks backwards, so a round starts on the data the previous round wrote
+    // last, which is still in L2 (the partial sums have fixed slots: the order changes no bits)
     int cur = -1;
-    for (unsigned t = blockIdx.x; t < nt; t += G) {
+    const unsigned cnt = blockIdx.x < nt ? (nt - 1 - blockIdx.x) / G + 1 : 0u;
+    for (unsigned k = 0; k < cnt; ++k) {
+      const unsigned t = blockIdx.x + G * ((r & 1) ? cnt - 1 - k : k);
       const int inst = A.tasks[t].x;
       if (inst != cur) {                     // this instance's scalars, through L2
         __syncthreads();
