@@ -108,6 +108,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--workload", choices=["layered", "batched", "inclusions"], default="layered",
+                    help="layered: the headline 256^3 slab; batched: 256 uneven grids (edges "
+                         "16..96, 200-step sweep); inclusions: 512^3 with polymer spheres")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default task depth and inner tolerance")
     ap.add_argument("--host-loop", action="store_true",
@@ -292,11 +295,54 @@ def timed_run(hf, torch, stream, itime0, steps):
     return e0.elapsed_time(e1), st
 
 
+def other_workload(args):
+    """Time-steps/s of the batched sweep or the 512^3 inclusion grid, mixed and FP64 (one JSON
+    line; the headline contract line is the layered slab's)."""
+    import torch
+    from heatflow_gb300.build import build_library
+    from heatflow_gb300.problem import batched_sweep, inclusions
+    from heatflow_gb300.solver import HeatFlow
+    build_library()
+    if args.workload == "batched":
+        probs = batched_sweep(256, seed=0)
+        name = "batched sweep: 256 grids, edges U{16..96}, lognormal kappa, 1-4 sources, Cattaneo"
+    else:
+        probs = [inclusions(512)]
+        name = "512^3 inclusion grid (5 % polymer spheres), periodic x/y, Cattaneo"
+    cells = sum(p.ncells for p in probs)
+    stream = torch.cuda.Stream()
+    W, K = max(args.warmup, 0), max(args.steps, 1)
+    out = {"workload": name, "grids": len(probs), "cells": cells, "steps": K, "warmup": W,
+           "data": "synthetic", "unit": "time-steps/s (every grid advances one step)"}
+    for prec, tol in (("mixed", args.tol), ("fp64", args.tol)):
+        hf = HeatFlow(probs, precision=prec, criterion="true", tol=tol, use_graph=1)
+        hf.set_stream(stream.cuda_stream)
+        hf.initial_evolve()
+        if W:
+            hf.run(1, W)
+        tuned = None
+        if not args.no_autotune:
+            best = next(r for r in hf.autotune(itime0=W + 1, steps=4) if r["chosen"])
+            tuned = {"task_depth": best["task_depth"], "inner_tol": best["inner_tol"]}
+        ms, st = timed_run(hf, torch, stream, W + 1, K)
+        out[prec] = {"steps_per_s": K / (ms / 1000.0), "ms_per_step": ms / K,
+                     "cell_steps_per_s": cells * K / (ms / 1000.0),
+                     "iterations_per_step": (st["iterations"] + st["inner_iterations"]) / K,
+                     "unconverged": st["unconverged"], "last_true_relres": st["last_true_relres"],
+                     "kernel_launches_per_step": st["kernel_launches"] / K, "autotuned": tuned}
+        hf.close()
+    out["mixed_over_fp64"] = out["mixed"]["steps_per_s"] / out["fp64"]["steps_per_s"]
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     rank, world, local = dist_info()
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.workload != "layered":
+        return other_workload(args)
 
     import torch
     from heatflow_gb300 import abi
