@@ -1067,6 +1067,37 @@ int time_solve(Ctx& c, int reps, double* ms) {
 
 extern "C" {
 
+int hf_check_barrier_timeout(hf_ctx* h, int32_t wait_ms, int32_t* status, double* seconds) {
+  if (!h || !status || wait_ms < 1 || wait_ms > 10000) return set_err(HF_EARG, "bad arguments");
+  Ctx& c = h->c;
+  if (!c.state_set) return set_err(HF_ESTATE, "hf_set_state must be called first");
+  if (solve_grid_blocks(c, c.opts.precision == HF_PREC_MIXED ? 1 : 0) < 2)
+    return set_err(HF_EARG, "the check needs a grid of at least two blocks");
+  int rc = sync_scal(c);
+  if (rc) return rc;
+  std::vector<InstScal> saved(c.h_scal, c.h_scal + c.ninst);
+  CU(launch_step_begin(c, saved[0].itime + 1, 0));
+  CU(launch_rhs(c));
+  CU(launch_finalize(c, FIN_RHS, nullptr, 0, 0));
+  cudaEvent_t e0, e1;
+  CU(cudaEventCreate(&e0));
+  CU(cudaEventCreate(&e1));
+  CU(cudaEventRecord(e0, c.stream));
+  CU(launch_solve(c, (unsigned long long)wait_ms * 1000000ull, 0));
+  CU(cudaEventRecord(e1, c.stream));
+  CU(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  SolveCtl sc;
+  CU(cudaMemcpy(&sc, c.d_sctl, sizeof(sc), cudaMemcpyDeviceToHost));
+  *status = sc.err ? HF_EDEVICE : (sc.guard_hit ? HF_EDEVICE : HF_OK);
+  if (seconds) *seconds = ms * 1e-3;
+  std::memcpy(c.h_scal, saved.data(), sizeof(InstScal) * c.ninst);
+  return push_scal(c);
+}
+
 int hf_solve_profile(hf_ctx* h, int64_t cap, int64_t* rounds, int32_t* phases, double* round_us) {
   if (!h || !rounds || cap < 0 || (cap > 0 && (!phases || !round_us)))
     return set_err(HF_EARG, "bad arguments");

@@ -331,7 +331,7 @@ cudaError_t launch_inner_iteration(Ctx& c, int fp32, CtrlState* ctrl = nullptr,
                                    cudaGraphConditionalHandle hw = 0, int graph = 0);
 cudaError_t launch_step_end(Ctx& c);
 // Persistent solve: one cooperative launch runs the whole refinement loop of a step.
-cudaError_t launch_solve(Ctx& c);
+cudaError_t launch_solve(Ctx& c, unsigned long long wait_ns = 4000000000ull, int leaver = -1);
 int solve_grid_blocks(Ctx& c, int fp32);
 cudaError_t launch_apply(Ctx& c, const double* x, double* y);
 cudaError_t launch_single(Ctx& c, int which);

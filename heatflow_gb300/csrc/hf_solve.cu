@@ -1170,11 +1170,11 @@ __global__ void k_ctrl_select(DevArrays A, CtrlState* ctrl, cudaGraphConditional
 // L2 at the start of each round.  Tasks are assigned statically (task t to block t mod grid).
 // The kernel returns when the last epilogue reports that no instance has work left.
 //
-// Termination: every barrier wait is bounded in time (kBarrierWaitNs) and in polls; a block that
+// Termination: every barrier wait is bounded in time (wait_ns, 4 s by default) and in polls; a block that
 // gives up records SolveCtl::err and returns, and the blocks still waiting see the flag and return
 // too.  The number of rounds is bounded by `limit`.  Co-residency of all blocks, which the barrier
 // needs, is guaranteed by the cooperative launch (the grid never exceeds the occupancy bound).
-constexpr unsigned long long kBarrierWaitNs = 4000000000ull;
+constexpr unsigned long long kBarrierWaitNs = 4000000000ull;   // default barrier time limit
 
 __device__ __forceinline__ unsigned long long gtimer() {
   unsigned long long t;
@@ -1270,7 +1270,8 @@ __device__ int all_epilogues(const DevArrays& A, double* red) {
 // the wait gave up; `any` = some instance has work in the next round.
 template <typename T>
 __device__ bool grid_barrier_epilogue(const DevArrays& A, SolveCtl* ctl, unsigned nblocks,
-                                      int64_t round, double* red, unsigned& any) {
+                                      int64_t round, double* red, unsigned long long wait_ns,
+                                      unsigned& any) {
   __shared__ unsigned s_gen, s_any;
   __shared__ int s_last, s_ok;
   __syncthreads();
@@ -1302,7 +1303,7 @@ __device__ bool grid_barrier_epilogue(const DevArrays& A, SolveCtl* ctl, unsigne
     unsigned polls = 0;
     while (ld_acquire_u32(&ctl->gen) == g) {
       if (*(volatile int*)&ctl->err) { ok = 0; break; }
-      if ((++polls & 255u) == 0u && (gtimer() - t0 > kBarrierWaitNs || polls > (1u << 27))) {
+      if ((++polls & 255u) == 0u && (gtimer() - t0 > wait_ns || polls > (1u << 27))) {
         atomicExch(&ctl->err, 1);
         ok = 0;
         break;
@@ -1343,7 +1344,7 @@ __device__ __forceinline__ void round_task(const DevArrays& A, double* part, int
 // Blocks per SM: 3 (85 registers: the FP64 stencil and the FP32 vector pass need about that).
 template <typename T>
 __global__ void __launch_bounds__(kBlock, 3)
-    k_solve(DevArrays A, SolveCtl* ctl, int64_t limit) {
+    k_solve(DevArrays A, SolveCtl* ctl, int64_t limit, unsigned long long wait_ns, int leaver) {
   __shared__ InstScal sh;
   __shared__ double red[32 * 2];
   const unsigned G = gridDim.x;
@@ -1372,7 +1373,10 @@ __global__ void __launch_bounds__(kBlock, 3)
       if (sh.phase != PH_IDLE) round_task<T>(A, A.partials, t, sh);
     }
     unsigned any = 0;
-    if (!grid_barrier_epilogue<T>(A, ctl, G, r, red, any)) return;
+    // failure-path check only (leaver >= 0): that block leaves without arriving, so the others'
+    // waits run out and record SolveCtl::err
+    if ((int)blockIdx.x == leaver) return;
+    if (!grid_barrier_epilogue<T>(A, ctl, G, r, red, wait_ns, any)) return;
     if (!any) return;
   }
 }
@@ -1398,7 +1402,7 @@ int solve_grid_blocks(Ctx& c, int fp32) {
 }
 
 // Zero the control block, then launch the persistent solve cooperatively on the context stream.
-cudaError_t launch_solve(Ctx& c) {
+cudaError_t launch_solve(Ctx& c, unsigned long long wait_ns, int leaver) {
   const bool fp32 = c.opts.precision == HF_PREC_MIXED;
   const int g = solve_grid_blocks(c, fp32 ? 1 : 0);
   if (g < 1) return cudaErrorInvalidConfiguration;
@@ -1416,8 +1420,8 @@ cudaError_t launch_solve(Ctx& c) {
   at[0].val.cooperative = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  if (fp32) return cudaLaunchKernelEx(&cfg, k_solve<float>, c.A, c.d_sctl, limit);
-  return cudaLaunchKernelEx(&cfg, k_solve<double>, c.A, c.d_sctl, limit);
+  if (fp32) return cudaLaunchKernelEx(&cfg, k_solve<float>, c.A, c.d_sctl, limit, wait_ns, leaver);
+  return cudaLaunchKernelEx(&cfg, k_solve<double>, c.A, c.d_sctl, limit, wait_ns, leaver);
 }
 
 // ---- launchers ---------------------------------------------------------------------------------

@@ -252,6 +252,14 @@ int hf_subbox_async(hf_ctx* ctx, int64_t inst, const int64_t* lo, const int64_t*
                     double* host, int64_t* ticket);
 int hf_subbox_wait(hf_ctx* ctx, int64_t ticket);
 
+/* ---- failure-path check ------------------------------------------------------------------------
+ * No counterpart in the reference.  Runs the next step's persistent solve once with one block
+ * that leaves without arriving at the first grid barrier and a barrier time limit of wait_ms:
+ * the other blocks give up after wait_ms, record the failure and return, and *status receives the
+ * code the step loop would report (HF_EDEVICE).  The temperature state and the scalars are
+ * restored, so the context stays usable.  For tests of the bounded-wait path (no GPU fault). */
+int hf_check_barrier_timeout(hf_ctx* ctx, int32_t wait_ms, int32_t* status, double* seconds);
+
 /* ---- autotuner ------------------------------------------------------------------------------
  * No counterpart in the reference.  Chooses the stencil task shape (z-planes per 32 x 8 column
  * tile: 8, 16 or 32) and, on the mixed path, the inner FP32 tolerance (1e-4, 1e-5, 1e-6) for this
