@@ -104,6 +104,10 @@ void drop_graph(Ctx& c) {
   if (c.graph) cudaGraphDestroy(c.graph);
   c.graph_exec = nullptr;
   c.graph = nullptr;
+  if (c.loop_exec) cudaGraphExecDestroy(c.loop_exec);
+  if (c.loop_graph) cudaGraphDestroy(c.loop_graph);
+  c.loop_exec = nullptr;
+  c.loop_graph = nullptr;
 }
 
 void free_all(Ctx& c) {
@@ -356,6 +360,69 @@ int build_graph_persistent(Ctx& c) {
     return set_err(HF_ECUDA, "graph capture: " + err);
   }
   c.graph = g;
+  return HF_OK;
+}
+
+// The whole time loop as one graph: a WHILE conditional node whose body is one step (step begin,
+// RHS and its finalize, the persistent solve, step end).  k_graph_step_end sets the condition
+// from the device step counter (CtrlState::itime < itime_end, and no failed solve), so a single
+// launch runs any number of steps and always ends.  Built once per options; not every runtime
+// accepts a cooperative kernel in a conditional body, and then hf_run launches the per-step graph
+// back to back instead.
+int build_loop_graph(Ctx& c) {
+  if (c.loop_exec) return HF_OK;
+  if (c.loop_unsupported) return HF_EARG;
+  if (!c.d_ctrl) {
+    int r = dalloc(c, &c.d_ctrl, 1);
+    if (r) return r;
+    CU(cudaMemset(c.d_ctrl, 0, sizeof(CtrlState)));
+  }
+  if (solve_grid_blocks(c, c.opts.precision == HF_PREC_MIXED ? 1 : 0) < 1)
+    return set_err(HF_ECUDA, "no co-resident grid for the persistent solve kernel");
+  cudaStream_t cs = nullptr;
+  CU(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  cudaStream_t saved = c.stream;
+  cudaGraph_t g = nullptr;
+  std::string err;
+  auto chk = [&](cudaError_t e, const char* what) {
+    if (e != cudaSuccess && err.empty()) err = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaSuccess;
+  };
+  do {
+    if (!chk(cudaGraphCreate(&g, 0), "cudaGraphCreate")) break;
+    cudaGraphConditionalHandle hl;
+    if (!chk(cudaGraphConditionalHandleCreate(&hl, g, 1, cudaGraphCondAssignDefault), "handle")) break;
+    cudaGraphNodeParams wp = {};
+    wp.type = cudaGraphNodeTypeConditional;
+    wp.conditional.handle = hl;
+    wp.conditional.type = cudaGraphCondTypeWhile;
+    wp.conditional.size = 1;
+    cudaGraphNode_t wnode = nullptr;
+    if (!chk(cudaGraphAddNode(&wnode, g, nullptr, nullptr, 0, &wp), "while node")) break;
+    cudaGraph_t body = wp.conditional.phGraph_out[0];
+    if (!chk(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed),
+             "capture body")) break;
+    c.stream = cs;
+    chk(launch_graph_step_begin(c, c.d_ctrl, 5), "step begin");
+    chk(launch_rhs(c), "rhs");
+    chk(launch_finalize(c, FIN_RHS, nullptr, 0, 0), "rhs finalize");
+    chk(launch_solve(c), "persistent solve");
+    chk(launch_graph_step_end(c, c.d_ctrl, c.d_sctl, hl, 1), "step end");
+    cudaGraph_t tmp = nullptr;
+    chk(cudaStreamEndCapture(cs, &tmp), "end capture");
+    if (err.empty()) chk(cudaGraphInstantiate(&c.loop_exec, g, 0), "instantiate");
+  } while (0);
+  c.stream = saved;
+  cudaStreamDestroy(cs);
+  if (!err.empty()) {
+    if (c.loop_exec) cudaGraphExecDestroy(c.loop_exec);
+    c.loop_exec = nullptr;
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    c.loop_unsupported = true;
+    return set_err(HF_ECUDA, "whole-loop graph: " + err);
+  }
+  c.loop_graph = g;
   return HF_OK;
 }
 
@@ -851,13 +918,19 @@ int run_steps(Ctx& c, int64_t itime0, int64_t nsteps, hf_stats* stats) {
   int64_t done = 0;
   if (c.opts.use_graph && nsteps > 0) {
     if ((rc = build_graph(c))) return rc;
+    const bool loop = c.opts.use_graph == 1 && build_loop_graph(c) == HF_OK;
     const bool fp32 = c.opts.precision == HF_PREC_MIXED;
     const int64_t per = fp32 ? c.opts.inner_itmax : c.opts.itmax;
     CtrlState cs{};
     cs.itime = itime0;
+    cs.itime_end = itime0 + nsteps;
     cs.limit = 2 * (int64_t)(c.opts.max_refine + 3) * (per + 3);
     CU(cudaMemcpyAsync(c.d_ctrl, &cs, sizeof(cs), cudaMemcpyHostToDevice, c.stream));
-    for (int64_t k = 0; k < nsteps; ++k) CU(cudaGraphLaunch(c.graph_exec, c.stream));
+    if (loop) {
+      CU(cudaGraphLaunch(c.loop_exec, c.stream));                    // the whole time loop
+    } else {
+      for (int64_t k = 0; k < nsteps; ++k) CU(cudaGraphLaunch(c.graph_exec, c.stream));
+    }
     CU(cudaMemcpyAsync(&cs, c.d_ctrl, sizeof(cs), cudaMemcpyDeviceToHost, c.stream));
     CU(cudaStreamSynchronize(c.stream));
     if (cs.guard_hit & 2)

@@ -45,6 +45,10 @@ struct Ctx {
   SolveCtl* d_sctl = nullptr;    // control block of the persistent solve kernel
   int solve_blocks[2] = {0, 0};  // co-resident grid of the persistent solve (FP64, FP32)
   int graph_mode = 0;            // use_graph value the graph was captured for
+  // use_graph = 1: the whole time loop as one graph (WHILE node around one step)
+  cudaGraphExec_t loop_exec = nullptr;
+  cudaGraph_t loop_graph = nullptr;
+  bool loop_unsupported = false;  // capture or instantiation refused: per-step graphs instead
   int graph_precision = -1;     // options the graph was captured with
   int graph_criterion = -1;
   int64_t launches = 0;          // kernels launched on the device since creation

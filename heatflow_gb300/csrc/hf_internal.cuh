@@ -105,6 +105,7 @@ struct CtrlState {
   int32_t guard_hit;  // the bound was reached (reported as HF_EDEVICE)
   uint32_t fin_count; // finalize blocks arrived (last one sets the loop condition)
   int64_t launches;   // kernels the captured steps launched
+  int64_t itime_end;  // one past the last step of a whole-loop graph launch
 };
 
 // Phases of an instance inside the persistent solve kernel (one per grid-wide round).
@@ -336,7 +337,8 @@ int solve_grid_blocks(Ctx& c, int fp32);
 cudaError_t launch_apply(Ctx& c, const double* x, double* y);
 cudaError_t launch_single(Ctx& c, int which);
 cudaError_t launch_graph_step_begin(Ctx& c, CtrlState* ctrl, int launches_per_step);
-cudaError_t launch_graph_step_end(Ctx& c, CtrlState* ctrl, const SolveCtl* sctl);
+cudaError_t launch_graph_step_end(Ctx& c, CtrlState* ctrl, const SolveCtl* sctl,
+                                  cudaGraphConditionalHandle hloop = 0, int loop = 0);
 cudaError_t launch_ctrl_select(Ctx& c, CtrlState* ctrl, cudaGraphConditionalHandle hs,
                                cudaGraphConditionalHandle hw);
 // Finalize kernels: sum the tile partials of each instance and run the scalar epilogue of the

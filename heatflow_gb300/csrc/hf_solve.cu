@@ -1127,12 +1127,16 @@ __global__ void k_graph_step_begin(DevArrays A, CtrlState* ctrl, int launches_pe
 
 // One block: every instance rotates, then the step counter advances.  A persistent solve that
 // gave up (barrier time limit or round bound) is recorded in ctrl->guard_hit, which stays set.
-__global__ void k_graph_step_end(DevArrays A, CtrlState* ctrl, const SolveCtl* sctl) {
+// In a whole-loop graph (loop != 0) it also sets the WHILE condition: another step follows while
+// the step counter is below itime_end and no solve has failed, so the loop always ends.
+__global__ void k_graph_step_end(DevArrays A, CtrlState* ctrl, const SolveCtl* sctl,
+                                 cudaGraphConditionalHandle hloop, int loop) {
   for (int64_t i = threadIdx.x; i < A.ninst; i += blockDim.x) end_step(A.scal[i]);
   __syncthreads();
   if (threadIdx.x == 0) {
     ctrl->itime += 1;
     if (sctl && (sctl->err || sctl->guard_hit)) ctrl->guard_hit |= sctl->err ? 2 : 1;
+    if (loop) cudaGraphSetConditional(hloop, (ctrl->itime < ctrl->itime_end && !ctrl->guard_hit) ? 1u : 0u);
   }
 }
 
@@ -1477,8 +1481,9 @@ cudaError_t launch_graph_step_begin(Ctx& c, CtrlState* ctrl, int launches_per_st
                                                                                launches_per_step);
   return cudaGetLastError();
 }
-cudaError_t launch_graph_step_end(Ctx& c, CtrlState* ctrl, const SolveCtl* sctl) {
-  k_graph_step_end<<<1, 256, 0, c.stream>>>(c.A, ctrl, sctl);
+cudaError_t launch_graph_step_end(Ctx& c, CtrlState* ctrl, const SolveCtl* sctl,
+                                  cudaGraphConditionalHandle hloop, int loop) {
+  k_graph_step_end<<<1, 256, 0, c.stream>>>(c.A, ctrl, sctl, hloop, loop);
   return cudaGetLastError();
 }
 cudaError_t launch_ctrl_select(Ctx& c, CtrlState* ctrl, cudaGraphConditionalHandle hs,
