@@ -113,6 +113,9 @@ def parse():
                          "16..96, 200-step sweep); inclusions: 512^3 with polymer spheres")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the default task depth and inner tolerance")
+    ap.add_argument("--per-step-graph", action="store_true",
+                    help="one graph launch per step instead of one for the whole loop (profilers "
+                         "see the kernels)")
     ap.add_argument("--host-loop", action="store_true",
                     help="drive the solve loop from the host instead of the captured graph")
     ap.add_argument("--cpu-seconds", type=float, default=90.0,
@@ -278,7 +281,9 @@ def workload_config(args, prob):
               f"(L2 129 MB), no flush needed",
         "parallelism": f"replicas x{args.gpus}",
         "step_loop": "host-polled kernels" if args.host_loop else
-                     "CUDA graph per step: RHS + one persistent cooperative solve kernel",
+                     ("one CUDA graph launch per step" if args.per_step_graph else
+                      "the whole loop as one CUDA graph (WHILE node)") +
+                     ": RHS + one persistent cooperative solve kernel per step",
     }
 
 
@@ -367,7 +372,7 @@ def main():
 
     prob = layered_slab(args.n, icattaneo=0 if args.fourier else 1)
     N = prob.ncells
-    graph = 0 if args.host_loop else 1
+    graph = 0 if args.host_loop else (3 if args.per_step_graph else 1)
     stream = torch.cuda.Stream()
     W, K = max(args.warmup, 0), max(args.steps, 1)
 
@@ -427,8 +432,9 @@ def main():
                 "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_kind": f"of {peak_kind}",
                 "traffic": ratio * solve_bpc * N if ratio else None,
-                "traffic_source": "ncu DRAM read+write of an 11-round k_solve launch at 256^3 per "
-                                  "algorithmic byte, times this launch's algorithmic bytes",
+                "traffic_source": "ncu DRAM read+write per algorithmic byte of the k_solve launches "
+                                  "this bench times (256^3, profiles/solve_kernel_layered_slab_"
+                                  "256cube_dram.md), times this launch's algorithmic bytes",
                 "algorithmic_bytes_per_launch": solve_bpc * N, "ms_per_launch": solve_ms,
                 "rounds_per_launch": nrounds, "share_of_step": solve_ms / (ms / K),
                 "phases": phases,

@@ -150,7 +150,7 @@ int validate_opts(const hf_solver_opts& o) {
     return set_err(HF_EARG, "the reference's recursive criterion is defined for the FP64 path");
   if (!(o.tol >= 0.0) || o.itmax < 1 || o.inner_itmax < 1 || o.max_refine < 1 || o.check_every < 1)
     return set_err(HF_EARG, "tol >= 0, itmax, inner_itmax, max_refine, check_every >= 1");
-  if (o.use_graph < 0 || o.use_graph > 2) return set_err(HF_EARG, "use_graph must be 0, 1 or 2");
+  if (o.use_graph < 0 || o.use_graph > 3) return set_err(HF_EARG, "use_graph must be 0, 1, 2 or 3");
   if (o.task_depth != 0 && (o.task_depth < kMinTaskDepth || o.task_depth > 1024))
     return set_err(HF_EARG, "task_depth must be 0 (default) or 4..1024");
   return HF_OK;
@@ -918,7 +918,7 @@ int run_steps(Ctx& c, int64_t itime0, int64_t nsteps, hf_stats* stats) {
   int64_t done = 0;
   if (c.opts.use_graph && nsteps > 0) {
     if ((rc = build_graph(c))) return rc;
-    const bool loop = c.opts.use_graph == 1 && build_loop_graph(c) == HF_OK;
+    const bool loop = c.opts.use_graph == 1 && build_loop_graph(c) == HF_OK;   // 3: per-step graphs
     const bool fp32 = c.opts.precision == HF_PREC_MIXED;
     const int64_t per = fp32 ? c.opts.inner_itmax : c.opts.itmax;
     CtrlState cs{};
@@ -1302,7 +1302,7 @@ namespace {
 // The solve of hf_solve / hf_solve_device after the scalars were set up: one persistent launch
 // (use_graph = 1) or the host-polled kernels.
 int device_solve(Ctx& c) {
-  if (c.opts.use_graph == 1) {
+  if (c.opts.use_graph == 1 || c.opts.use_graph == 3) {
     if (solve_grid_blocks(c, c.opts.precision == HF_PREC_MIXED ? 1 : 0) < 1)
       return set_err(HF_ECUDA, "no co-resident grid for the persistent solve kernel");
     CU(launch_solve(c));

@@ -96,10 +96,12 @@ typedef struct hf_solver_opts {
   int32_t inner_itmax;  /* mixed: max FP32 CG iterations per inner solve */
   int32_t max_refine;   /* mixed: max FP64 refinement sweeps per step */
   int32_t check_every;  /* iterations launched between host convergence polls */
-  int32_t use_graph;    /* hf_run's step: 0 = kernels launched and polled by the host;
-                           1 = a CUDA graph per step whose solve is one persistent cooperative
-                           kernel (grid-wide rounds, no host round trip);
-                           2 = a CUDA graph per step with conditional WHILE/SWITCH nodes */
+  int32_t use_graph;    /* hf_run's step loop: 0 = kernels launched and polled by the host;
+                           1 = the whole loop as one CUDA graph (a WHILE node around a step whose
+                           solve is one persistent cooperative kernel: no host round trip);
+                           2 = a CUDA graph per step with conditional WHILE/SWITCH nodes;
+                           3 = as 1, but one graph launch per step (kernels visible to profilers,
+                           which do not see kernels inside conditional nodes) */
   int32_t task_depth;   /* z-planes per task of the step kernels (0: 16; otherwise 4..1024) */
 } hf_solver_opts;
 
