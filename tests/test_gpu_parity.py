@@ -327,3 +327,44 @@ def test_autotune_leaves_state_and_picks_a_candidate(cuda_lib, precision):
         T2 = h2.get_state()[0]
     assert np.array_equal(T, T2)
     assert st["inner_iterations"] == st2["inner_iterations"]
+
+
+def _vector_cases():
+    """Grids whose rows hold a multiple of 4 cells, so every step pass takes its 16-byte vector
+    form (RHS, direction update, SpMV, CG update, x update)."""
+    c = {}
+    c["heaters_em_4"] = _heater_problem(0.3)
+    c["heaters_4"] = _heater_problem(0.0)
+    c["periodic_xyz_8"] = _rng_problem(8, 4, 6, periodic=(1, 1, 1))
+    c["periodic_x_40"] = _rng_problem(40, 3, 4, periodic=(1, 0, 0))
+    c["neumann_12"] = _rng_problem(12, 5, 4, cg_face=(1, 0, 0, 1, 0, 1), t_bath_cg=2.0)
+    c["steady_8"] = _rng_problem(8, 3, 3, isteady=1,
+                                 iheater=np.r_[np.zeros(37), 1, np.zeros(34)].astype(np.int64),
+                                 power_in=1e-6)
+    c["fourier_16"] = _rng_problem(16, 8, 5, icattaneo=0)
+    c["wide_36"] = _rng_problem(36, 9, 17)
+    return c
+
+
+VECTOR_CASES = _vector_cases()
+
+
+@pytest.mark.parametrize("g", [0, 1])
+@pytest.mark.parametrize("name", sorted(VECTOR_CASES))
+def test_vector_paths_match_oracle(cuda_lib, name, g):
+    """Three FP64 steps (true residual <= 1e-14) on the vector paths against the oracle's
+    reference-rule BiCG: the fields agree to 1e-11 relative L2."""
+    prob = VECTOR_CASES[name]
+    assert prob.nx % 4 == 0
+    o = Oracle(prob)
+    o.set_state(*prob.initial_state())
+    rc, _ = o.run(3, itime0=1, mode=0, tol=1e-32, itmax=50000)
+    assert rc == 0
+    Tref, Tpref = o.get_state()
+    with HeatFlow(prob, precision="fp64", criterion="true", tol=1e-14, use_graph=g) as hf:
+        hf.initial_evolve()
+        st = hf.run(1, 3)
+        T, Tp = hf.get_state()
+    err = np.linalg.norm(T - Tref) / np.linalg.norm(Tref)
+    assert err <= 1e-11, (name, err, st)
+    assert np.linalg.norm(Tp - Tpref) / np.linalg.norm(Tpref) <= 1e-11
