@@ -119,6 +119,8 @@ _SIGNATURES = {
     "hf_subbox_async": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                   C.c_int, _dp, C.POINTER(C.c_int64)]),
     "hf_subbox_wait": (C.c_int, [C.c_void_p, C.c_int64]),
+    "hf_set_property_tables": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), _dp,
+                                         C.POINTER(C.c_int32)]),
     "hf_check_barrier_timeout": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), _dp]),
     "hf_autotune": (C.c_int, [C.c_void_p, C.c_int64, C.c_int32, C.POINTER(HfTuneResult), C.c_int32,
                               C.POINTER(C.c_int32)]),

@@ -224,6 +224,10 @@ int run_one_step(Ctx& c, int64_t itime) {
   if (rc) return rc;
   CU(launch_step_end(c));
   c.launches += 1;
+  if (c.tempdep) {
+    CU(launch_tempdep(c));
+    c.launches += 4;
+  }
   return HF_OK;
 }
 
@@ -253,7 +257,7 @@ int build_graph_cond(Ctx& c) {
     if (!chk(cudaGraphConditionalHandleCreate(&hw, g, 0, cudaGraphCondAssignDefault), "handle(while)")) break;
     if (!chk(cudaStreamBeginCaptureToGraph(cs, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed), "capture")) break;
     c.stream = cs;
-    chk(launch_graph_step_begin(c, c.d_ctrl, 6), "step begin");
+    chk(launch_graph_step_begin(c, c.d_ctrl, c.tempdep ? 10 : 6), "step begin");
     chk(launch_rhs(c), "rhs");
     chk(launch_finalize(c, FIN_RHS, c.d_ctrl, hw, 1), "rhs finalize");
     chk(launch_residual(c, 0, c.d_ctrl, hw, 1), "residual init");
@@ -303,6 +307,7 @@ int build_graph_cond(Ctx& c) {
     }
     c.stream = cs;
     chk(launch_graph_step_end(c, c.d_ctrl, nullptr), "step end");
+    if (c.tempdep) chk(launch_tempdep(c), "properties");
     cudaGraph_t outg = nullptr;
     chk(cudaStreamEndCapture(cs, &outg), "end capture");
     if (err.empty()) chk(cudaGraphInstantiate(&c.graph_exec, g, 0), "instantiate");
@@ -342,11 +347,12 @@ int build_graph_persistent(Ctx& c) {
   };
   if (chk(cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed), "capture")) {
     c.stream = cs;
-    chk(launch_graph_step_begin(c, c.d_ctrl, 5), "step begin");
+    chk(launch_graph_step_begin(c, c.d_ctrl, c.tempdep ? 9 : 5), "step begin");
     chk(launch_rhs(c), "rhs");
     chk(launch_finalize(c, FIN_RHS, nullptr, 0, 0), "rhs finalize");
     chk(launch_solve(c), "persistent solve");
     chk(launch_graph_step_end(c, c.d_ctrl, c.d_sctl), "step end");
+    if (c.tempdep) chk(launch_tempdep(c), "properties");
     chk(cudaStreamEndCapture(cs, &g), "end capture");
     if (err.empty()) chk(cudaGraphInstantiate(&c.graph_exec, g, 0), "instantiate");
   }
@@ -403,11 +409,12 @@ int build_loop_graph(Ctx& c) {
     if (!chk(cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed),
              "capture body")) break;
     c.stream = cs;
-    chk(launch_graph_step_begin(c, c.d_ctrl, 5), "step begin");
+    chk(launch_graph_step_begin(c, c.d_ctrl, c.tempdep ? 9 : 5), "step begin");
     chk(launch_rhs(c), "rhs");
     chk(launch_finalize(c, FIN_RHS, nullptr, 0, 0), "rhs finalize");
     chk(launch_solve(c), "persistent solve");
     chk(launch_graph_step_end(c, c.d_ctrl, c.d_sctl, hl, 1), "step end");
+    if (c.tempdep) chk(launch_tempdep(c), "properties");
     cudaGraph_t tmp = nullptr;
     chk(cudaStreamEndCapture(cs, &tmp), "end capture");
     if (err.empty()) chk(cudaGraphInstantiate(&c.loop_exec, g, 0), "instantiate");
@@ -988,6 +995,65 @@ int snapshot_restore(Ctx& c, const Snapshot& sn) {
 }  // namespace
 
 extern "C" {
+
+int hf_set_property_tables(hf_ctx* h, int32_t ntables, const int32_t* offsets, const double* rows,
+                           const int32_t* cell_table) {
+  if (!h || ntables < 0 || (ntables > 0 && (!offsets || !rows || !cell_table)))
+    return set_err(HF_EARG, "bad arguments");
+  Ctx& c = h->c;
+  if (ntables == 0) {                         // back to fixed properties
+    c.tempdep = false;
+    drop_graph(c);
+    return HF_OK;
+  }
+  if (offsets[0] != 0) return set_err(HF_EARG, "offsets[0] must be 0");
+  for (int32_t k = 0; k < ntables; ++k) {
+    const int32_t m = offsets[k + 1] - offsets[k];
+    if (m < 1) return set_err(HF_EARG, "every table needs at least one row");
+    for (int32_t r = offsets[k]; r < offsets[k + 1]; ++r) {
+      if (!(rows[4 * r + 1] > 0.0) || !(rows[4 * r + 2] > 0.0) || !(rows[4 * r + 3] > 0.0))
+        return set_err(HF_EARG, "table kappa, rho and c must be positive");
+      if (r > offsets[k] && !(rows[4 * r] > rows[4 * (r - 1)]))
+        return set_err(HF_EARG, "table temperatures must increase");
+    }
+  }
+  int64_t total = 0;
+  for (int64_t i = 0; i < c.ninst; ++i) total += c.h_inst[i].n;
+  std::vector<int32_t> ct((size_t)c.ncells, -1);
+  {
+    int64_t pos = 0;
+    for (int64_t i = 0; i < c.ninst; ++i) {
+      const InstDesc& d = c.h_inst[i];
+      for (int64_t l = 0; l < d.n; ++l) {
+        const int32_t t = cell_table[pos + l];
+        if (t < -1 || t >= ntables) return set_err(HF_EARG, "cell table index out of range");
+        ct[(size_t)(d.off + l)] = t;
+      }
+      pos += d.n;
+    }
+  }
+  (void)total;
+  if (!c.d_cell_table) {
+    int r = dalloc(c, &c.d_cell_table, (size_t)c.ncells);
+    if (r) return r;
+  }
+  for (void* p : {(void*)c.d_toff, (void*)c.d_trows}) {
+    if (!p) continue;
+    cudaFree(p);
+    c.allocs.erase(std::remove(c.allocs.begin(), c.allocs.end(), p), c.allocs.end());
+  }
+  c.d_toff = nullptr;
+  c.d_trows = nullptr;
+  int r = dalloc(c, &c.d_toff, (size_t)ntables + 1);
+  if (!r) r = dalloc(c, &c.d_trows, 4 * (size_t)offsets[ntables]);
+  if (r) return r;
+  CU(cudaMemcpy(c.d_toff, offsets, sizeof(int32_t) * ((size_t)ntables + 1), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(c.d_trows, rows, sizeof(double) * 4 * (size_t)offsets[ntables], cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(c.d_cell_table, ct.data(), sizeof(int32_t) * ct.size(), cudaMemcpyHostToDevice));
+  c.tempdep = true;
+  drop_graph(c);                              // the captured steps gain the rebuild kernels
+  return HF_OK;
+}
 
 int hf_subbox_async(hf_ctx* h, int64_t inst, const int64_t* lo, const int64_t* hi, int which,
                     double* host, int64_t* ticket) {

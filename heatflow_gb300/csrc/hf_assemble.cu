@@ -328,6 +328,46 @@ __global__ void k_apply_exact(DevArrays A, const double* xin, double* yout) {
 // ---- launchers ------------------------------------------------------------------------------
 static inline unsigned nblk(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
 
+// ---- tabulated properties (extension of TempDepProp) ------------------------------------------
+// After a step, every cell with a table takes kappa, rho and c at its new temperature T^n: rows
+// (T ascending, kappa, rho, c) held constant below the first and above the last row, linear in
+// between, in the oracle's operation order (compiled without contraction, so the values match
+// bit for bit); then rho*c and tau'*rho*c follow, and the operator is rebuilt by k_assemble.
+__device__ __forceinline__ double table_value(const double* rows, int m, int col, double T) {
+  if (T <= rows[0]) return rows[col];
+  if (T >= rows[4 * (m - 1)]) return rows[4 * (m - 1) + col];
+  int k = 0;
+  while (k + 1 < m - 1 && !(T < rows[4 * (k + 1)])) ++k;
+  const double f = (T - rows[4 * k]) / (rows[4 * (k + 1)] - rows[4 * k]);
+  return rows[4 * k + col] + f * (rows[4 * (k + 1) + col] - rows[4 * k + col]);
+}
+
+__global__ void k_tempdep(DevArrays A, const int32_t* toff, const double* trows,
+                          const int32_t* cell_table, double* kappa) {
+  int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= A.ncells) return;
+  const int inst = A.tile_inst[g / kTile];
+  const InstDesc& d = A.inst[inst];
+  if (g - d.off >= d.n) return;
+  const int32_t t = cell_table[g];
+  if (t < 0) return;
+  const double* rows = trows + 4 * (int64_t)toff[t];
+  const int m = toff[t + 1] - toff[t];
+  const double T = A.tbuf[A.scal[inst].role[0]][g];
+  kappa[g] = table_value(rows, m, 1, T);
+  const double rc = table_value(rows, m, 2, T) * table_value(rows, m, 3, T);
+  A.rhoc[g] = rc;
+  A.ccat[g] = A.tau_s[g] * rc;
+}
+
+cudaError_t launch_tempdep(Ctx& c) {
+  k_tempdep<<<nblk(c.ncells, 256), 256, 0, c.stream>>>(c.A, c.d_toff, c.d_trows, c.d_cell_table,
+                                                       c.asm_.kappa);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return launch_assemble(c);
+}
+
 cudaError_t launch_props(Ctx& c, const double* rho, const double* hc, const double* tau,
                          const double* em) {
   k_props<<<nblk(c.ncells, 256), 256, 0, c.stream>>>(c.A, rho, hc, tau, em);

@@ -63,6 +63,11 @@ struct Ctx {
   SubSlot sub[kSubSlots];
   cudaStream_t copy_stream = nullptr;
   int64_t next_ticket = 0;
+  // tabulated properties re-evaluated after every step (hf_set_property_tables)
+  bool tempdep = false;
+  int32_t* d_toff = nullptr;
+  double* d_trows = nullptr;
+  int32_t* d_cell_table = nullptr;
 };
 
 }  // namespace hf

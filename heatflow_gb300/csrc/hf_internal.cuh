@@ -318,6 +318,8 @@ cudaError_t launch_coo(Ctx& c, int64_t instance, int64_t* d_counts, int64_t* d_i
 cudaError_t launch_step_begin(Ctx& c, int64_t itime, int first_of_run);
 cudaError_t launch_rhs(Ctx& c);
 cudaError_t launch_task_heat(Ctx& c);
+// Tabulated properties at the current T^n, then the operator rebuilt (4 kernels).
+cudaError_t launch_tempdep(Ctx& c);
 cudaError_t launch_subbox_gather(Ctx& c, int64_t inst, const int64_t* lo, const int64_t* hi,
                                  int which, double* dst);
 cudaError_t launch_rhs_parts(Ctx& c, double* B, double* Q, double* Qd, double* Sc);

@@ -112,6 +112,24 @@ class HeatFlow:
         n = min(rounds.value, cap, 64)
         return [(abi.PHASE_NAMES.get(ph[i], str(ph[i])), us[i]) for i in range(n)], rounds.value
 
+    def set_property_tables(self, tables, cell_table):
+        """Temperature-dependent properties: `tables` = list of (m, 4) arrays of rows
+        (T ascending, kappa, rho, c); `cell_table` = a table index or -1 per cell (all grids, cell
+        order).  After every step each such cell takes its properties at its new T^n and the
+        operator is rebuilt on the device.  An empty list returns to fixed properties."""
+        if not tables:
+            abi.check(self.lib.hf_set_property_tables(self.h, 0, None, None, None),
+                      "hf_set_property_tables")
+            return
+        offsets = np.cumsum([0] + [len(t) for t in tables]).astype(np.int32)
+        rows = np.ascontiguousarray(np.concatenate([np.asarray(t, np.float64) for t in tables]))
+        ct = np.ascontiguousarray(cell_table, np.int32)
+        assert ct.size == self.n
+        self._tables = (offsets, rows, ct)      # the library copies them; keep until the call ends
+        abi.check(self.lib.hf_set_property_tables(
+            self.h, len(tables), offsets.ctypes.data_as(C.POINTER(C.c_int32)), _d(rows),
+            ct.ctypes.data_as(C.POINTER(C.c_int32))), "hf_set_property_tables")
+
     def subbox_async(self, lo, hi, which: int = 1, out=None, instance: int = 0):
         """Start copying the box lo..hi (0-based, inclusive, (x, y, z)) of T^(n-1) (which=1, the
         field the reference logs) or T^n (which=0) into `out` (float64, x fastest; pinned for

@@ -240,6 +240,19 @@ enum {
  * round's length in microseconds (device %globaltimer; round 0 counts from the kernel's start). */
 int hf_solve_profile(hf_ctx* ctx, int64_t cap, int64_t* rounds, int32_t* phases, double* round_us);
 
+/* ---- temperature-dependent properties -------------------------------------------------------
+ * The reference's TempDepProp = 1 rebuilds H after every step from unchanged properties (its
+ * table lookup is commented out, mod_tempdep.f90:66-95; the rebuild is called at
+ * mod_evolve.f90:172-174).  This call makes the rebuild real: after every step, each cell with a
+ * table takes kappa, rho and c at its new temperature T^n -- rows (T ascending, kappa, rho, c),
+ * held constant below the first and above the last row, linear in between -- and the operator,
+ * the boundary vector and the solver scaling are rebuilt on the device inside the captured step.
+ * Tables k = 0..ntables-1 are rows[4*offsets[k] .. 4*offsets[k+1]); cell_table holds one table
+ * index (or -1: fixed properties) per cell of all instances in cell order.  ntables = 0 returns
+ * to fixed properties (the ones in effect stay). */
+int hf_set_property_tables(hf_ctx* ctx, int32_t ntables, const int32_t* offsets, const double* rows,
+                           const int32_t* cell_table);
+
 /* ---- sub-box snapshots overlapped with stepping --------------------------------------------
  * The reference logs a sub-box of the field after a step (data_write, mod_output.f90:57-66,
  * :92-113: Temp_pp, i.e. T^(n-1) after the state rotation, for start_i..end_i on each axis).

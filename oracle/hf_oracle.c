@@ -45,6 +45,11 @@ typedef struct or_sys {
   int64_t *irow, *jcol;
   double* val;
   double *temp_p, *temp_pp;
+  /* tabulated properties (extension): tables of rows (T, kappa, rho, c), a table per cell or -1 */
+  int32_t ntables;
+  int32_t* toff;
+  double* trows;
+  int32_t* cell_table;
 } or_sys;
 
 /* altmod, mod_hmatrix.f90:330-338 */
@@ -216,6 +221,7 @@ void or_destroy(void* h) {
   free(s->kappa); free(s->rho); free(s->hc); free(s->tau_s); free(s->em); free(s->rhoc);
   free(s->power); free(s->iheater); free(s->irow); free(s->jcol); free(s->val);
   free(s->temp_p); free(s->temp_pp);
+  free(s->toff); free(s->trows); free(s->cell_table);
   free(s);
 }
 
@@ -569,6 +575,49 @@ int or_pcg(void* h, const double* b, double* x, double tol, int64_t itmax, int64
 /* simulate(itime), mod_evolve.f90:45-177.  mode 0: linbcg with (itol=1, tol, itmax) as the
  * reference calls it (tol=1e-32, itmax=50000 at :142-144); mode 1: or_pcg to a true relative
  * residual tol.  Returns 0 or a HF_ENAN_* code (the reference's `stop 1`). */
+/* Property of one table column at temperature T: rows (T ascending) held constant below the first
+ * and above the last row, linear in between: v_k + (T - T_k) / (T_k1 - T_k) * (v_k1 - v_k). */
+static double table_value(const double* rows, int32_t m, int col, double T) {
+  if (T <= rows[0]) return rows[col];
+  if (T >= rows[4 * (m - 1)]) return rows[4 * (m - 1) + col];
+  int32_t k = 0;
+  while (k + 1 < m - 1 && !(T < rows[4 * (k + 1)])) ++k;
+  const double f = (T - rows[4 * k]) / (rows[4 * (k + 1)] - rows[4 * k]);
+  return rows[4 * k + col] + f * (rows[4 * (k + 1) + col] - rows[4 * k + col]);
+}
+
+/* Tabulated kappa, rho, c (extension of TempDepProp, whose reference lookup is commented out,
+ * mod_tempdep.f90:66-95): after every step, cells with a table take their properties at their
+ * new temperature and H is rebuilt (ChangeProp -> sparse_Hmatrix, mod_evolve.f90:172-174). */
+int or_set_property_tables(void* h, int32_t ntables, const int32_t* offsets, const double* rows,
+                           const int32_t* cell_table) {
+  or_sys* s = (or_sys*)h;
+  free(s->toff); free(s->trows); free(s->cell_table);
+  s->ntables = ntables;
+  s->toff = (int32_t*)malloc(sizeof(int32_t) * (size_t)(ntables + 1));
+  memcpy(s->toff, offsets, sizeof(int32_t) * (size_t)(ntables + 1));
+  s->trows = (double*)malloc(sizeof(double) * 4 * (size_t)offsets[ntables]);
+  memcpy(s->trows, rows, sizeof(double) * 4 * (size_t)offsets[ntables]);
+  s->cell_table = (int32_t*)malloc(sizeof(int32_t) * (size_t)s->na);
+  memcpy(s->cell_table, cell_table, sizeof(int32_t) * (size_t)s->na);
+  return 0;
+}
+
+static void change_prop(or_sys* s) {
+  for (int64_t i = 0; i < s->na; ++i) {
+    const int32_t t = s->cell_table[i];
+    if (t < 0) continue;
+    const double* rows = s->trows + 4 * (size_t)s->toff[t];
+    const int32_t m = s->toff[t + 1] - s->toff[t];
+    const double T = s->temp_p[i];
+    s->kappa[i] = table_value(rows, m, 1, T);
+    s->rho[i] = table_value(rows, m, 2, T);
+    s->hc[i] = table_value(rows, m, 3, T);
+    s->rhoc[i] = s->rho[i] * s->hc[i];
+  }
+  sparse_hmatrix(s);
+}
+
 int or_simulate(void* h, int64_t itime, int mode, double tol, int64_t itmax, int64_t* iter,
                 double* err) {
   or_sys* s = (or_sys*)h;
@@ -585,6 +634,7 @@ int or_simulate(void* h, int64_t itime, int mode, double tol, int64_t itmax, int
   if (rc == 0) {
     memcpy(s->temp_pp, s->temp_p, bytes);  /* Temp_pp = Temp_p; Temp_p = x (:169-170) */
     memcpy(s->temp_p, x, bytes);
+    if (s->cell_table) change_prop(s);
   }
   free(B); free(Q); free(Qd); free(Sc); free(S); free(x);
   return rc;

@@ -55,6 +55,9 @@ def lib():
         L.or_true_relres.argtypes = [C.c_void_p, _dp, _dp]
         L.or_simulate.restype = C.c_int
         L.or_simulate.argtypes = [C.c_void_p, C.c_int64, C.c_int, C.c_double, C.c_int64, _ip, _dp]
+        L.or_set_property_tables.restype = C.c_int
+        L.or_set_property_tables.argtypes = [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), _dp,
+                                             C.POINTER(C.c_int32)]
         L.or_set_threads.restype = C.c_int
         L.or_set_threads.argtypes = [C.c_int]
         _lib = L
@@ -83,6 +86,14 @@ class Oracle:
             self.h = None
 
     # --- state
+    def set_property_tables(self, tables, cell_table):
+        """tables: list of (m, 4) arrays of rows (T, kappa, rho, c); cell_table: per cell."""
+        offsets = np.cumsum([0] + [len(t) for t in tables]).astype(np.int32)
+        rows = np.ascontiguousarray(np.concatenate([np.asarray(t, np.float64) for t in tables]))
+        ct = np.ascontiguousarray(cell_table, np.int32)
+        lib().or_set_property_tables(self.h, len(tables), offsets.ctypes.data_as(C.POINTER(C.c_int32)),
+                                     _d(rows), ct.ctypes.data_as(C.POINTER(C.c_int32)))
+
     def set_state(self, tp, tpp):
         tp = np.ascontiguousarray(tp, np.float64)
         tpp = np.ascontiguousarray(tpp, np.float64)

@@ -1,0 +1,98 @@
+"""Temperature-dependent properties (tabulated kappa, rho, c re-evaluated after every step, the
+operator rebuilt): the oracle's restatement and the GPU paths agree."""
+import numpy as np
+import pytest
+
+from heatflow_gb300.problem import Problem
+
+
+def table_a():
+    # a conductor whose kappa falls and whose heat capacity rises with temperature
+    T = np.array([250.0, 290.0, 300.0, 305.0, 320.0, 400.0])
+    return np.c_[T, 150.0 - 0.6 * (T - 250.0), 2300.0 - 0.1 * (T - 250.0), 700.0 + 0.8 * (T - 250.0)]
+
+
+def table_b():
+    return np.array([[290.0, 0.3, 1200.0, 1100.0], [330.0, 0.2, 1150.0, 1300.0]])
+
+
+def tempdep_problem():
+    nx, ny, nz = 12, 10, 8
+    N = nx * ny * nz
+    rng = np.random.default_rng(2)
+    ih = np.zeros(N, np.int64)
+    ih[rng.choice(N, 4, replace=False)] = 1
+    power = np.where(ih > 0, 3e-6, 0.0)
+    prob = Problem(nx=nx, ny=ny, nz=nz, lx=nx * 1e-9, ly=ny * 1e-9, lz=nz * 1e-9, kappa=149.0,
+                   rho=2329.0, heat_capacity=710.0, tau=1e-12, em=0.0, iheater=ih, power=power,
+                   time_step=1e-13, icattaneo=1, qdens_mode=1, kappa_bound=(149.0,) * 6,
+                   t_bath_face=(300.0,) * 6, t_bath=300.0)
+    iz = np.repeat(np.arange(nz), nx * ny)
+    cell_table = np.where(iz < 3, 1, 0).astype(np.int32)
+    cell_table[iz == nz - 1] = -1                           # a layer with fixed properties
+    return prob, [table_a(), table_b()], cell_table
+
+
+def test_oracle_tables_change_the_run():
+    from oracle.oracle import Oracle
+    prob, tables, ct = tempdep_problem()
+    out = []
+    for with_tables in (False, True):
+        o = Oracle(prob)
+        if with_tables:
+            o.set_property_tables(tables, ct)
+        o.set_state(*prob.initial_state())
+        rc, _ = o.run(5, itime0=1, mode=0, tol=1e-32, itmax=50000)
+        assert rc == 0
+        out.append(o.get_state()[0])
+    assert np.isfinite(out[1]).all()
+    assert np.linalg.norm(out[1] - out[0]) / np.linalg.norm(out[0] - 300.0) > 1e-3
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("use_graph", [0, 1, 2])
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_tables_match_oracle(cuda_lib, precision, use_graph):
+    """8 steps with the properties re-evaluated after each: the operator after the run equals the
+    oracle's bit for bit, and the fields agree to 1e-10 (FP64) / 1e-9 (mixed) relative L2."""
+    from oracle.oracle import Oracle
+    from heatflow_gb300.solver import HeatFlow, geometric_to_dense
+    prob, tables, ct = tempdep_problem()
+    o = Oracle(prob)
+    o.set_property_tables(tables, ct)
+    o.set_state(*prob.initial_state())
+    rc, _ = o.run(8, itime0=1, mode=0, tol=1e-32, itmax=50000)
+    assert rc == 0
+    Tref, _ = o.get_state()
+    tol = 1e-13 if precision == "fp64" else 1e-10
+    with HeatFlow(prob, precision=precision, criterion="true", tol=tol, use_graph=use_graph) as hf:
+        hf.set_property_tables(tables, ct)
+        hf.initial_evolve()
+        st = hf.run(1, 8)
+        T, _ = hf.get_state()
+        H = geometric_to_dense(prob, hf.operator())
+    err = np.linalg.norm(T - Tref) / np.linalg.norm(Tref)
+    assert err <= (1e-10 if precision == "fp64" else 1e-9), err
+    assert st["unconverged"] == 0
+    # the rebuilt operator is exactly the one of the properties at the GPU's final field
+    kappa, rho, hc = prob.kappa.copy(), prob.rho.copy(), prob.heat_capacity.copy()
+    for i in np.nonzero(ct >= 0)[0]:
+        rows = tables[ct[i]]
+        kappa[i], rho[i], hc[i] = (table_value(rows, c, T[i]) for c in (1, 2, 3))
+    import dataclasses
+    ref_prob = dataclasses.replace(prob, kappa=kappa, rho=rho, heat_capacity=hc, _keep=[])
+    assert np.array_equal(H, Oracle(ref_prob).dense())
+
+
+def table_value(rows, col, T):
+    """The tables' rule (held constant outside, linear inside), in the kernels' operation order."""
+    m = len(rows)
+    if T <= rows[0, 0]:
+        return rows[0, col]
+    if T >= rows[m - 1, 0]:
+        return rows[m - 1, col]
+    k = 0
+    while k + 1 < m - 1 and not (T < rows[k + 1, 0]):
+        k += 1
+    f = (T - rows[k, 0]) / (rows[k + 1, 0] - rows[k, 0])
+    return rows[k, col] + f * (rows[k + 1, col] - rows[k, col])
