@@ -209,6 +209,113 @@ __global__ void k_assemble(DevArrays A, const InstBC* bcs, const double* kappa) 
   if (bad) atomicOr(&A.scal[inst].devcheck, 1);
 }
 
+// ---- operator rebuild of a step (temperature-dependent properties) -----------------------------
+// The coefficients of k_assemble + k_sinv, bit for bit, with each conductivity evaluated once.
+// Interior face P|Q (Q the + neighbour): calculate_conductivity(P->Q) (kin = kappa_P) is both the
+// stored slot of P (hmatrixfunc(Q,P)) and the - face term of Q's diagonal; (Q->P) is P's + face
+// term.  The products (L+L)*kin*kout round differently in the two orders, so both are evaluated.
+// Pass 1 writes P->Q per axis into the a64 arrays (k_scale rewrites them afterwards); on the last
+// cell of a periodic axis it writes last->first, the - face term of the first cell.  Pass 2 forms
+// the + face terms, the diagonal in hmatrixfunc's summation order, the wrap slots (the + face term
+// of the last cell), the boundary vector and 1/sqrt|H_II|.  k_assemble instead evaluates
+// hmatrixfunc whole per stored slot (six conductivities each) and checks slot consistency, which
+// the one-time set-up affords and a rebuild on every step does not.
+__global__ void k_faces_step(DevArrays A, const InstBC* bcs, const double* kappa) {
+  int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= A.ncells) return;
+  const int inst = A.tile_inst[g / kTile];
+  const InstDesc& d = A.inst[inst];
+  HM h{d, bcs[inst], kappa + d.off, A.rhoc + d.off, A.tau_s + d.off};
+  const int64_t l = g - d.off;
+  if (l >= d.n) return;
+  const int64_t nx = d.nx, ny = d.ny, nz = d.nz;
+  const int64_t x = l % nx + 1, y = (l / nx) % ny + 1, z = l / (nx * ny) + 1;
+  A.a64x[g] = x < nx ? h.cond(x, y, z, x + 1, y, z) : (d.px ? h.cond(x, y, z, 1, y, z) : 0.0);
+  A.a64y[g] = y < ny ? h.cond(x, y, z, x, y + 1, z) : (d.py ? h.cond(x, y, z, x, 1, z) : 0.0);
+  A.a64z[g] = z < nz ? h.cond(x, y, z, x, y, z + 1) : (d.pz ? h.cond(x, y, z, x, y, 1) : 0.0);
+}
+
+__global__ void k_diag_step(DevArrays A, const InstBC* bcs, const double* kappa) {
+  int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= A.ncells) return;
+  const int inst = A.tile_inst[g / kTile];
+  const InstDesc& d = A.inst[inst];
+  const InstBC& bc = bcs[inst];
+  HM h{d, bc, kappa + d.off, A.rhoc + d.off, A.tau_s + d.off};
+  const int64_t l = g - d.off;
+  if (l >= d.n) { A.sinv[g] = 0.0; return; }
+  const int64_t nx = d.nx, ny = d.ny, nz = d.nz, nxy = nx * ny;
+  const int64_t x = l % nx + 1, y = (l / nx) % ny + 1, z = l / nxy + 1;
+  // hmatrixfunc(I,I): alpha, then the six face terms (mod_hmatrix.f90:62-248)
+  double alpha = 0.0;
+  if (d.isteady == 0) {
+    double tau = A.tau_s[g];
+    if (d.icattaneo == 0) tau = 0.0;
+    alpha = (tau * A.rhoc[g]) + (d.inv_dt * A.rhoc[g]);
+  }
+  int64_t xp = x + 1, xm = x - 1, yp = y + 1, ym = y - 1, zp = z + 1, zm = z - 1;
+  if (d.px) { if (xp > nx) xp = 1; if (xm < 1) xm = nx; }
+  if (d.py) { if (yp > ny) yp = 1; if (ym < 1) ym = ny; }
+  if (d.pz) { if (zp > nz) zp = 1; if (zm < 1) zm = nz; }
+  const double Af = x > 1 ? A.a64x[g - 1] : (d.px ? A.a64x[g + nx - 1] : h.cond(xm, y, z, x, y, z));
+  const double Bf = h.cond(xp, y, z, x, y, z);
+  const double Df = y > 1 ? A.a64y[g - nx] : (d.py ? A.a64y[g + (ny - 1) * nx] : h.cond(x, ym, z, x, y, z));
+  const double Ef = h.cond(x, yp, z, x, y, z);
+  const double Ff = z > 1 ? A.a64z[g - nxy] : (d.pz ? A.a64z[g + (nz - 1) * nxy] : h.cond(x, y, zm, x, y, z));
+  const double Gf = h.cond(x, y, zp, x, y, z);
+  const double dg = -(Af + Bf + Df + Ef + Ff + Gf) - alpha;
+  A.diag[g] = dg;
+  auto keep = [](double v) { return fabs(v) < kTiny ? 0.0 : v; };   // sparse_Hmatrix's drop rule
+  double cxv = 0.0, cyv = 0.0, czv = 0.0;
+  if (x < nx) cxv = keep(A.a64x[g]);
+  else if (d.px && nx > 1) cxv = keep(Bf);
+  if (ny > 1) {
+    if (y < ny) cyv = keep(A.a64y[g]);
+    else if (d.py) cyv = keep(Ef);
+  }
+  if (nz > 1) {
+    if (z < nz) czv = keep(A.a64z[g]);
+    else if (d.pz) czv = keep(Gf);
+  }
+  A.cx[g] = cxv;
+  A.cy[g] = cyv;
+  A.cz[g] = czv;
+  // boundary(B), mod_boundary.f90:72-150
+  double Bv = 0.0;
+  const double kap = kappa[g];
+  const int64_t c[3] = {x, y, z}, n[3] = {nx, ny, nz};
+  const int per[3] = {d.px, d.py, d.pz};
+  for (int a = 0; a < 3; ++a) {
+    if (per[a]) continue;
+    double L = d.len[a];
+    if (c[a] == 1) {
+      int f = 2 * a;
+      if (bc.cg[f]) {
+        Bv = bc.pd[f];
+      } else {
+        double kh = (2.0 * kap * bc.kb[f] / (kap + bc.kb[f])) / (L * L);
+        if (kap != bc.kb[f]) kh = kh * bc.br;
+        Bv = Bv + (kh) * bc.tb[f];
+      }
+    }
+    if (c[a] == n[a]) {
+      int f = 2 * a + 1;
+      if (bc.cg[f]) {
+        Bv = bc.pd[f];
+      } else {
+        double kh = (2.0 * kap * bc.kb[f] / (kap + bc.kb[f])) / (L * L);
+        if (kap != bc.kb[f]) kh = kh * bc.br;
+        Bv = Bv + (kh) * bc.tb[f];
+      }
+    }
+  }
+  A.bvec[g] = Bv;
+  if (isnan(Bv)) atomicOr(&A.scal[inst].status, 1 << (HF_ENAN_B - HF_ENAN_B));
+  if (dg >= 0.0) atomicOr(&A.scal[inst].devcheck, 2);
+  A.sinv[g] = 1.0 / sqrt(fabs(dg));
+  A.sinv32[g] = (float)A.sinv[g];
+}
+
 // ---- Jacobi scaling: sinv = 1/sqrt|H_II|, a = -c * sinv_I * sinv_E ----------------------------
 __global__ void k_sinv(DevArrays A) {
   int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -333,13 +440,27 @@ static inline unsigned nblk(int64_t n, int b) { return (unsigned)((n + b - 1) / 
 // (T ascending, kappa, rho, c) held constant below the first and above the last row, linear in
 // between, in the oracle's operation order (compiled without contraction, so the values match
 // bit for bit); then rho*c and tau'*rho*c follow, and the operator is rebuilt by k_assemble.
-__device__ __forceinline__ double table_value(const double* rows, int m, int col, double T) {
-  if (T <= rows[0]) return rows[col];
-  if (T >= rows[4 * (m - 1)]) return rows[4 * (m - 1) + col];
+// Interval of T in a table (rows of T, kappa, rho, c with ascending T) and its fraction; the same
+// search and fraction serve all three columns.  Outside the table: the end row, f = 0.
+struct TableAt {
+  const double* r0;
+  const double* r1;
+  double f;
+  bool inside;
+};
+
+__device__ __forceinline__ TableAt table_at(const double* rows, int m, double T) {
+  if (T <= rows[0]) return {rows, rows, 0.0, false};
+  if (T >= rows[4 * (m - 1)]) return {rows + 4 * (m - 1), rows + 4 * (m - 1), 0.0, false};
   int k = 0;
   while (k + 1 < m - 1 && !(T < rows[4 * (k + 1)])) ++k;
   const double f = (T - rows[4 * k]) / (rows[4 * (k + 1)] - rows[4 * k]);
-  return rows[4 * k + col] + f * (rows[4 * (k + 1) + col] - rows[4 * k + col]);
+  return {rows + 4 * k, rows + 4 * (k + 1), f, true};
+}
+
+__device__ __forceinline__ double table_col(const TableAt& t, int col) {
+  if (!t.inside) return t.r0[col];
+  return t.r0[col] + t.f * (t.r1[col] - t.r0[col]);
 }
 
 __global__ void k_tempdep(DevArrays A, const int32_t* toff, const double* trows,
@@ -354,8 +475,9 @@ __global__ void k_tempdep(DevArrays A, const int32_t* toff, const double* trows,
   const double* rows = trows + 4 * (int64_t)toff[t];
   const int m = toff[t + 1] - toff[t];
   const double T = A.tbuf[A.scal[inst].role[0]][g];
-  kappa[g] = table_value(rows, m, 1, T);
-  const double rc = table_value(rows, m, 2, T) * table_value(rows, m, 3, T);
+  const TableAt at = table_at(rows, m, T);
+  kappa[g] = table_col(at, 1);
+  const double rc = table_col(at, 2) * table_col(at, 3);
   A.rhoc[g] = rc;
   A.ccat[g] = A.tau_s[g] * rc;
 }
@@ -363,9 +485,10 @@ __global__ void k_tempdep(DevArrays A, const int32_t* toff, const double* trows,
 cudaError_t launch_tempdep(Ctx& c) {
   k_tempdep<<<nblk(c.ncells, 256), 256, 0, c.stream>>>(c.A, c.d_toff, c.d_trows, c.d_cell_table,
                                                        c.asm_.kappa);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  return launch_assemble(c);
+  k_faces_step<<<nblk(c.ncells, 256), 256, 0, c.stream>>>(c.A, c.d_bc, c.asm_.kappa);
+  k_diag_step<<<nblk(c.ncells, 256), 256, 0, c.stream>>>(c.A, c.d_bc, c.asm_.kappa);
+  k_scale<<<nblk(c.ncells, 256), 256, 0, c.stream>>>(c.A);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_props(Ctx& c, const double* rho, const double* hc, const double* tau,

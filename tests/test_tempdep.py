@@ -96,3 +96,63 @@ def table_value(rows, col, T):
         k += 1
     f = (T - rows[k, 0]) / (rows[k + 1, 0] - rows[k, 0])
     return rows[k, col] + f * (rows[k + 1, col] - rows[k, col])
+
+
+def periodic_problem(nx, ny, nz, periodic):
+    N = nx * ny * nz
+    rng = np.random.default_rng(nx * 100 + ny * 10 + nz)
+    ih = np.zeros(N, np.int64)
+    ih[rng.choice(N, max(1, N // 20), replace=False)] = 1
+    power = np.where(ih > 0, 3e-6, 0.0)
+    prob = Problem(nx=nx, ny=ny, nz=nz, lx=nx * 1e-9, ly=ny * 1e-9, lz=nz * 1e-9, kappa=149.0,
+                   rho=2329.0, heat_capacity=710.0, tau=1e-12, em=0.0, iheater=ih, power=power,
+                   time_step=1e-13, icattaneo=1, qdens_mode=1, kappa_bound=(149.0,) * 6,
+                   t_bath_face=(300.0,) * 6, t_bath=300.0, periodic=periodic)
+    cell_table = (rng.random(N) < 0.5).astype(np.int32)
+    cell_table[rng.random(N) < 0.1] = -1
+    return prob, [table_a(), table_b()], cell_table
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dims,periodic", [
+    ((12, 10, 8), (0, 0, 0)),
+    ((8, 6, 4), (1, 1, 1)),
+    ((2, 5, 3), (1, 0, 0)),      # nx = 2: both x faces of a cell join the same neighbour
+    ((6, 2, 4), (0, 1, 0)),      # ny = 2 periodic
+    ((4, 3, 2), (0, 0, 1)),      # nz = 2 periodic
+    ((5, 4, 1), (1, 1, 0)),      # one layer, odd nx (scalar passes)
+])
+def test_step_rebuild_equals_setup_assembly(cuda_lib, dims, periodic):
+    """The operator rebuilt inside the step (one conductivity evaluation per face orientation)
+    equals, bit for bit, the set-up assembly's (hmatrixfunc per stored slot) and the oracle's
+    dense H for the same properties, on periodic axes, two-cell axes and one-cell axes."""
+    from oracle.oracle import Oracle
+    from heatflow_gb300.solver import HeatFlow, geometric_to_dense
+    import dataclasses
+    prob, tables, ct = periodic_problem(*dims, periodic)
+    with HeatFlow(prob, precision="fp64", criterion="true", tol=1e-13, use_graph=1) as hf:
+        hf.set_property_tables(tables, ct)
+        hf.initial_evolve()
+        hf.run(1, 3)
+        T, _ = hf.get_state()
+        op = hf.operator()
+    kappa, rho, hc = prob.kappa.copy(), prob.rho.copy(), prob.heat_capacity.copy()
+    for i in np.nonzero(ct >= 0)[0]:
+        rows = tables[ct[i]]
+        kappa[i], rho[i], hc[i] = (table_value(rows, c, T[i]) for c in (1, 2, 3))
+    assert len(np.unique(kappa)) > 2                     # the properties really vary cell to cell
+    ref_prob = dataclasses.replace(prob, kappa=kappa, rho=rho, heat_capacity=hc, _keep=[])
+    with HeatFlow(ref_prob, precision="fp64", criterion="true", tol=1e-13, use_graph=0) as hf0:
+        op0 = hf0.operator()
+    for key in ("diag", "cx", "cy", "cz"):
+        assert np.array_equal(op[key], op0[key]), key
+    assert np.array_equal(geometric_to_dense(prob, op), Oracle(ref_prob).dense())
+
+
+def test_oracle_one_cell_periodic_axis_has_zero_diagonal():
+    """A periodic axis one cell long: hmatrixfunc's wrap rule for that axis (offset (n-1)*stride = 0)
+    overwrites the diagonal with the self-face term, 0, so the set-up's check that H_II < 0 rejects
+    such a grid; the oracle shows the zero diagonal the check is guarding against."""
+    from oracle.oracle import Oracle
+    prob, _, _ = periodic_problem(6, 1, 4, (0, 1, 0))
+    assert np.all(np.diag(Oracle(prob).dense()) == 0.0)
