@@ -41,10 +41,13 @@ UNIT = "time-steps/s"
 BYTES_PER_CELL = {
     # T^n, T^(n-1), rho*c, tau'*rho*c, B, heater power (8 B each) + heater case (1 B); writes S, x0
     "rhs": 6 * 8 + 1 + 2 * 8,
-    # mixed: x, diag, cx, cy, cz, S (8 B) + 1/sqrt|H_II| (4 B) read; g (4 B) written
-    "residual_mixed": 6 * 8 + 4 + 4,
-    # FP64: x, diag, cx, cy, cz, S, 1/sqrt|H_II| (8 B) read; g (8 B) written
-    "residual_fp64": 7 * 8 + 8,
+    # mixed: x, diag, cx, cy, cz, S (8 B) + 1/sqrt|H_II| (4 B) read; g (4 B) + H x (8 B) written
+    "residual_mixed": 6 * 8 + 4 + 4 + 8,
+    # mixed step start from the stored products: S, H T^n, H T^(n-1), H*1 (8 B) + 1/sqrt|H_II|
+    # (4 B) read; g (4 B) written
+    "residual_init_hx_mixed": 4 * 8 + 4 + 4,
+    # FP64: x, diag, cx, cy, cz, S, 1/sqrt|H_II| (8 B) read; g, H x (8 B) written
+    "residual_fp64": 7 * 8 + 8 + 8,
     # direction update: r, p_old read, p written; SpMV: p, ax, ay, az read, q written
     "cg_p_fp32": 3 * 4, "cg_spmv_fp32": 5 * 4, "cg_update_fp32": 6 * 4,
     # fused direction update + SpMV: r, p_old, ax, ay, az read, p, q written
@@ -56,19 +59,22 @@ BYTES_PER_CELL = {
     "cg_p_fp64": 3 * 8, "cg_spmv_fp64": 5 * 8, "cg_update_fp64": 6 * 8,
 }
 # FP64 floating-point operations per cell (an FMA counts 2) of the FP64-pipe kernels: the
-# residual does 7 FMA for S - Hx and 1 FMA for ||r||^2; the RHS 2 mul (rho c T/dt), 1 FMA + 1 mul
-# (S_cat), 1 add, 2 add + 1 sub (x0 and its test), 1 FMA (||S||^2).
-FP64_FLOPS_PER_CELL = {"residual_mixed": 16, "residual_fp64": 18, "rhs": 12}
+# residual does 7 FMA for S - Hx, 1 FMA for ||r||^2 and 1 sub for H x = S - r; the step-start
+# residual from the stored products 1 FMA + 1 add (S - 2 H T^n + H T^(n-1)), 1 FMA (TINY) and 1 FMA
+# (||r||^2); the RHS 2 mul (rho c T/dt), 1 FMA + 1 mul (S_cat), 1 add, 2 add + 1 sub (x0 and its
+# test), 1 FMA (||S||^2).
+FP64_FLOPS_PER_CELL = {"residual_mixed": 17, "residual_fp64": 19, "residual_init_hx_mixed": 7,
+                       "rhs": 12}
 
 # Algorithmic bytes per cell of each round of the persistent solve kernel (k_solve), by phase:
 # (bytes, bytes of the first inner iteration / of an update without a correction).  The first
 # residual also reads H*1 (the x0 + TINY rule applies on this workload: far-field cells do not
 # move, so x0 - T < TINY somewhere every step).
 PHASE_BYTES = {
-    "mixed": {"res_init": (64, 64), "res": (56, 56), "cg_p": (12, 8), "cg_q": (20, 20),
-              "cg_pq": (28, 24), "cg_b": (24, 20), "xupd": (24, 16)},
-    "fp64": {"res_init": (72, 72), "res": (64, 64), "cg_p": (24, 16), "cg_q": (40, 40),
-             "cg_b": (48, 40), "xupd": (32, 16)},
+    "mixed": {"res_init": (64, 64), "res_init_hx": (40, 40), "res": (64, 64), "cg_p": (12, 8),
+              "cg_q": (20, 20), "cg_pq": (28, 24), "cg_b": (24, 20), "xupd": (24, 16)},
+    "fp64": {"res_init": (72, 72), "res_init_hx": (48, 48), "res": (72, 72), "cg_p": (24, 16),
+             "cg_q": (40, 40), "cg_b": (48, 40), "xupd": (32, 16)},
 }
 
 
@@ -78,7 +84,7 @@ def solve_bytes_per_cell(rounds, precision):
     total, first_cg, first_b, have_y = 0, True, True, False
     for ph, _ in rounds:
         full, alt = table.get(ph, (0, 0))
-        if ph in ("res_init", "res"):
+        if ph in ("res_init", "res_init_hx", "res"):
             total += full
             first_cg = first_b = True
             have_y = False
@@ -419,7 +425,9 @@ def main():
         e["GB/s_upper"] = full * N / (e["us_per_round"] * 1e-6) / 1e9 if full else None
     kernels = {"cg_p_fp32": abi.HF_KERNEL_CG_P, "cg_spmv_fp32": abi.HF_KERNEL_CG_SPMV,
                "cg_pq_fp32": abi.HF_KERNEL_CG_PQ, "cg_update_fp32": abi.HF_KERNEL_CG_UPDATE,
-               "xupdate_mixed": abi.HF_KERNEL_XUPDATE, "residual_mixed": abi.HF_KERNEL_RESIDUAL}
+               "xupdate_mixed": abi.HF_KERNEL_XUPDATE,
+               "residual_init_hx_mixed": abi.HF_KERNEL_RESIDUAL_INIT,   # before the sweep below,
+               "residual_mixed": abi.HF_KERNEL_RESIDUAL}                # which rewrites H x
     kms = {name: hf.time_kernel(k, reps=10) for name, k in kernels.items()}
     kms["rhs"] = rhs_ms
     f64 = C.c_double()

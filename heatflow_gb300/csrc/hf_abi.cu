@@ -163,7 +163,12 @@ int sync_scal(Ctx& c) {
   return HF_OK;
 }
 
-int push_scal(Ctx& c) {
+// Scalars written from the host mean state or scratch changed outside the step sequence (a restored
+// snapshot, a timing run, a standalone solve, a new state): the stored products H T^n, H T^(n-1)
+// are then not trusted, unless the caller restored them too (keep_hx).
+int push_scal(Ctx& c, bool keep_hx = false) {
+  if (!keep_hx)
+    for (int64_t i = 0; i < c.ninst; ++i) c.h_scal[i].hx_ok = 0;
   CU(cudaMemcpyAsync(c.A.scal, c.h_scal, sizeof(InstScal) * c.ninst, cudaMemcpyHostToDevice,
                      c.stream));
   CU(cudaStreamSynchronize(c.stream));
@@ -675,6 +680,7 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
   if (c.any_em) ALLOC(A.emc, N);
   if (c.any_heater) ALLOC(A.icase, N);
   for (int k = 0; k < 4; ++k) ALLOC(A.tbuf[k], N);
+  ALLOC(A.hx[0], N); ALLOC(A.hx[1], N);
   ALLOC(A.b, N); ALLOC(A.y, N); ALLOC(A.r, N); ALLOC(A.p, N); ALLOC(A.q, N); ALLOC(A.p2, N);
   ALLOC(A.y32, N); ALLOC(A.r32, N); ALLOC(A.p32, N); ALLOC(A.q32, N); ALLOC(A.p232, N);
   double *d_rho, *d_hc, *d_tau, *d_em = nullptr;
@@ -693,7 +699,7 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
                   (void*)d_rho, (void*)d_hc, (void*)d_tau, (void*)A.rhoc, (void*)A.ccat,
                   (void*)A.bvec, (void*)A.tau_s, (void*)A.a64x, (void*)A.a64y, (void*)A.a64z,
                   (void*)A.b, (void*)A.y, (void*)A.r, (void*)A.p, (void*)A.q, (void*)A.rsum,
-                  (void*)A.p2})
+                  (void*)A.p2, (void*)A.hx[0], (void*)A.hx[1]})
     CK(cudaMemsetAsync(p, 0, N * sizeof(double), c.stream));
   for (void* p : {(void*)A.a32x, (void*)A.a32y, (void*)A.a32z, (void*)A.y32, (void*)A.r32,
                   (void*)A.p32, (void*)A.q32, (void*)A.sinv32, (void*)A.p232})
@@ -859,9 +865,8 @@ int hf_set_state(hf_ctx* h, const double* tp, const double* tpp) {
     CU(cudaMemcpyAsync(c.A.tbuf[s.role[1]] + d.off, tpp + pos, 8 * d.n, cudaMemcpyHostToDevice, c.stream));
     pos += d.n;
   }
-  CU(cudaStreamSynchronize(c.stream));
   c.state_set = true;
-  return HF_OK;
+  return push_scal(c);   // a new state: the stored products H T are stale
 }
 
 int hf_get_state(hf_ctx* h, double* tp, double* tpp) {
@@ -895,7 +900,9 @@ int hf_state_device(hf_ctx* h, double** tp, double** tpp) {
 int hf_state_device_ready(hf_ctx* h) {
   if (!h) return set_err(HF_EARG, "null context");
   h->c.state_set = true;
-  return HF_OK;
+  int rc = sync_scal(h->c);
+  if (rc) return rc;
+  return push_scal(h->c);   // the state was written in place: the stored products H T are stale
 }
 
 int hf_step(hf_ctx* h, int64_t itime, hf_stats* stats) {
@@ -963,20 +970,25 @@ int run_steps(Ctx& c, int64_t itime0, int64_t nsteps, hf_stats* stats) {
   return first_error(c);
 }
 
-// Saved temperature state and scalars of all instances (autotuner).
+// Saved temperature state, stored products H T and scalars of all instances (autotuner).
 struct Snapshot {
-  double* t = nullptr;                  // [T^n | T^(n-1)] of every instance, cells in order
+  double* t = nullptr;   // [T^n | T^(n-1) | H T^n | H T^(n-1)] of every instance, cells in order
   std::vector<InstScal> scal;
 };
+// Field k of instance i in the context: T^n, T^(n-1), H T^n, H T^(n-1).
+double* snapshot_field(Ctx& c, const InstScal& s, int k) {
+  if (k < 2) return c.A.tbuf[s.role[k]];
+  return c.A.hx[k == 2 ? s.hx_role : 1 - s.hx_role];
+}
 int snapshot_take(Ctx& c, Snapshot& sn) {
   int rc = sync_scal(c);
   if (rc) return rc;
   sn.scal.assign(c.h_scal, c.h_scal + c.ninst);
-  CU(cudaMalloc((void**)&sn.t, sizeof(double) * 2 * (size_t)c.ncells));
+  CU(cudaMalloc((void**)&sn.t, sizeof(double) * 4 * (size_t)c.ncells));
   for (int64_t i = 0; i < c.ninst; ++i) {
     const InstDesc& d = c.h_inst[i];
-    for (int k = 0; k < 2; ++k)
-      CU(cudaMemcpyAsync(sn.t + k * c.ncells + d.off, c.A.tbuf[sn.scal[i].role[k]] + d.off,
+    for (int k = 0; k < 4; ++k)
+      CU(cudaMemcpyAsync(sn.t + k * c.ncells + d.off, snapshot_field(c, sn.scal[i], k) + d.off,
                          8 * (size_t)d.n, cudaMemcpyDeviceToDevice, c.stream));
   }
   CU(cudaStreamSynchronize(c.stream));
@@ -985,12 +997,12 @@ int snapshot_take(Ctx& c, Snapshot& sn) {
 int snapshot_restore(Ctx& c, const Snapshot& sn) {
   for (int64_t i = 0; i < c.ninst; ++i) {
     const InstDesc& d = c.h_inst[i];
-    for (int k = 0; k < 2; ++k)
-      CU(cudaMemcpyAsync(c.A.tbuf[sn.scal[i].role[k]] + d.off, sn.t + k * c.ncells + d.off,
+    for (int k = 0; k < 4; ++k)
+      CU(cudaMemcpyAsync(snapshot_field(c, sn.scal[i], k) + d.off, sn.t + k * c.ncells + d.off,
                          8 * (size_t)d.n, cudaMemcpyDeviceToDevice, c.stream));
   }
   std::memcpy(c.h_scal, sn.scal.data(), sizeof(InstScal) * c.ninst);
-  return push_scal(c);
+  return push_scal(c, true);
 }
 }  // namespace
 
@@ -1169,17 +1181,47 @@ namespace {
 // Time the persistent solve alone: each repetition begins the next step and forms its RHS
 // (untimed), then times one solve with CUDA events on the context stream.  T^n and T^(n-1) are
 // not modified (the step's end, which rotates them, does not run); the scalars are restored.
+// A copy of every instance's H T^(n-1) (the product slot a solve's last sweep overwrites), for the
+// calls that run solves outside the step sequence and then give the context back unchanged.
+struct HxKeep {
+  Ctx& c;
+  const std::vector<InstScal>& scal;
+  double* buf = nullptr;
+  HxKeep(Ctx& ctx, const std::vector<InstScal>& s) : c(ctx), scal(s) {}
+  ~HxKeep() { if (buf) cudaFree(buf); }
+  double* slot(int64_t i) const { return c.A.hx[1 - scal[i].hx_role] + c.h_inst[i].off; }
+  cudaError_t copy(bool save) {
+    for (int64_t i = 0; i < c.ninst; ++i) {
+      const int64_t off = c.h_inst[i].off, n = c.h_inst[i].n;
+      cudaError_t e = save ? cudaMemcpyAsync(buf + off, slot(i), 8 * n, cudaMemcpyDeviceToDevice, c.stream)
+                           : cudaMemcpyAsync(slot(i), buf + off, 8 * n, cudaMemcpyDeviceToDevice, c.stream);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  }
+  int save() {
+    cudaError_t e = cudaMalloc(&buf, sizeof(double) * (size_t)c.ncells);
+    if (e == cudaSuccess) e = copy(true);
+    return e == cudaSuccess ? HF_OK : set_err(HF_ECUDA, std::string("H T copy: ") + cudaGetErrorString(e));
+  }
+};
+
 int time_solve(Ctx& c, int reps, double* ms) {
   if (!c.state_set) return set_err(HF_ESTATE, "hf_set_state must be called first");
   int rc = sync_scal(c);
   if (rc) return rc;
   std::vector<InstScal> saved(c.h_scal, c.h_scal + c.ninst);
   const int64_t itime = saved[0].itime + 1;
+  // each solve's last sweep overwrites H T^(n-1), which the next repetition's first residual
+  // reads: put it back before every repetition (outside the timed region)
+  HxKeep keep(c, saved);
+  if ((rc = keep.save())) return rc;
   cudaEvent_t e0, e1;
   CU(cudaEventCreate(&e0));
   CU(cudaEventCreate(&e1));
   double total = 0.0;
   for (int r = 0; r < reps; ++r) {
+    CU(keep.copy(false));
     CU(launch_step_begin(c, itime, 0));
     CU(launch_rhs(c));
     CU(launch_finalize(c, FIN_RHS, nullptr, 0, 0));
@@ -1193,10 +1235,12 @@ int time_solve(Ctx& c, int reps, double* ms) {
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  CU(keep.copy(false));
+  CU(cudaStreamSynchronize(c.stream));
   SolveCtl sc;
   CU(cudaMemcpy(&sc, c.d_sctl, sizeof(sc), cudaMemcpyDeviceToHost));
   std::memcpy(c.h_scal, saved.data(), sizeof(InstScal) * c.ninst);
-  if ((rc = push_scal(c))) return rc;
+  if ((rc = push_scal(c, true))) return rc;
   if (sc.err) return set_err(HF_EDEVICE, "persistent solve: a grid barrier wait reached its time limit");
   if (sc.guard_hit) return set_err(HF_EDEVICE, "persistent solve reached its round bound");
   *ms = total / reps;
@@ -1215,6 +1259,8 @@ int hf_check_barrier_timeout(hf_ctx* h, int32_t wait_ms, int32_t* status, double
   int rc = sync_scal(c);
   if (rc) return rc;
   std::vector<InstScal> saved(c.h_scal, c.h_scal + c.ninst);
+  HxKeep keep(c, saved);                 // the abandoned solve may have written H T^(n-1)
+  if ((rc = keep.save())) return rc;
   CU(launch_step_begin(c, saved[0].itime + 1, 0));
   CU(launch_rhs(c));
   CU(launch_finalize(c, FIN_RHS, nullptr, 0, 0));
@@ -1233,8 +1279,9 @@ int hf_check_barrier_timeout(hf_ctx* h, int32_t wait_ms, int32_t* status, double
   CU(cudaMemcpy(&sc, c.d_sctl, sizeof(sc), cudaMemcpyDeviceToHost));
   *status = sc.err ? HF_EDEVICE : (sc.guard_hit ? HF_EDEVICE : HF_OK);
   if (seconds) *seconds = ms * 1e-3;
+  CU(keep.copy(false));
   std::memcpy(c.h_scal, saved.data(), sizeof(InstScal) * c.ninst);
-  return push_scal(c);
+  return push_scal(c, true);
 }
 
 int hf_solve_profile(hf_ctx* h, int64_t cap, int64_t* rounds, int32_t* phases, double* round_us) {
@@ -1256,7 +1303,7 @@ int hf_solve_profile(hf_ctx* h, int64_t cap, int64_t* rounds, int32_t* phases, d
 }
 
 int hf_time_kernel(hf_ctx* h, int which, int reps, double* ms) {
-  if (!h || !ms || reps < 1 || which < HF_KERNEL_RHS || which > HF_KERNEL_CG_PQ)
+  if (!h || !ms || reps < 1 || which < HF_KERNEL_RHS || which > HF_KERNEL_RESIDUAL_INIT)
     return set_err(HF_EARG, "bad arguments");
   if (which == HF_KERNEL_SOLVE) return time_solve(h->c, reps, ms);
   Ctx& c = h->c;
@@ -1269,7 +1316,7 @@ int hf_time_kernel(hf_ctx* h, int which, int reps, double* ms) {
     s.outer_active = 1;
     const bool cg = (which >= HF_KERNEL_CG_P && which <= HF_KERNEL_CG_UPDATE) || which == HF_KERNEL_CG_PQ;
     s.inner_active = cg ? 1 : 0;
-    s.refine = 1;
+    s.refine = which == HF_KERNEL_RESIDUAL_INIT ? 0 : 1;
     s.iter = (which == HF_KERNEL_CG_P || which == HF_KERNEL_CG_UPDATE || which == HF_KERNEL_CG_PQ ||
               which == HF_KERNEL_RESIDUAL) ? 1 : 0;
     s.status = 0;
@@ -1295,7 +1342,8 @@ int hf_time_kernel(hf_ctx* h, int which, int reps, double* ms) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   std::memcpy(c.h_scal, saved.data(), sizeof(InstScal) * c.ninst);
-  if ((rc = push_scal(c))) return rc;
+  // only the residual sweep after an update writes the stored products H T
+  if ((rc = push_scal(c, which != HF_KERNEL_RESIDUAL))) return rc;
   *ms = total / reps;
   return HF_OK;
 }
@@ -1432,9 +1480,8 @@ int hf_set_state_device(hf_ctx* h, const double* tp, const double* tpp) {
   const InstScal& s = c.h_scal[0];
   CU(cudaMemcpyAsync(c.A.tbuf[s.role[0]] + d.off, tp, 8 * d.n, cudaMemcpyDeviceToDevice, c.stream));
   CU(cudaMemcpyAsync(c.A.tbuf[s.role[1]] + d.off, tpp, 8 * d.n, cudaMemcpyDeviceToDevice, c.stream));
-  CU(cudaStreamSynchronize(c.stream));
   c.state_set = true;
-  return HF_OK;
+  return push_scal(c);   // a new state: the stored products H T are stale
 }
 
 int hf_get_state_device(hf_ctx* h, double* tp, double* tpp) {

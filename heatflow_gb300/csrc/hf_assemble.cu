@@ -470,6 +470,7 @@ __global__ void k_tempdep(DevArrays A, const int32_t* toff, const double* trows,
   const int inst = A.tile_inst[g / kTile];
   const InstDesc& d = A.inst[inst];
   if (g - d.off >= d.n) return;
+  if (g == d.off) A.scal[inst].hx_ok = 0;      // H changes: the stored products H T are stale
   const int32_t t = cell_table[g];
   if (t < 0) return;
   const double* rows = trows + 4 * (int64_t)toff[t];

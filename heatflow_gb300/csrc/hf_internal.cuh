@@ -92,6 +92,10 @@ struct InstScal {
   int32_t tiny_pending; // x still needs the reference's +TINY (applied with the next update)
   int32_t phase;        // persistent solve: work of this instance in the current round (PH_*)
   int32_t role[4];      // temperature buffers: [0]=T^n, [1]=T^(n-1), [2]=x read, [3]=x write
+  int32_t hx_role;      // hx[hx_role] = H T^n, hx[1 - hx_role] = H T^(n-1) (when hx_ok says so)
+  int32_t hx_ok;        // how many of those two products are valid (trailing steps, 0..2)
+  int32_t hx_fresh;     // this step's last sweep stored H x of its final x in hx[1 - hx_role]
+  int32_t pad3;
   double sigma_prev;    // scale used by the previous residual sweep
   double last_err, last_relres;   // of the last finished step
   int64_t last_iter;
@@ -163,6 +167,9 @@ struct DevArrays {
   double* tau_s;          // tau/dt^2 (heater case 5)
   // state: four temperature-sized buffers, roles per instance in InstScal::role
   double* tbuf[4];
+  // H T^n and H T^(n-1), stored by the final residual sweep of each step: the next step's first
+  // residual is then S - H x0 = S - 2 H T^n + H T^(n-1), pointwise (x0 = 2 T^n - T^(n-1))
+  double* hx[2];
   // solver
   double *b, *y, *r, *p, *q, *p2;
   float *y32, *r32, *p32, *q32, *p232;   // p / p2: search directions, ping-pong by iteration

@@ -60,17 +60,30 @@ __device__ __forceinline__ void begin_step(InstScal& s, int64_t itime) {
   s.x0flag = 0;
   s.tiny_pending = 0;
   s.err = 0.0;
+  s.hx_fresh = 0;
   s.phase = s.outer_active ? PH_RES_INIT : PH_IDLE;   // the persistent solve's first round
 }
 
 // Finished steps rotate the temperature roles: T^(n-1) <- T^n, T^n <- x (mod_evolve.f90:169-170).
+// The stored H x of the final x becomes H T^n, the previous H T^n becomes H T^(n-1); a step that
+// ended without a sweep of its final x (accepted at its first residual) leaves no valid product.
 __device__ __forceinline__ void end_step(InstScal& s) {
-  if (s.status != 0) return;
+  if (s.status != 0) {
+    s.hx_ok = 0;
+    return;
+  }
   const int r0 = s.role[0], r1 = s.role[1], r2 = s.role[2], r3 = s.role[3];
   s.role[0] = r2;  // x
   s.role[1] = r0;  // old T^n
   s.role[2] = r1;  // free
   s.role[3] = r3;  // free
+  if (s.hx_fresh) {
+    s.hx_role ^= 1;
+    s.hx_ok = s.hx_ok < 2 ? s.hx_ok + 1 : 2;
+  } else {
+    s.hx_ok = 0;
+  }
+  s.hx_fresh = 0;
 }
 
 __global__ void k_step_begin(DevArrays A, int64_t itime) {
@@ -173,13 +186,67 @@ __device__ __forceinline__ int y_south(const TCell& c) {
   return c.py ? (c.ny - 1) * c.nx : kNoNbr;
 }
 
+// First residual of a step from the products the last two steps stored: x0 = T^n + (T^n - T^(n-1))
+// (mod_evolve.f90:141), so S - H x0 = S - 2 H T^n + H T^(n-1) up to the rounding of x0 (~1e-16 of
+// the terms).  Pointwise: 40 B and 4 FP64 instructions per cell (mixed) instead of the stencil
+// sweep's 64 B and 9.  The step's acceptance test stays the FP64 residual of the final x.
+template <typename TR>
+__device__ __forceinline__ void res_hx_task(const DevArrays& A, double* part, int64_t task,
+                                            const InstScal& s) {
+  const TCell c = task_cell(A, task);
+  const int64_t off = c.off;
+  const double* __restrict__ b = A.b + off;
+  const double* __restrict__ yc = A.hx[s.hx_role] + off;
+  const double* __restrict__ yp = A.hx[1 - s.hx_role] + off;
+  const double* __restrict__ rsum = A.rsum + off;
+  const float* __restrict__ sinv32 = A.sinv32 + off;
+  const double* __restrict__ sinv = A.sinv + off;
+  TR* R = Vec<TR>::r(A) + off;
+  const float isig = (float)(1.0 / s.sigma);
+  const bool tiny = s.x0flag != 0;            // the residual of x0 + TINY: r(x0) - TINY * H1
+  double rr = 0.0, gg64 = 0.0;
+  float gg = 0.f;
+  if (c.act(0)) {
+    const int nxy = c.nxy, base = c.base(0);
+#pragma unroll 4
+    for (int z = c.z0; z < c.z1; ++z) {
+      const int l = base + z * nxy;
+      double a = fma(-2.0, yc[l], b[l]);
+      a = a + yp[l];
+      if (tiny) a = fma(-kTiny, rsum[l], a);
+      rr = fma(a, a, rr);
+      if (sizeof(TR) == 4) {
+        const float g = -sinv32[l] * f64_to_f32_trunc(a) * isig;
+        R[l] = (TR)g;
+        gg = fmaf(g, g, gg);
+      } else {
+        const double g = -sinv[l] * a;
+        R[l] = (TR)g;
+        gg64 = fma(g, g, gg64);
+      }
+    }
+  }
+  if (sizeof(TR) == 4) {
+    task_store_f(part + task * kNR, 1, gg);
+    const double v[1] = {rr};
+    tile_store<1>(part + task * kNR, v);
+  } else {
+    const double v[2] = {rr, gg64};
+    tile_store<2>(part + task * kNR, v);
+  }
+}
+
 // FP64 true residual of one task: r = S - H x with x in the x-read buffer (INIT: x0 from the RHS
 // kernel) or, after an update, in the x-write buffer (the epilogue then swaps the roles).  Writes
 // g = -S^-1 r / sigma into the inner residual (type TR).  FP64 work per cell: 7 FMA for S - Hx,
-// 1 FMA for ||r||^2.
+// 1 FMA for ||r||^2; after an update also H x = S - r into hx[1 - hx_role] (1 subtraction).
 template <bool INIT, typename TR>
 __device__ __forceinline__ void res_task(const DevArrays& A, double* part, int64_t task,
                                           const InstScal& s) {
+  if (INIT && s.hx_ok >= 2) {
+    res_hx_task<TR>(A, part, task, s);
+    return;
+  }
   const TCell c = task_cell(A, task);
   const int64_t off = c.off;
   const double* X = A.tbuf[INIT ? s.role[2] : s.role[3]] + off;
@@ -192,6 +259,7 @@ __device__ __forceinline__ void res_task(const DevArrays& A, double* part, int64
   const float* __restrict__ sinv32 = A.sinv32 + off;
   const double* __restrict__ sinv = A.sinv + off;
   TR* R = Vec<TR>::r(A) + off;
+  double* HX = A.hx[1 - s.hx_role] + off;
   const float isig = (float)(1.0 / s.sigma);
   // INIT: the residual of x0 + TINY (mod_evolve.f90:141) is r(x0) - TINY * H1
   const bool tiny = INIT && s.x0flag;
@@ -208,11 +276,12 @@ __device__ __forceinline__ void res_task(const DevArrays& A, double* part, int64
   for (int z = c.z0; z < c.z1; ++z) {
     const int l = base + z * nxy;
     const double xn = plane_above<double>(c, 0, xval, z);
-    double cxc = 0.0, a = 0.0, xwl = 0.0, cxwl = 0.0, xel = 0.0;
+    double cxc = 0.0, a = 0.0, bl = 0.0, xwl = 0.0, cxwl = 0.0, xel = 0.0;
     double cyn = 0.0, xyn = 0.0, cys = 0.0, xys = 0.0, czc = 0.0;
     if (act) {
       cxc = cx[l];
-      a = fma(-diag[l], xc, b[l]);
+      bl = b[l];
+      a = fma(-diag[l], xc, bl);
       if (tiny) a = fma(-kTiny, rsum[l], a);
       if (xe.w != kNoNbr) { xwl = X[l + xe.w]; cxwl = cx[l + xe.w]; }
       if (xe.e != kNoNbr) xel = X[l + xe.e];
@@ -234,6 +303,7 @@ __device__ __forceinline__ void res_task(const DevArrays& A, double* part, int64
         a = fma(-czm, xm, a);
       }
       rr = fma(a, a, rr);
+      if (!INIT) HX[l] = bl - a;
       if (sizeof(TR) == 4) {             // mixed: g in FP32, scaled by 1/sigma
         const float g = -sinv32[l] * f64_to_f32_trunc(a) * isig;
         R[l] = (TR)g;
@@ -983,6 +1053,7 @@ __device__ void epi_residual_s(InstScal& s, const InstDesc& G, const DevOpts& o,
   }
   if (done) {
     s.outer_active = 0;
+    s.hx_fresh = INIT ? 0 : 1;           // a sweep after an update stored H x of the final x
     if (!converged) s.unconverged += 1;
     s.last_relres = s.relres;
     s.last_err = (o.criterion == HF_STOP_RECURSIVE) ? s.err : s.relres;
@@ -1290,7 +1361,11 @@ __device__ bool grid_barrier_epilogue(const DevArrays& A, SolveCtl* ctl, unsigne
   __syncthreads();
   const unsigned g = s_gen;
   if (s_last) {
-    if (threadIdx.x == 0 && round < kRoundLog) ctl->phase_log[round] = __ldcg(&A.scal[0].phase);
+    if (threadIdx.x == 0 && round < kRoundLog) {
+      int32_t ph = __ldcg(&A.scal[0].phase);
+      if (ph == PH_RES_INIT && __ldcg(&A.scal[0].hx_ok) >= 2) ph = HF_PHASE_RES_INIT_HX;
+      ctl->phase_log[round] = ph;
+    }
     const int act = all_epilogues<T>(A, red);
     if (threadIdx.x == 0) {
       ctl->result[(g + 1) & 1] = act ? 1u : 0u;
@@ -1520,6 +1595,10 @@ cudaError_t launch_single(Ctx& c, int which) {
     case HF_KERNEL_RESIDUAL:
       if (fp32) k_residual<false, float><<<nb, kBlock, 0, c.stream>>>(c.A);
       else k_residual<false, double><<<nb, kBlock, 0, c.stream>>>(c.A);
+      break;
+    case HF_KERNEL_RESIDUAL_INIT:
+      if (fp32) k_residual<true, float><<<nb, kBlock, 0, c.stream>>>(c.A);
+      else k_residual<true, double><<<nb, kBlock, 0, c.stream>>>(c.A);
       break;
     case HF_KERNEL_XUPDATE:
       if (fp32) k_xupdate<float><<<nb, kBlock, 0, c.stream>>>(c.A);

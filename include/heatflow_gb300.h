@@ -148,7 +148,9 @@ int64_t hf_instance_cells(const hf_ctx* ctx, int64_t instance);
 int hf_set_stream(hf_ctx* ctx, void* stream);
 
 /* ---- state (Temp_p = T^n, Temp_pp = T^(n-1); globe_data, mod_global.f90:10) ------------- */
-/* Replaces initial_evolve (mod_init_evolve.f90:34-51). */
+/* Replaces initial_evolve (mod_init_evolve.f90:34-51).  A state written from the host (this call,
+ * hf_set_state_device, hf_state_device_ready) drops the products H T^n, H T^(n-1) the library keeps
+ * from its own steps, so the next two steps form their first residual with the stencil sweep. */
 int hf_set_state(hf_ctx* ctx, const double* temp_p, const double* temp_pp);
 int hf_get_state(hf_ctx* ctx, double* temp_p, double* temp_pp);
 /* Device-resident state for zero-copy callers (torch): the context's own buffers. */
@@ -211,8 +213,9 @@ enum {
   HF_KERNEL_XUPDATE = 5,     /* FP64 solution update x += S^-1 y */
   HF_KERNEL_SOLVE = 6,       /* the persistent solve kernel: one whole solve of the next step's
                                 system (the step's RHS runs before each timed launch) */
-  HF_KERNEL_CG_PQ = 7        /* the fused direction update + SpMV pass of the persistent solve's
+  HF_KERNEL_CG_PQ = 7,       /* the fused direction update + SpMV pass of the persistent solve's
                                 FP32 inner CG, launched on its own (FP64: CG_P then CG_SPMV) */
+  HF_KERNEL_RESIDUAL_INIT = 8 /* the step-start residual sweep r = S - H (x0 + TINY) */
 };
 /* Launch one kernel `reps` times on the current state, each bracketed by CUDA events on the
  * context's stream, and return its mean duration in milliseconds.  Solver scalars are restored
@@ -232,7 +235,8 @@ enum {
   HF_PHASE_CG_PQ = 5,     /* FP32 inner CG: p = r + beta p and q = Ah p in one pass */
   HF_PHASE_CG_B = 6,      /* inner CG: y += alpha p, r -= alpha q, r.r */
   HF_PHASE_XUPD = 7,      /* x += sigma S^-1 y */
-  HF_PHASE_RES = 8        /* true residual of the updated x */
+  HF_PHASE_RES = 8,       /* true residual of the updated x */
+  HF_PHASE_RES_INIT_HX = 9 /* first true residual from the stored H T^n and H T^(n-1) (pointwise) */
 };
 /* Round profile of the context's last persistent solve (use_graph = 1, or hf_time_kernel with
  * HF_KERNEL_SOLVE).  No counterpart in the reference.  *rounds = grid-wide rounds run; for the
