@@ -114,6 +114,12 @@ _SIGNATURES = {
     "hf_assemble_coo": (C.c_int, [C.c_void_p, C.c_int64, C.c_int64, _ip, _ip, _dp, _ip, _ip]),
     "hf_time_kernel": (C.c_int, [C.c_void_p, C.c_int, C.c_int, _dp]),
     "hf_measure_fp_rates": (C.c_int, [_dp, _dp]),
+    "hf_step_host_async": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_double),
+                                     C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "hf_host_sync": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "hf_host_register": (C.c_int, [C.c_void_p, C.c_size_t]),
+    "hf_host_unregister": (C.c_int, [C.c_void_p]),
+    "hf_step_timeline": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "hf_solve_profile": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_int64),
                                    C.POINTER(C.c_int32), _dp]),
     "hf_subbox_async": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_int64), C.POINTER(C.c_int64),

@@ -111,7 +111,16 @@ void drop_graph(Ctx& c) {
 }
 
 void free_all(Ctx& c) {
+  if (c.stream) cudaStreamSynchronize(c.stream);   // queued host-buffer steps may still run
   drop_graph(c);
+  for (cudaEvent_t* e : {&c.ev_placed, &c.ev_in, &c.ev_out_done}) {
+    if (*e) cudaEventDestroy(*e);
+    *e = nullptr;
+  }
+  for (auto& e : c.ev_chunk) {
+    if (e) cudaEventDestroy(e);
+    e = nullptr;
+  }
   if (c.copy_stream) cudaStreamSynchronize(c.copy_stream);
   for (auto& sl : c.sub) {
     if (sl.dev) cudaFree(sl.dev);
@@ -157,6 +166,8 @@ int validate_opts(const hf_solver_opts& o) {
 }
 
 int sync_scal(Ctx& c) {
+  if (c.async_pending)
+    return set_err(HF_ESTATE, "host-buffer steps are queued: call hf_host_sync first");
   CU(cudaMemcpyAsync(c.h_scal, c.A.scal, sizeof(InstScal) * c.ninst, cudaMemcpyDeviceToHost,
                      c.stream));
   CU(cudaStreamSynchronize(c.stream));
@@ -573,7 +584,7 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
   c.own_stream = true;
   c.ninst = count;
   // ---- layout: instances at multiples of kTile cells
-  int64_t off = 0, tiles = 0;
+  int64_t off = 0, tiles = 0, hoff = 0;
   std::vector<int32_t> tile_inst;
   c.h_inst.resize(count);
   c.h_bc.resize(count);
@@ -584,6 +595,8 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
     d.nx = (int32_t)p.nx; d.ny = (int32_t)p.ny; d.nz = (int32_t)p.nz;
     d.n = (int32_t)(p.nx * p.ny * p.nz);
     d.off = off;
+    d.hoff = hoff;
+    hoff += d.n;
     d.tile0 = tiles;
     d.ntiles = (int32_t)((d.n + kTile - 1) / kTile);
     for (int t = 0; t < d.ntiles; ++t) tile_inst.push_back((int32_t)i);
@@ -681,6 +694,7 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
   if (c.any_heater) ALLOC(A.icase, N);
   for (int k = 0; k < 4; ++k) ALLOC(A.tbuf[k], N);
   ALLOC(A.hx[0], N); ALLOC(A.hx[1], N);
+  ALLOC(A.stamps, (size_t)kStamps);
   ALLOC(A.b, N); ALLOC(A.y, N); ALLOC(A.r, N); ALLOC(A.p, N); ALLOC(A.q, N); ALLOC(A.p2, N);
   ALLOC(A.y32, N); ALLOC(A.r32, N); ALLOC(A.p32, N); ALLOC(A.q32, N); ALLOC(A.p232, N);
   double *d_rho, *d_hc, *d_tau, *d_em = nullptr;
@@ -695,6 +709,7 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
   CK(cudaMemsetAsync(A.counters, 0, sizeof(unsigned) * count, c.stream));
   CK(cudaMemsetAsync(d_scal, 0, sizeof(InstScal) * count, c.stream));
   CK(cudaMemsetAsync(c.d_sctl, 0, sizeof(SolveCtl), c.stream));
+  CK(cudaMemsetAsync(A.stamps, 0, sizeof(unsigned long long) * kStamps, c.stream));
   for (void* p : {(void*)A.diag, (void*)A.cx, (void*)A.cy, (void*)A.cz, (void*)c.asm_.kappa,
                   (void*)d_rho, (void*)d_hc, (void*)d_tau, (void*)A.rhoc, (void*)A.ccat,
                   (void*)A.bvec, (void*)A.tau_s, (void*)A.a64x, (void*)A.a64y, (void*)A.a64z,
@@ -814,6 +829,8 @@ int hf_destroy(hf_ctx* h) {
 
 int hf_set_opts(hf_ctx* h, const hf_solver_opts* opts) {
   if (!h || !opts) return set_err(HF_EARG, "null argument");
+  if (h->c.async_pending)
+    return set_err(HF_ESTATE, "host-buffer steps are queued: call hf_host_sync first");
   int rc = validate_opts(*opts);
   if (rc) return rc;
   h->c.opts = *opts;
@@ -918,6 +935,133 @@ extern "C" {
 int hf_run(hf_ctx* h, int64_t itime0, int64_t nsteps, hf_stats* stats) {
   if (!h || nsteps < 0) return set_err(HF_EARG, "null context or nsteps < 0");
   return run_steps(h->c, itime0, nsteps, stats);
+}
+
+}  // extern "C"
+
+namespace {
+// Device-side view of a pinned (page-locked, mapped) host array, or null.
+double* pinned_view(const void* p) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
+  if (((uintptr_t)at.devicePointer & 7u) != 0u) return nullptr;
+  return static_cast<double*>(at.devicePointer);
+}
+}  // namespace
+
+extern "C" {
+
+int hf_step_host_async(hf_ctx* h, int64_t itime, const double* tp, const double* tpp, double* out) {
+  if (!h || !tp || !tpp || !out) return set_err(HF_EARG, "null argument");
+  Ctx& c = h->c;
+  if (!pinned_view(tp) || !pinned_view(tpp) || !pinned_view(out))
+    return set_err(HF_EARG, "hf_step_host_async: tp, tpp and out must be pinned host memory "
+                            "(cudaHostAlloc, or hf_host_register)");
+  if (c.opts.use_graph != 1 && c.opts.use_graph != 3)
+    return set_err(HF_EARG, "hf_step_host_async: needs use_graph 1 or 3 (captured steps)");
+  int64_t total = 0;
+  for (const auto& d : c.h_inst) total += d.n;
+  int rc;
+  if (!c.async_pending) {            // first step of a queue: nothing of ours is in flight
+    if ((rc = sync_scal(c))) return rc;
+    c.async_before.assign(c.h_scal, c.h_scal + c.ninst);
+    c.async_steps = 0;
+    if ((rc = build_graph(c))) return rc;
+    if (!c.copy_stream) CU(cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking));
+    for (cudaEvent_t* e : {&c.ev_placed, &c.ev_in, &c.ev_out_done})
+      if (!*e) CU(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    for (auto& e : c.ev_chunk)
+      if (!e) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    for (double** b : {&c.d_stage_p, &c.d_stage_pp, &c.d_stage_out})
+      if (!*b && (rc = dalloc(c, b, (size_t)total))) return rc;
+    CU(cudaEventRecord(c.ev_placed, c.stream));
+    c.last_out = nullptr;
+  }
+  const bool loop = c.opts.use_graph == 1 && build_loop_graph(c) == HF_OK;
+  const int64_t chunk = (total + Ctx::kHostChunks - 1) / Ctx::kHostChunks;
+  // Copy stream.  The staging buffers are free once the previous step placed its inputs; by then
+  // every download older than the previous step's is done too (the main stream is in order).
+  // T^(n-1) is normally such an older result, so its upload overlaps the previous step's solve.
+  // T^n is normally the previous step's result: each chunk follows that chunk's download, so the
+  // two directions of the link run at once.
+  CU(cudaStreamWaitEvent(c.copy_stream, c.ev_placed, 0));
+  if (tpp == c.last_out) CU(cudaStreamWaitEvent(c.copy_stream, c.ev_out_done, 0));
+  CU(cudaMemcpyAsync(c.d_stage_pp, tpp, sizeof(double) * (size_t)total, cudaMemcpyHostToDevice,
+                     c.copy_stream));
+  for (int k = 0; k < Ctx::kHostChunks; ++k) {
+    const int64_t lo = k * chunk, n = std::min<int64_t>(chunk, total - lo);
+    if (n <= 0) break;
+    if (tp == c.last_out) CU(cudaStreamWaitEvent(c.copy_stream, c.ev_chunk[k], 0));
+    CU(cudaMemcpyAsync(c.d_stage_p + lo, tp + lo, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice,
+                       c.copy_stream));
+  }
+  CU(cudaEventRecord(c.ev_in, c.copy_stream));
+  // Main stream: place the inputs, run the step, gather its result, download it chunk by chunk.
+  CU(cudaStreamWaitEvent(c.stream, c.ev_in, 0));
+  CU(launch_host_in(c, c.d_stage_p, 0, c.stream));
+  CU(launch_host_in(c, c.d_stage_pp, 1, c.stream));
+  CU(cudaEventRecord(c.ev_placed, c.stream));
+  const int64_t per = c.opts.precision == HF_PREC_MIXED ? c.opts.inner_itmax : c.opts.itmax;
+  CU(launch_ctrl_init(c, itime, 2 * (int64_t)(c.opts.max_refine + 3) * (per + 3)));
+  CU(cudaGraphLaunch(loop ? c.loop_exec : c.graph_exec, c.stream));
+  CU(launch_host_out(c, c.d_stage_out, c.stream));
+  for (int k = 0; k < Ctx::kHostChunks; ++k) {
+    const int64_t lo = k * chunk, n = std::min<int64_t>(chunk, total - lo);
+    if (n > 0)
+      CU(cudaMemcpyAsync(out + lo, c.d_stage_out + lo, sizeof(double) * (size_t)n,
+                         cudaMemcpyDeviceToHost, c.stream));
+    CU(cudaEventRecord(c.ev_chunk[k], c.stream));
+  }
+  CU(cudaEventRecord(c.ev_out_done, c.stream));
+  c.last_out = out;
+  c.async_pending = true;
+  c.async_steps += 1;
+  c.state_set = true;
+  return HF_OK;
+}
+
+int hf_host_sync(hf_ctx* h, hf_stats* stats) {
+  if (!h) return set_err(HF_EARG, "null context");
+  Ctx& c = h->c;
+  if (!c.async_pending) {
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    return HF_OK;
+  }
+  c.async_pending = false;
+  CtrlState cs{};
+  CU(cudaMemcpyAsync(&cs, c.d_ctrl, sizeof(cs), cudaMemcpyDeviceToHost, c.stream));
+  CU(cudaStreamSynchronize(c.stream));
+  CU(cudaStreamSynchronize(c.copy_stream));
+  const int64_t steps = c.async_steps;
+  c.async_steps = 0;
+  c.launches += cs.launches + 4 * steps;
+  if (cs.guard_hit & 2)
+    return set_err(HF_EDEVICE, "persistent solve: a grid barrier wait reached its time limit");
+  if (cs.guard_hit) return set_err(HF_EDEVICE, "captured solve loop reached its iteration bound");
+  int rc = sync_scal(c);
+  if (rc) return rc;
+  if ((rc = diagnose(c))) return rc;
+  fill_stats(c, stats, steps, c.async_before);
+  if (stats) stats->kernel_launches = cs.launches + 4 * steps;
+  return first_error(c);
+}
+
+int hf_host_register(void* ptr, size_t bytes) {
+  if (!ptr || bytes == 0) return set_err(HF_EARG, "null pointer or zero size");
+  cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterMapped | cudaHostRegisterPortable);
+  if (e != cudaSuccess) return set_err(HF_ECUDA, std::string("cudaHostRegister: ") + cudaGetErrorString(e));
+  return HF_OK;
+}
+
+int hf_host_unregister(void* ptr) {
+  if (!ptr) return set_err(HF_EARG, "null pointer");
+  cudaError_t e = cudaHostUnregister(ptr);
+  if (e != cudaSuccess) return set_err(HF_ECUDA, std::string("cudaHostUnregister: ") + cudaGetErrorString(e));
+  return HF_OK;
 }
 
 }  // extern "C"
@@ -1282,6 +1426,20 @@ int hf_check_barrier_timeout(hf_ctx* h, int32_t wait_ms, int32_t* status, double
   CU(keep.copy(false));
   std::memcpy(c.h_scal, saved.data(), sizeof(InstScal) * c.ninst);
   return push_scal(c, true);
+}
+
+int hf_step_timeline(hf_ctx* h, double* us) {
+  if (!h || !us) return set_err(HF_EARG, "null argument");
+  Ctx& c = h->c;
+  unsigned long long t[kStamps];
+  CU(cudaStreamSynchronize(c.stream));
+  CU(cudaMemcpy(t, c.A.stamps, sizeof(t), cudaMemcpyDeviceToHost));
+  // intervals between consecutive stamps; -1 where a stamp of the chain was not written in order
+  for (int k = 0; k < 5; ++k) {
+    const unsigned long long a = t[k], b = t[k + 1];
+    us[k] = (a != 0 && b >= a) ? (double)(b - a) * 1e-3 : -1.0;
+  }
+  return HF_OK;
 }
 
 int hf_solve_profile(hf_ctx* h, int64_t cap, int64_t* rounds, int32_t* phases, double* round_us) {

@@ -63,6 +63,20 @@ struct Ctx {
   SubSlot sub[kSubSlots];
   cudaStream_t copy_stream = nullptr;
   int64_t next_ticket = 0;
+  // host-buffer steps queued without host round trips (hf_step_host_async): copy engines move
+  // compact staging buffers; kernels place them into (and gather from) the role buffers
+  static constexpr int kHostChunks = 8;
+  cudaEvent_t ev_placed = nullptr;     // the last queued step's inputs are in their role buffers
+  cudaEvent_t ev_in = nullptr;         // the next step's inputs are in the staging buffers
+  cudaEvent_t ev_out_done = nullptr;   // the last queued step's result is on the host
+  cudaEvent_t ev_chunk[kHostChunks] = {};   // ... chunk by chunk
+  double* d_stage_p = nullptr;         // T^n of the next step (compact layout)
+  double* d_stage_pp = nullptr;        // T^(n-1) of the next step
+  double* d_stage_out = nullptr;       // the last step's result
+  const double* last_out = nullptr;    // host array of the last queued download
+  bool async_pending = false;          // steps queued since the last hf_host_sync
+  int64_t async_steps = 0;
+  std::vector<InstScal> async_before;  // scalars before the first queued step
   // tabulated properties re-evaluated after every step (hf_set_property_tables)
   bool tempdep = false;
   int32_t* d_toff = nullptr;

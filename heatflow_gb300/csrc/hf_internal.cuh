@@ -60,6 +60,7 @@ struct InstDesc {
   int64_t task0;      // first task of the step kernels
   int32_t ntask;      // tasks of this instance
   int32_t zc;         // planes per task (the task depth)
+  int64_t hoff;       // first cell in the compact host layout (instances back to back, no padding)
 };
 
 // Per-instance mutable scalars (device memory).
@@ -170,6 +171,8 @@ struct DevArrays {
   // H T^n and H T^(n-1), stored by the final residual sweep of each step: the next step's first
   // residual is then S - H x0 = S - 2 H T^n + H T^(n-1), pointwise (x0 = 2 T^n - T^(n-1))
   double* hx[2];
+  // step timeline: %globaltimer when the kernels of the latest step started (kStamp* slots)
+  unsigned long long* stamps;
   // solver
   double *b, *y, *r, *p, *q, *p2;
   float *y32, *r32, *p32, *q32, *p232;   // p / p2: search directions, ping-pong by iteration
@@ -177,6 +180,16 @@ struct DevArrays {
   const int4* tasks;        // (instance, x0, y0, z0) per task
   int64_t ncells, ntiles, ninst, ntasks;
 };
+
+// Slots of DevArrays::stamps: step begin, RHS start, RHS finalize start, solve start, end of the
+// solve's last round, step end.
+enum { kStampBegin = 0, kStampRhs, kStampFin, kStampSolve, kStampSolveEnd, kStampEnd, kStamps = 8 };
+
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 
 // ---- helpers ---------------------------------------------------------------------------------
 // IEEE-754 bit access through inline PTX, so that tests and format conversions stay integer
@@ -329,6 +342,12 @@ cudaError_t launch_task_heat(Ctx& c);
 cudaError_t launch_tempdep(Ctx& c);
 cudaError_t launch_subbox_gather(Ctx& c, int64_t inst, const int64_t* lo, const int64_t* hi,
                                  int which, double* dst);
+// Temperature role buffer `which` of every instance <-> a compact device array, on `stream`;
+// host_in drops the stored products H T of an instance whose state it changes.
+cudaError_t launch_host_in(Ctx& c, const double* src, int which, cudaStream_t stream);
+cudaError_t launch_host_out(Ctx& c, double* dst, cudaStream_t stream);
+// Control block of a one-step graph launch queued without the host (async host-buffer steps).
+cudaError_t launch_ctrl_init(Ctx& c, int64_t itime, int64_t limit);
 cudaError_t launch_rhs_parts(Ctx& c, double* B, double* Q, double* Qd, double* Sc);
 cudaError_t launch_rhs_diagnose(Ctx& c);
 cudaError_t launch_adj_rhs(Ctx& c, const double* g, const double* l1, const double* l2, double* out);

@@ -155,6 +155,7 @@ template <bool PARTS, bool DIAG>
 __global__ void __launch_bounds__(kBlock, 4) k_rhs(DevArrays A, double* oB, double* oQ, double* oQd,
                                                 double* oSc) {
   const int64_t task = blockIdx.x;
+  if (!PARTS && !DIAG && task == 0 && threadIdx.x == 0) A.stamps[kStampRhs] = gtimer();
   if (!PARTS && !DIAG) {          // the step's pass: vector form where the rows allow it
     const int inst = A.tasks[task].x;
     const InstDesc& d = A.inst[inst];
@@ -421,6 +422,70 @@ cudaError_t launch_subbox_gather(Ctx& c, int64_t inst, const int64_t* lo, const 
   const unsigned nb = (unsigned)std::min<int64_t>((n + 255) / 256, 4096);
   k_subbox_gather<<<nb, 256, 0, c.stream>>>(c.A, (int)inst, which, (int)lo[0], (int)lo[1], (int)lo[2],
                                             bx, by, bz, dst);
+  return cudaGetLastError();
+}
+
+// ---- host-buffer steps: staging arrays <-> role buffers -----------------------------------------
+// The copy engines move compact arrays (instance i's cells from InstDesc::hoff, no padding); these
+// kernels place them into, or gather them from, the temperature role buffers, whose indices live
+// on the device, so they can be queued behind the step that rotates the roles.  Placing compares
+// bit patterns first: an input that is exactly the state already there (a caller feeding back the
+// results it downloaded) keeps the stored products H T^n, H T^(n-1); any other drops them.
+__global__ void k_host_in(DevArrays A, const double* __restrict__ src, int which) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < A.ncells; g += stride) {
+    const int inst = A.tile_inst[g / kTile];
+    const InstDesc& d = A.inst[inst];
+    const int64_t l = g - d.off;
+    if (l >= d.n) continue;
+    double* dst = A.tbuf[A.scal[inst].role[which]];
+    const double v = src[d.hoff + l];
+    if (dbits(dst[g]) != dbits(v)) A.scal[inst].hx_ok = 0;
+    dst[g] = v;
+  }
+}
+
+__global__ void k_host_out(DevArrays A, double* __restrict__ dst) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < A.ncells; g += stride) {
+    const int inst = A.tile_inst[g / kTile];
+    const InstDesc& d = A.inst[inst];
+    const int64_t l = g - d.off;
+    if (l >= d.n) continue;
+    dst[d.hoff + l] = A.tbuf[A.scal[inst].role[0]][g];
+  }
+}
+
+// itime of the next one-step launch; the kernel count and the failure flag accumulate over the
+// queued steps (reset = first step of a queue).
+__global__ void k_ctrl_init(CtrlState* ctrl, int64_t itime, int64_t limit, int reset) {
+  ctrl->itime = itime;
+  ctrl->itime_end = itime + 1;
+  ctrl->loop_iter = 0;
+  ctrl->limit = limit;
+  ctrl->fin_count = 0u;
+  if (reset) {
+    ctrl->guard_hit = 0;
+    ctrl->launches = 0;
+  }
+}
+
+static unsigned host_copy_blocks(Ctx& c) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>((c.ncells + 255) / 256, 152 * 8));
+}
+
+cudaError_t launch_host_in(Ctx& c, const double* src, int which, cudaStream_t stream) {
+  k_host_in<<<host_copy_blocks(c), 256, 0, stream>>>(c.A, src, which);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_host_out(Ctx& c, double* dst, cudaStream_t stream) {
+  k_host_out<<<host_copy_blocks(c), 256, 0, stream>>>(c.A, dst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ctrl_init(Ctx& c, int64_t itime, int64_t limit) {
+  k_ctrl_init<<<1, 1, 0, c.stream>>>(c.d_ctrl, itime, limit, c.async_steps == 0 ? 1 : 0);
   return cudaGetLastError();
 }
 

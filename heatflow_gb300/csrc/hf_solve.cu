@@ -88,11 +88,13 @@ __device__ __forceinline__ void end_step(InstScal& s) {
 
 __global__ void k_step_begin(DevArrays A, int64_t itime) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < kStamps) A.stamps[i] = i == kStampBegin ? gtimer() : 0ull;
   if (i < A.ninst) begin_step(A.scal[i], itime);
 }
 
 __global__ void k_step_end(DevArrays A) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i == 0) A.stamps[kStampEnd] = gtimer();
   if (i < A.ninst) end_step(A.scal[i]);
 }
 
@@ -1149,6 +1151,7 @@ __global__ void __launch_bounds__(256) k_finalize(DevArrays A, CtrlState* ctrl,
                                                   cudaGraphConditionalHandle hw, int graph) {
   constexpr int NR = (KIND == FIN_RHS_DIAG) ? 5 : (KIND == FIN_SPMV ? 1 : 2);
   const int inst = blockIdx.x;
+  if (KIND == FIN_RHS && inst == 0 && threadIdx.x == 0) A.stamps[kStampFin] = gtimer();
   const InstDesc& d = A.inst[inst];
   if (took_part<KIND>(A.scal[inst])) {
     double acc[NR];
@@ -1189,6 +1192,7 @@ __global__ void __launch_bounds__(256) k_finalize(DevArrays A, CtrlState* ctrl,
 // ---- captured step: control kernels of the conditional nodes -----------------------------------
 __global__ void k_graph_step_begin(DevArrays A, CtrlState* ctrl, int launches_per_step) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < kStamps) A.stamps[i] = i == kStampBegin ? gtimer() : 0ull;
   if (i == 0) {
     ctrl->loop_iter = 0;
     ctrl->launches += launches_per_step;   // the step's kernels outside the solve loop
@@ -1202,6 +1206,7 @@ __global__ void k_graph_step_begin(DevArrays A, CtrlState* ctrl, int launches_pe
 // the step counter is below itime_end and no solve has failed, so the loop always ends.
 __global__ void k_graph_step_end(DevArrays A, CtrlState* ctrl, const SolveCtl* sctl,
                                  cudaGraphConditionalHandle hloop, int loop) {
+  if (threadIdx.x == 0) A.stamps[kStampEnd] = gtimer();
   for (int64_t i = threadIdx.x; i < A.ninst; i += blockDim.x) end_step(A.scal[i]);
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -1251,11 +1256,6 @@ __global__ void k_ctrl_select(DevArrays A, CtrlState* ctrl, cudaGraphConditional
 // needs, is guaranteed by the cooperative launch (the grid never exceeds the occupancy bound).
 constexpr unsigned long long kBarrierWaitNs = 4000000000ull;   // default barrier time limit
 
-__device__ __forceinline__ unsigned long long gtimer() {
-  unsigned long long t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
   unsigned v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
@@ -1369,7 +1369,9 @@ __device__ bool grid_barrier_epilogue(const DevArrays& A, SolveCtl* ctl, unsigne
     const int act = all_epilogues<T>(A, red);
     if (threadIdx.x == 0) {
       ctl->result[(g + 1) & 1] = act ? 1u : 0u;
-      if (round < kRoundLog) ctl->t_round[round] = gtimer();
+      const unsigned long long t = gtimer();
+      if (round < kRoundLog) ctl->t_round[round] = t;
+      A.stamps[kStampSolveEnd] = t;
       ctl->rounds = round + 1;
       ctl->count = 0u;
       __threadfence();
@@ -1428,7 +1430,7 @@ __global__ void __launch_bounds__(kBlock, 3)
   __shared__ double red[32 * 2];
   const unsigned G = gridDim.x;
   const unsigned nt = (unsigned)A.ntasks;
-  if (blockIdx.x == 0 && threadIdx.x == 0) ctl->t_start = gtimer();
+  if (blockIdx.x == 0 && threadIdx.x == 0) A.stamps[kStampSolve] = ctl->t_start = gtimer();
   for (int64_t r = 0;; ++r) {
     if (r >= limit) {
       if (blockIdx.x == 0 && threadIdx.x == 0) ctl->guard_hit = 1;

@@ -112,6 +112,14 @@ class HeatFlow:
         n = min(rounds.value, cap, 64)
         return [(abi.PHASE_NAMES.get(ph[i], str(ph[i])), us[i]) for i in range(n)], rounds.value
 
+    def step_timeline(self):
+        """Microseconds of the latest step: step begin -> RHS, RHS -> its finalize, finalize ->
+        persistent solve, solve (to the end of its last round), -> step end (None where absent)."""
+        us = (C.c_double * 5)()
+        abi.check(self.lib.hf_step_timeline(self.h, us), "hf_step_timeline")
+        keys = ("begin_to_rhs", "rhs", "finalize", "solve", "solve_to_end")
+        return {k: (us[i] if us[i] >= 0 else None) for i, k in enumerate(keys)}
+
     def set_property_tables(self, tables, cell_table):
         """Temperature-dependent properties: `tables` = list of (m, 4) arrays of rows
         (T ascending, kappa, rho, c); `cell_table` = a table index or -1 per cell (all grids, cell
@@ -209,6 +217,21 @@ class HeatFlow:
     def run(self, itime0: int, nsteps: int) -> dict:
         st = abi.HfStats()
         abi.check(self.lib.hf_run(self.h, int(itime0), int(nsteps), C.byref(st)), "run")
+        return st.as_dict()
+
+    def step_host_async(self, itime: int, tp, tpp, out):
+        """Queue one step from pinned host arrays (tp = T^n, tpp = T^(n-1)) into pinned `out`
+        (all float64, total_cells long, kept alive and untouched until host_sync)."""
+        for a in (tp, tpp, out):
+            assert a.dtype == np.float64 and a.flags.c_contiguous and a.size == self.n
+        self._queued = getattr(self, "_queued", []) + [(tp, tpp, out)]
+        abi.check(self.lib.hf_step_host_async(self.h, int(itime), _d(tp), _d(tpp), _d(out)),
+                  "hf_step_host_async")
+
+    def host_sync(self) -> dict:
+        st = abi.HfStats()
+        self._queued = []
+        abi.check(self.lib.hf_host_sync(self.h, C.byref(st)), "hf_host_sync")
         return st.as_dict()
 
     # ---- parity probes

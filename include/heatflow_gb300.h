@@ -203,6 +203,27 @@ int hf_adjoint_rhs(hf_ctx* ctx, const double* g, const double* lam1, const doubl
 int hf_adjoint_accumulate(hf_ctx* ctx, const double* lam, const double* x, int64_t itime,
                           double* grad_logk, double* grad_src);
 
+/* ---- host-buffer steps queued without host round trips (no reference counterpart) -------------
+ * For callers that keep the state in host arrays, as simulate() does (Temp_p/Temp_pp): each call
+ * queues one step whose inputs come from and whose result goes to pinned host memory, and returns
+ * at once.  Copy engines move compact staging buffers (kernels place them into the state's role
+ * buffers, whose indices live on the device, and gather the result).  T^(n-1) - normally the
+ * result of two calls back - is uploaded on a second stream while the previous step is still
+ * solving; T^n - normally the previous call's temp_out - is uploaded chunk by chunk right behind
+ * that download, so both directions of the host link run at once.  Any arrays may be passed:
+ * an input that is the previous call's temp_out waits for its download.  Every array
+ * holds total_cells doubles (instances back to back) and must stay valid and untouched until
+ * hf_host_sync returns.  Needs use_graph 1 or 3.  While steps are queued, every other call that
+ * reads or changes the state returns HF_ESTATE. */
+int hf_step_host_async(hf_ctx* ctx, int64_t itime, const double* temp_p, const double* temp_pp,
+                       double* temp_out);
+/* Wait for the queued steps; statistics over them and the first error (HF_ENAN_*, HF_EDEVICE). */
+int hf_host_sync(hf_ctx* ctx, hf_stats* stats);
+/* Page-lock and map an existing host array (e.g. Fortran's Temp_p) so it can be passed to
+ * hf_step_host_async; wraps cudaHostRegister. */
+int hf_host_register(void* ptr, size_t bytes);
+int hf_host_unregister(void* ptr);
+
 /* ---- measurement (no reference counterpart: the reference times with cpu_time only) ------- */
 enum {
   HF_KERNEL_RHS = 0,         /* per-step right-hand side */
@@ -217,6 +238,12 @@ enum {
                                 FP32 inner CG, launched on its own (FP64: CG_P then CG_SPMV) */
   HF_KERNEL_RESIDUAL_INIT = 8 /* the step-start residual sweep r = S - H (x0 + TINY) */
 };
+/* Timeline of the latest step, from %globaltimer stamps its kernels write when they start
+ * (microseconds): us[0] step begin -> RHS, us[1] RHS -> RHS finalize, us[2] finalize -> persistent
+ * solve, us[3] solve start -> end of its last round, us[4] -> step end.  -1 where the step had no
+ * such kernel (the per-kernel solve paths, use_graph 0 and 2, have no persistent solve).  No
+ * counterpart in the reference. */
+int hf_step_timeline(hf_ctx* ctx, double* us);
 /* Launch one kernel `reps` times on the current state, each bracketed by CUDA events on the
  * context's stream, and return its mean duration in milliseconds.  Solver scalars are restored
  * afterwards; the temperature state is not modified.  Call after at least one step. */

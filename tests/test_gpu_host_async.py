@@ -1,0 +1,127 @@
+"""Host-buffer steps queued without host round trips (hf_step_host_async / hf_host_sync): a caller
+that feeds back the results it downloads gets the bits of an uninterrupted hf_run (the stored
+products H T^n, H T^(n-1) survive an input equal to the device's state), on one grid and on a
+batch, with torch-pinned and with registered host arrays; a changed input drops the products as
+hf_set_state does; pageable arrays and calls while steps are queued are refused."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from heatflow_gb300 import abi
+from heatflow_gb300.problem import layered_slab, point_source_cube
+from heatflow_gb300.solver import HeatFlow
+
+pytestmark = pytest.mark.gpu
+
+KW = dict(precision="mixed", criterion="true", tol=1e-10, use_graph=1)
+
+
+def _pinned(n, fill):
+    torch = pytest.importorskip("torch")
+    return torch.full((n,), fill, dtype=torch.float64).pin_memory().numpy()
+
+
+def _run_ref(probs, tp, tpp, itime0, K):
+    """An uninterrupted run from a host-written state."""
+    with HeatFlow(probs, **KW) as hf:
+        hf.set_state(tp, tpp)
+        st = hf.run(itime0, K)
+        T, Tp = hf.get_state()
+        return T, Tp, st["inner_iterations"]
+
+
+def _run_async(hf, bufs, itime0, K, rot=(0, 1, 2)):
+    cur, prev, free = rot
+    for k in range(K):
+        hf.step_host_async(itime0 + k, bufs[cur], bufs[prev], bufs[free])
+        cur, prev, free = free, cur, prev
+    return hf.host_sync(), (cur, prev, free)
+
+
+def _initial(probs):
+    with HeatFlow(probs, **KW) as hf:
+        hf.initial_evolve()
+        hf.run(1, 2)
+        return hf.get_state()
+
+
+def test_async_equals_uninterrupted_run(cuda_lib):
+    prob = layered_slab(16, nz=20, layer=5)
+    tp, tpp = _initial(prob)
+    T_ref, Tp_ref, iters = _run_ref(prob, tp, tpp, 3, 7)
+    bufs = [_pinned(prob.ncells, 0.0) for _ in range(3)]
+    bufs[0][:] = tp
+    bufs[1][:] = tpp
+    with HeatFlow(prob, **KW) as hf:
+        st, (cur, prev, _) = _run_async(hf, bufs, 3, 7)
+    assert np.array_equal(bufs[cur], T_ref) and np.array_equal(bufs[prev], Tp_ref)
+    assert st["steps"] == 7 and st["inner_iterations"] == iters and st["unconverged"] == 0
+
+
+def test_async_products_used_and_dropped(cuda_lib):
+    """Fed-back inputs keep the products (the first residual is pointwise from the third step on);
+    a changed input makes the next two steps use the stencil, like a fresh context."""
+    prob = layered_slab(16, nz=20, layer=5)
+    tp, tpp = _initial(prob)
+    bufs = [_pinned(prob.ncells, 0.0) for _ in range(3)]
+    bufs[0][:] = tp
+    bufs[1][:] = tpp
+    kw = dict(KW, use_graph=3)
+    with HeatFlow(prob, **kw) as hf:
+        rot = (0, 1, 2)
+        first = []
+        for k in range(4):
+            _, rot = _run_async(hf, bufs, 3 + k, 1, rot)
+            first.append(hf.solve_profile()[0][0][0])
+        assert first == ["res_init", "res_init", "res_init_hx", "res_init_hx"], first
+        cur, prev, free = rot
+        bufs[cur][123] += 1e-3                      # the caller changes the state
+        T0, Tp0 = bufs[cur].copy(), bufs[prev].copy()
+        _, rot = _run_async(hf, bufs, 7, 3, rot)
+        assert hf.solve_profile()[0][0][0] == "res_init_hx"
+        T = bufs[rot[0]].copy()
+    T_ref, _, _ = _run_ref(prob, T0, Tp0, 7, 3)
+    assert np.array_equal(T, T_ref)
+
+
+def test_async_batch_registered(cuda_lib):
+    probs = [point_source_cube(12), layered_slab(8, nz=10, layer=3)]
+    tp, tpp = _initial(probs)
+    T_ref, Tp_ref, _ = _run_ref(probs, tp, tpp, 3, 5)
+    bufs = [np.zeros(tp.size) for _ in range(3)]
+    lib = abi.load_library()
+    for b in bufs:
+        assert lib.hf_host_register(b.ctypes.data_as(C.c_void_p), b.nbytes) == abi.HF_OK
+    try:
+        bufs[0][:] = tp
+        bufs[1][:] = tpp
+        with HeatFlow(probs, **KW) as hf:
+            _, (cur, prev, _) = _run_async(hf, bufs, 3, 5)
+        assert np.array_equal(bufs[cur], T_ref) and np.array_equal(bufs[prev], Tp_ref)
+    finally:
+        for b in bufs:
+            lib.hf_host_unregister(b.ctypes.data_as(C.c_void_p))
+
+
+def test_pageable_arrays_refused(cuda_lib):
+    prob = point_source_cube(8)
+    with HeatFlow(prob, **KW) as hf:
+        a = np.full(prob.ncells, 300.0)
+        with pytest.raises(abi.HeatFlowError) as e:
+            hf.step_host_async(1, a, a.copy(), a.copy())
+        assert e.value.code == abi.HF_EARG
+
+
+def test_calls_refused_while_queued(cuda_lib):
+    prob = point_source_cube(10)
+    bufs = [_pinned(prob.ncells, 300.0) for _ in range(3)]
+    with HeatFlow(prob, **KW) as hf:
+        hf.step_host_async(1, bufs[0], bufs[1], bufs[2])
+        with pytest.raises(abi.HeatFlowError) as e:
+            hf.get_state()
+        assert e.value.code == abi.HF_ESTATE
+        st = hf.host_sync()
+        assert st["steps"] == 1
+        T, Tp = hf.get_state()
+        assert np.array_equal(T, bufs[2]) and np.array_equal(Tp, bufs[0])
