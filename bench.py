@@ -63,10 +63,10 @@ BYTES_PER_CELL = {
 # FP64 floating-point operations per cell (an FMA counts 2) of the FP64-pipe kernels: the
 # residual does 7 FMA for S - Hx, 1 FMA for ||r||^2 and 1 sub for H x = S - r; the step-start
 # residual from the stored products 1 FMA + 1 add (S - 2 H T^n + H T^(n-1)), 1 FMA (TINY) and 1 FMA
-# (||r||^2); the RHS 2 mul (rho c T/dt), 1 FMA + 1 mul (S_cat), 1 add, 2 add + 1 sub (x0 and its
-# test), 1 FMA (||S||^2).
+# (||r||^2); the RHS 2 mul (rho c T/dt), 1 FMA + 1 mul (S_cat), 1 add, 2 add (x0) - its x0 - T <
+# TINY test and ||S||^2 run on the integer/FP32 pipes.
 FP64_FLOPS_PER_CELL = {"residual_mixed": 17, "residual_fp64": 19, "residual_init_hx_mixed": 7,
-                       "rhs": 12}
+                       "rhs": 8}
 
 # Algorithmic bytes per cell of each round of the persistent solve kernel (k_solve), by phase:
 # (bytes, bytes of the first inner iteration / of an update without a correction).  The first

@@ -227,6 +227,23 @@ __device__ __forceinline__ float f64_to_f32_trunc(double v) {
   if (fe <= 0) return __uint_as_float(sign);
   return __uint_as_float(sign | ((unsigned)fe << 23) | (unsigned)((u >> 29) & 0x7fffffull));
 }
+// v * 2^-k -> FP32 by truncation of the mantissa (integer instructions only); saturates like
+// f64_to_f32_trunc.  For |v| 2^-k in the FP32 normal range the result is exactly
+// f64_to_f32_trunc(v) 2^-k.
+__device__ __forceinline__ float f64_to_f32_trunc_pow2(double v, int k) {
+  const unsigned long long u = dbits(v);
+  const unsigned sign = (unsigned)(u >> 63) << 31;
+  const int e = (int)((u >> 52) & 0x7ffull);
+  if (e == 0x7ff) return __uint_as_float(sign | 0x7f800000u | ((u & 0xfffffffffffffull) ? 0x400000u : 0u));
+  if (e == 0) return __uint_as_float(sign);
+  const int fe = e - 1023 + 127 - k;
+  if (fe >= 255) return __uint_as_float(sign | 0x7f800000u);
+  if (fe <= 0) return __uint_as_float(sign);
+  return __uint_as_float(sign | ((unsigned)fe << 23) | (unsigned)((u >> 29) & 0x7fffffull));
+}
+// 2^k as an FP64 value (|k| <= 1022).
+__device__ __forceinline__ double pow2d(int k) { return bitsd((unsigned long long)(1023 + k) << 52); }
+
 // FP32 -> FP64, exact (integer instructions only).
 __device__ __forceinline__ double f32_to_f64(float f) {
   const unsigned u = __float_as_uint(f);

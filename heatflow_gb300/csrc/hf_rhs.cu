@@ -40,6 +40,44 @@ __device__ __forceinline__ double heat_case(int cs, double P, double tau, int64_
   }
 }
 
+// x0 - T < TINY (mod_evolve.f90:140-141) for x0 = RN(T + d), d = RN(T - T_old), decided from d with
+// integer compares where the rounding of x0 cannot change the answer: d <= 0 gives x0 <= T; for
+// 0 < T < 2048 the rounding of x0 and of x0 - T is below 0.23 TINY, so d <= TINY/2 and d >= 2 TINY
+// decide it.  The FP64 subtraction remains for the band between and other temperatures; the
+// result is that of dbl_lt_pos(x0 - T, TINY) in every case (a NaN d keeps its sign's answer).
+__device__ __forceinline__ bool x0_below_tiny(double tp, double d, double x0) {
+  const long long bd = (long long)dbits(d);
+  if (bd <= 0) return true;
+  const long long bt = (long long)dbits(tp);
+  if (bt > 0 && bt < (long long)dbits(2048.0)) {
+    if (bd <= (long long)dbits(0.5 * kTiny)) return true;
+    if (bd >= (long long)dbits(2.0 * kTiny)) return false;
+  }
+  return dbl_lt_pos(x0 - tp, kTiny);
+}
+
+// ||S||^2 of one thread's cells summed in FP32 over S 2^-k, k the exponent of the thread's first
+// nonzero S (integer instructions: the RHS pass is bound by the FP64 pipe, its FP32/integer pipes
+// are idle).  Relative error ~1e-6, enough for a norm that scales a threshold test.  A sum that is
+// not finite (a NaN or an out-of-range S) is redone in FP64 by the caller (recount()).
+struct SqSum {
+  float s = 0.f;
+  int k = 0;
+  bool have_k = false;
+  __device__ __forceinline__ void add(double v) {
+    if (!have_k) {
+      const int e = (int)((dbits(v) >> 52) & 0x7ffull);
+      if (e == 0) return;                     // zero (or subnormal): contributes nothing here
+      k = e - 1023;
+      have_k = true;
+    }
+    const float f = f64_to_f32_trunc_pow2(v, k);
+    s = fmaf(f, f, s);
+  }
+  __device__ __forceinline__ bool ok() const { return isfinite(s) && k > -500 && k < 500; }
+  __device__ __forceinline__ double value() const { return have_k ? f32_to_f64(s) * pow2d(2 * k) : 0.0; }
+};
+
 // The per-cell work of the step RHS (shared by the scalar and the vector forms): heater, S_cat,
 // S and the initial guess of cell l; returns S and sets x0 and the x0 - T < TINY flag.
 struct RhsCtx {
@@ -84,8 +122,9 @@ __device__ __forceinline__ double rhs_cell(const DevArrays& A, const InstDesc& d
     S = -qd;
     if (!dbl_is_zero(B)) S = S - B;
   }
-  x0 = tp + (tp - tpp);
-  flag |= dbl_lt_pos(x0 - tp, kTiny) ? 1 : 0;
+  const double dt = tp - tpp;
+  x0 = tp + dt;
+  flag |= x0_below_tiny(tp, dt, x0) ? 1 : 0;
   return S;
 }
 
@@ -112,6 +151,7 @@ __device__ __forceinline__ void rhs4_task(const DevArrays& A, int64_t task, cons
   const double* __restrict__ bvec = A.bvec + off;
   double* bout = A.b + off;
   double bb = 0.0;
+  SqSum sq;
   int flag = 0;
   if (act) {
     for (int z = za; z < zb; ++z) {
@@ -136,12 +176,21 @@ __device__ __forceinline__ void rhs4_task(const DevArrays& A, int64_t task, cons
           S[i] = rhs_cell<false>(A, d, r, off, l + i, tp[i], tpp[i], rh[i], cc[i], bv[i], x0[i], flag);
       }
 #pragma unroll
-      for (int i = 0; i < 4; ++i) bb = fma(S[i], S[i], bb);
+      for (int i = 0; i < 4; ++i) sq.add(S[i]);
       reinterpret_cast<double2*>(bout + l)[0] = make_double2(S[0], S[1]);
       reinterpret_cast<double2*>(bout + l)[1] = make_double2(S[2], S[3]);
       reinterpret_cast<double2*>(X + l)[0] = make_double2(x0[0], x0[1]);
       reinterpret_cast<double2*>(X + l)[1] = make_double2(x0[2], x0[3]);
     }
+  }
+  if (sq.ok()) {
+    bb = sq.value();
+  } else if (act) {                             // FP64 recount of this thread's cells
+    for (int z = za; z < zb; ++z)
+      for (int i = 0; i < 4; ++i) {
+        const double v = bout[lxy + z * nxy + i];
+        bb = fma(v, v, bb);
+      }
   }
   const int any_flag = __syncthreads_or(flag);
   if (threadIdx.x == 0) A.partials[task * kNR + 1] = any_flag ? 1.0 : 0.0;
@@ -199,6 +248,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_rhs(DevArrays A, double* oB, doub
   const double tb4 = has_em ? pow(d.t_bath, 4.0) : 0.0;
   const double dt2 = case5 ? pow(d.time_step, 2.0) : 0.0;
   double bb = 0.0;
+  SqSum sq;
   int flag = 0;
   int nan_q = 0, nan_qd = 0, nan_sc = 0, nan_s = 0;
   for (int z = c.z0; z < c.z1; ++z) {
@@ -239,11 +289,12 @@ __global__ void __launch_bounds__(kBlock, 4) k_rhs(DevArrays A, double* oB, doub
         if (!dbl_is_zero(B)) S = S - B;
       }
       if (DIAG) nan_s += dbl_is_nan(S);
-      const double x0 = tp + (tp - tpp);
-      flag |= dbl_lt_pos(x0 - tp, kTiny) ? 1 : 0;
+      const double dt = tp - tpp;
+      const double x0 = tp + dt;
+      flag |= x0_below_tiny(tp, dt, x0) ? 1 : 0;
       bout[l] = S;
       X[l] = x0;
-      bb = fma(S, S, bb);
+      sq.add(S);
       if (PARTS) {
         oB[off + l] = B;
         oQ[off + l] = q;
@@ -251,6 +302,17 @@ __global__ void __launch_bounds__(kBlock, 4) k_rhs(DevArrays A, double* oB, doub
         oSc[off + l] = sc;
       }
     }
+  }
+  if (sq.ok()) {
+    bb = sq.value();
+  } else {                                      // FP64 recount of this thread's cells
+    for (int z = c.z0; z < c.z1; ++z)
+#pragma unroll
+      for (int j = 0; j < kXC; ++j) {
+        if (!c.act(j)) continue;
+        const double v = bout[c.base(j) + z * c.nxy];
+        bb = fma(v, v, bb);
+      }
   }
   const int any_flag = __syncthreads_or(flag);
   if (DIAG) {
