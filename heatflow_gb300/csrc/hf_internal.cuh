@@ -241,7 +241,7 @@ __device__ __forceinline__ float f64_to_f32_trunc_pow2(double v, int k) {
   if (fe <= 0) return __uint_as_float(sign);
   return __uint_as_float(sign | ((unsigned)fe << 23) | (unsigned)((u >> 29) & 0x7fffffull));
 }
-// 2^k as an FP64 value (|k| <= 1022).
+// 2^k as an FP64 value (-1022 <= k <= 1023).
 __device__ __forceinline__ double pow2d(int k) { return bitsd((unsigned long long)(1023 + k) << 52); }
 
 // FP32 -> FP64, exact (integer instructions only).
@@ -259,6 +259,40 @@ __device__ __forceinline__ double f32_to_f64(float f) {
   }
   return bitsd(sign | ((unsigned long long)(e - 127 + 1023) << 52) | (m << 29));
 }
+
+// 2^m as an FP32 value for m <= 0 (subnormal below 2^-126, 0 below 2^-149).
+__device__ __forceinline__ float pow2f_neg(int m) {
+  if (m >= -126) return __uint_as_float((unsigned)(m + 127) << 23);
+  if (m >= -149) return __uint_as_float(1u << (m + 149));
+  return 0.f;
+}
+
+// Sum of squares of one thread's FP64 values in FP32 over v 2^-k, with k kept within 30 of the
+// largest exponent seen (the running sum is rescaled by an exact power of two when it moves), so
+// no term leaves the FP32 range and terms below 2^-60 of the largest vanish, as they would at this
+// precision anyway.  Integer and FP32 instructions only: for passes bound by the FP64 pipe, whose
+// FP32/integer pipes are idle.  Relative error ~1e-6, enough for norms that scale or feed threshold
+// tests.  NaN and infinity propagate.
+struct SqSum {
+  float s = 0.f;
+  int k = -2000;                  // no nonzero value yet
+  __device__ __forceinline__ void add(double v) {
+    const int e = (int)((dbits(v) >> 52) & 0x7ffull);
+    if (e == 0) return;           // zero or subnormal: nothing at this precision
+    const int ev = e - 1023;      // 1024 for infinity and NaN
+    if (ev > k + 30) {
+      s = k == -2000 ? 0.f : s * pow2f_neg(2 * (k - ev));
+      k = ev;
+    }
+    const float f = f64_to_f32_trunc_pow2(v, k);
+    s = fmaf(f, f, s);
+  }
+  __device__ __forceinline__ double value() const {
+    if (k == -2000) return 0.0;
+    if (!isfinite(s)) return isnan(s) ? (double)NAN : (double)INFINITY;
+    return f32_to_f64(s) * pow2d(k) * pow2d(k);
+  }
+};
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll

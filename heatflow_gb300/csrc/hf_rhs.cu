@@ -56,28 +56,6 @@ __device__ __forceinline__ bool x0_below_tiny(double tp, double d, double x0) {
   return dbl_lt_pos(x0 - tp, kTiny);
 }
 
-// ||S||^2 of one thread's cells summed in FP32 over S 2^-k, k the exponent of the thread's first
-// nonzero S (integer instructions: the RHS pass is bound by the FP64 pipe, its FP32/integer pipes
-// are idle).  Relative error ~1e-6, enough for a norm that scales a threshold test.  A sum that is
-// not finite (a NaN or an out-of-range S) is redone in FP64 by the caller (recount()).
-struct SqSum {
-  float s = 0.f;
-  int k = 0;
-  bool have_k = false;
-  __device__ __forceinline__ void add(double v) {
-    if (!have_k) {
-      const int e = (int)((dbits(v) >> 52) & 0x7ffull);
-      if (e == 0) return;                     // zero (or subnormal): contributes nothing here
-      k = e - 1023;
-      have_k = true;
-    }
-    const float f = f64_to_f32_trunc_pow2(v, k);
-    s = fmaf(f, f, s);
-  }
-  __device__ __forceinline__ bool ok() const { return isfinite(s) && k > -500 && k < 500; }
-  __device__ __forceinline__ double value() const { return have_k ? f32_to_f64(s) * pow2d(2 * k) : 0.0; }
-};
-
 // The per-cell work of the step RHS (shared by the scalar and the vector forms): heater, S_cat,
 // S and the initial guess of cell l; returns S and sets x0 and the x0 - T < TINY flag.
 struct RhsCtx {
@@ -183,15 +161,7 @@ __device__ __forceinline__ void rhs4_task(const DevArrays& A, int64_t task, cons
       reinterpret_cast<double2*>(X + l)[1] = make_double2(x0[2], x0[3]);
     }
   }
-  if (sq.ok()) {
-    bb = sq.value();
-  } else if (act) {                             // FP64 recount of this thread's cells
-    for (int z = za; z < zb; ++z)
-      for (int i = 0; i < 4; ++i) {
-        const double v = bout[lxy + z * nxy + i];
-        bb = fma(v, v, bb);
-      }
-  }
+  bb = sq.value();
   const int any_flag = __syncthreads_or(flag);
   if (threadIdx.x == 0) A.partials[task * kNR + 1] = any_flag ? 1.0 : 0.0;
   const double v[1] = {bb};
@@ -303,17 +273,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_rhs(DevArrays A, double* oB, doub
       }
     }
   }
-  if (sq.ok()) {
-    bb = sq.value();
-  } else {                                      // FP64 recount of this thread's cells
-    for (int z = c.z0; z < c.z1; ++z)
-#pragma unroll
-      for (int j = 0; j < kXC; ++j) {
-        if (!c.act(j)) continue;
-        const double v = bout[c.base(j) + z * c.nxy];
-        bb = fma(v, v, bb);
-      }
-  }
+  bb = sq.value();
   const int any_flag = __syncthreads_or(flag);
   if (DIAG) {
     const int c1 = __syncthreads_count(nan_q), c2 = __syncthreads_count(nan_qd);

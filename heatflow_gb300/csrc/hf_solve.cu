@@ -263,6 +263,9 @@ __device__ __forceinline__ void res_task(const DevArrays& A, double* part, int64
   TR* R = Vec<TR>::r(A) + off;
   double* HX = A.hx[1 - s.hx_role] + off;
   const float isig = (float)(1.0 / s.sigma);
+  // mixed, after an update: ||r||^2 summed in FP32 over per-thread scaled r (one FP64 instruction
+  // less per cell on this FP64-bound sweep)
+  SqSum rq;
   // INIT: the residual of x0 + TINY (mod_evolve.f90:141) is r(x0) - TINY * H1
   const bool tiny = INIT && s.x0flag;
   const bool act = c.act(0);
@@ -304,7 +307,8 @@ __device__ __forceinline__ void res_task(const DevArrays& A, double* part, int64
         a = fma(-czc, xn, a);
         a = fma(-czm, xm, a);
       }
-      rr = fma(a, a, rr);
+      if (INIT || sizeof(TR) == 8) rr = fma(a, a, rr);
+      else rq.add(a);
       if (!INIT) HX[l] = bl - a;
       if (sizeof(TR) == 4) {             // mixed: g in FP32, scaled by 1/sigma
         const float g = -sinv32[l] * f64_to_f32_trunc(a) * isig;
@@ -320,6 +324,7 @@ __device__ __forceinline__ void res_task(const DevArrays& A, double* part, int64
     xm = xc;
     xc = xn;
   }
+  if (!INIT && sizeof(TR) == 4) rr = rq.value();
   if (sizeof(TR) == 4) {
     task_store_f(part + task * kNR, 1, gg);
     const double v[1] = {rr};
