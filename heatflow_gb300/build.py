@@ -60,6 +60,30 @@ def _stale() -> bool:
     return any(os.path.getmtime(p) > t for p in deps)
 
 
+HOST = os.path.join(HERE, "host")
+DRIVER = os.path.join(OUT, "heatflow_gb300")
+HOST_SOURCES = ["deck.cpp", "heatflow_main.cpp"]
+
+
+def build_driver(force: bool = False) -> str:
+    """The C++ host program (HeatFlow's main program over the C ABI), linked against the library
+    with an $ORIGIN run path so it runs from the build folder."""
+    deps = [os.path.join(HOST, f) for f in os.listdir(HOST)] + [LIB, __file__]
+    if not force and os.path.exists(DRIVER) and all(os.path.getmtime(p) <= os.path.getmtime(DRIVER)
+                                                     for p in deps):
+        return DRIVER
+    gxx = shutil.which("g++") or "g++"
+    inc = os.path.join(os.path.dirname(HERE), "include")
+    cmd = [gxx, "-O2", "-std=c++17", "-Wall", "-Wextra", "-I", inc,
+           *[os.path.join(HOST, f) for f in HOST_SOURCES],
+           "-L", OUT, "-lheatflow_gb300", "-Wl,-rpath,$ORIGIN", "-o", DRIVER + ".tmp"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"g++ failed for the host program:\n{r.stderr}")
+    os.replace(DRIVER + ".tmp", DRIVER)
+    return DRIVER
+
+
 def build_library(force: bool = False, verbose: bool = False) -> str:
     if not force and not _stale():
         return LIB
@@ -77,3 +101,4 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
 
 if __name__ == "__main__":
     print(build_library(force=True, verbose=False))
+    print(build_driver(force=True))

@@ -1,0 +1,203 @@
+// HeatFlow's main program on libheatflow_gb300 (src/heatflow.f90): read the deck, set up, run
+// ntime steps, log the sub-box after step 1 and every write_every steps, and print the final
+// fields.  The reference's file layout is kept: ./inputs/{param,mat,system}.in,
+// ./restart/TempDis.dat[TPD] (initial_evolve, mod_init_evolve.f90:34-51),
+// ./outputs/output_<RunName>_NN (data_write, mod_output.f90:57-113) and
+// ./outputs/TempDis.dat[TPD] (final_print, mod_output.f90:207-238).
+//
+//   heatflow_gb300 [--inputs DIR] [--outputs DIR] [--restart DIR]
+//                  [--precision fp64|mixed] [--criterion recursive|true] [--tol X]
+//                  [--graph 0|1|2|3] [--dump-problem]
+//
+// Defaults follow the reference: FP64 with linbcg's stopping rule (recursive residual, tol 1e-32),
+// the whole step loop as CUDA graphs.  --dump-problem prints the parsed deck as JSON and stops
+// before any GPU call.  A fatal condition prints the reference's message and exits with status 1
+// (`stop 1`).
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <sys/stat.h>
+#include <vector>
+
+#include "deck.hpp"
+#include "heatflow_gb300.h"
+
+namespace {
+
+struct Options {
+  std::string inputs = "./inputs", outputs = "./outputs", restart = "./restart";
+  int precision = HF_PREC_FP64, criterion = HF_STOP_RECURSIVE, use_graph = 1;
+  double tol = -1.0;
+  bool dump_problem = false;
+};
+
+[[noreturn]] void usage(const char* msg) {
+  std::fprintf(stderr, "%s\nusage: heatflow_gb300 [--inputs DIR] [--outputs DIR] [--restart DIR] "
+                       "[--precision fp64|mixed] [--criterion recursive|true] [--tol X] "
+                       "[--graph 0|1|2|3] [--dump-problem]\n", msg);
+  std::exit(2);
+}
+
+Options parse_args(int argc, char** argv) {
+  Options o;
+  for (int i = 1; i < argc; ++i) {
+    const std::string a = argv[i];
+    auto next = [&]() -> std::string {
+      if (i + 1 >= argc) usage(("missing value after " + a).c_str());
+      return argv[++i];
+    };
+    if (a == "--inputs") o.inputs = next();
+    else if (a == "--outputs") o.outputs = next();
+    else if (a == "--restart") o.restart = next();
+    else if (a == "--precision") {
+      const std::string v = next();
+      if (v == "fp64") o.precision = HF_PREC_FP64;
+      else if (v == "mixed") o.precision = HF_PREC_MIXED;
+      else usage("--precision takes fp64 or mixed");
+    } else if (a == "--criterion") {
+      const std::string v = next();
+      if (v == "recursive") o.criterion = HF_STOP_RECURSIVE;
+      else if (v == "true") o.criterion = HF_STOP_TRUE;
+      else usage("--criterion takes recursive or true");
+    } else if (a == "--tol") o.tol = std::atof(next().c_str());
+    else if (a == "--graph") o.use_graph = std::atoi(next().c_str());
+    else if (a == "--dump-problem") o.dump_problem = true;
+    else usage(("unknown argument " + a).c_str());
+  }
+  return o;
+}
+
+int fail_lib(int rc, const char* where) {
+  const char* m = hf_strerror(rc);
+  std::fprintf(stdout, " %s\n", m ? m : "");
+  std::fprintf(stderr, "%s: %s\n", where, hf_last_error());
+  return 1;
+}
+
+bool write_file(const std::string& path, const std::string& text) {
+  FILE* f = std::fopen(path.c_str(), "wb");
+  if (!f) return false;
+  const bool ok = std::fwrite(text.data(), 1, text.size(), f) == text.size();
+  return std::fclose(f) == 0 && ok;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  const auto t0 = std::chrono::steady_clock::now();
+  const Options opt = parse_args(argc, argv);
+  std::printf(" Setup initialising\n");
+  hfhost::Deck deck;
+  try {
+    const std::string param = hfhost::read_text_file(opt.inputs + "/param.in", "Error cannot find file: param.in");
+    const std::string mat = hfhost::read_text_file(opt.inputs + "/mat.in", "Error cannot find file: mat.in");
+    const std::string sys = hfhost::read_text_file(opt.inputs + "/system.in", "Error cannot find file: system.in");
+    hfhost::build_deck(deck, param, mat, sys);
+  } catch (const hfhost::InputError& e) {
+    std::printf(" %s\n", e.what());
+    return 1;
+  }
+  if (opt.dump_problem) {
+    std::printf("%s\n", hfhost::problem_json(deck).c_str());
+    return 0;
+  }
+  const hfhost::Param& P = deck.param;
+  const int64_t n = deck.ncells();
+
+  hf_solver_opts so;
+  hf_default_opts(&so);
+  so.precision = opt.precision;
+  so.criterion = opt.criterion;
+  so.tol = opt.tol > 0 ? opt.tol : (opt.criterion == HF_STOP_RECURSIVE ? 1e-32 : 1e-10);
+  so.use_graph = opt.use_graph;
+  hf_ctx* ctx = nullptr;
+  int rc = hf_create(&deck.prob, &so, &ctx);
+  if (rc != HF_OK) return fail_lib(rc, "hf_create");
+  std::printf(" Setup complete, running simulation\n");
+
+  // initial_evolve
+  std::vector<double> tp(n), tpp(n);
+  try {
+    if (P.full_restart) {
+      tp = hfhost::parse_temp_file(hfhost::read_text_file(opt.restart + "/TempDis.dat", " Error: File not found: TempDis.dat"), n);
+      tpp = hfhost::parse_temp_file(hfhost::read_text_file(opt.restart + "/TempDisTPD.dat", " Error: File not found: TempDisTPD.dat"), n);
+    } else if (P.input_temp_dis) {
+      tp = hfhost::parse_temp_file(hfhost::read_text_file(opt.restart + "/TempDis.dat", " Error: File not found: TempDis.dat"), n);
+      tpp = tp;
+    } else {
+      std::fill(tp.begin(), tp.end(), P.t_system);
+      std::fill(tpp.begin(), tpp.end(), P.t_system);
+    }
+  } catch (const hfhost::InputError& e) {
+    std::printf(" %s\n", e.what());
+    hf_destroy(ctx);
+    return 1;
+  }
+  if ((rc = hf_set_state(ctx, tp.data(), tpp.data())) != HF_OK) return fail_lib(rc, "hf_set_state");
+
+  mkdir(opt.outputs.c_str(), 0755);
+  // sub-box of the log (1-based inclusive bounds of param.in; an empty box logs the time only)
+  const int64_t lo[3] = {P.start_ix - 1, P.start_iy - 1, P.start_iz - 1};
+  const int64_t hi[3] = {P.end_ix - 1, P.end_iy - 1, P.end_iz - 1};
+  const bool box = hi[0] >= lo[0] && hi[1] >= lo[1] && hi[2] >= lo[2];
+  const int64_t nbox = box ? (hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1) : 0;
+  std::vector<double> boxbuf(nbox > 0 ? nbox : 1);
+  FILE* log = nullptr;
+  auto log_record = [&](int64_t itime) -> int {
+    if (box) {
+      int64_t ticket = -1;
+      int r = hf_subbox_async(ctx, 0, lo, hi, 1, boxbuf.data(), &ticket);
+      if (r == HF_OK) r = hf_subbox_wait(ctx, ticket);
+      if (r != HF_OK) return r;
+    }
+    const std::string rec = hfhost::format_record((double)(itime - 1) * P.time_step, boxbuf.data(), nbox);
+    std::fwrite(rec.data(), 1, rec.size(), log);
+    return HF_OK;
+  };
+  auto final_print = [&]() -> int {
+    int r = hf_get_state(ctx, tp.data(), tpp.data());
+    if (r != HF_OK) return r;
+    if (!write_file(opt.outputs + "/TempDis.dat", hfhost::format_temp_file(tp.data(), n)) ||
+        !write_file(opt.outputs + "/TempDisTPD.dat", hfhost::format_temp_file(tpp.data(), n))) {
+      std::fprintf(stderr, "cannot write %s/TempDis.dat\n", opt.outputs.c_str());
+      return HF_EARG;
+    }
+    return HF_OK;
+  };
+
+  for (int64_t itime = 1; itime <= P.ntime; ++itime) {
+    hf_stats st;
+    rc = hf_step(ctx, itime, &st);
+    if (rc != HF_OK) {
+      fail_lib(rc, "hf_step");
+      hf_destroy(ctx);
+      return 1;
+    }
+    // data_write (mod_output.f90:57-146)
+    if (itime == 1 && !P.test_run) {
+      log = std::fopen(hfhost::next_log_name(opt.outputs, P.run_name).c_str(), "w");
+      if (!log) {
+        std::fprintf(stderr, "cannot open the log in %s\n", opt.outputs.c_str());
+        hf_destroy(ctx);
+        return 1;
+      }
+      if ((rc = log_record(itime)) != HF_OK) return fail_lib(rc, "data_write");
+    } else if (!P.test_run && P.write_to_txt && P.write_every > 0 && itime % P.write_every == 0) {
+      if ((rc = log_record(itime)) != HF_OK) return fail_lib(rc, "data_write");
+    }
+    if (P.iverb >= 3 && (rc = final_print()) != HF_OK) return fail_lib(rc, "final_print");
+    if (itime == P.ntime) {
+      if (log) std::fclose(log);
+      log = nullptr;
+      if ((rc = final_print()) != HF_OK) return fail_lib(rc, "final_print");
+    }
+  }
+  if (log) std::fclose(log);
+  hf_destroy(ctx);
+  const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  std::printf(" time=%12.6f\n", secs);
+  std::printf(" all done\n");
+  return 0;
+}

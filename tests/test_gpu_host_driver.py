@@ -1,0 +1,48 @@
+"""The C++ host program runs the reference's test deck end to end on the GPU: ./inputs read,
+10 steps, ./outputs/TempDis.dat and TempDisTPD.dat in final_print's layout, and the sub-box log
+output_<RunName>_00 with one record after step 1 and one every write_every steps."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from heatflow_gb300 import inputs
+from heatflow_gb300.build import build_driver, build_library
+from heatflow_gb300.output import parse_records
+from heatflow_gb300.solver import HeatFlow
+
+pytestmark = pytest.mark.gpu
+
+
+def test_driver_runs_the_golden_deck(cuda_lib, golden, tmp_path):
+    build_library()
+    drv = build_driver()
+    work = tmp_path / "run"
+    (work / "inputs").mkdir(parents=True)
+    for key, name in (("param_in", "param.in"), ("mat_in", "mat.in"), ("system_in", "system.in")):
+        (work / "inputs" / name).write_text(golden[key])
+    r = subprocess.run([drv], cwd=work, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "all done" in r.stdout
+    param, prob = inputs.read_all_files(golden["param_in"], golden["mat_in"], golden["system_in"])
+    n = prob.ncells
+    T = inputs.parse_temp_file((work / "outputs" / "TempDis.dat").read_text(), n)
+    gold = np.asarray(golden["tempdis"])
+    assert np.linalg.norm(T - gold) / np.linalg.norm(gold) < 1.1e-9
+    # the same library through Python: identical fields, identical file text
+    with HeatFlow(prob, precision="fp64", criterion="recursive", tol=1e-32) as hf:
+        hf.initial_evolve()
+        states = []
+        for k in range(1, param["ntime"] + 1):
+            hf.run(k, 1)
+            states.append(hf.get_state())
+    Tp, Tpp = states[-1]
+    assert (work / "outputs" / "TempDis.dat").read_text() == inputs.format_temp_file(Tp)
+    assert (work / "outputs" / "TempDisTPD.dat").read_text() == inputs.format_temp_file(Tpp)
+    # the log: T^(n-1) after each logged step over the 25 x 25 x 1 box, at time (itime-1) dt
+    recs = parse_records((work / "outputs" / "output_IntRun_00").read_text())
+    assert len(recs) == param["ntime"]
+    for k, (t, vals) in enumerate(recs, start=1):
+        assert t == float(np.float32((k - 1) * param["time_step"]))
+        assert np.allclose(vals, states[k - 1][1], rtol=1e-15, atol=0)
