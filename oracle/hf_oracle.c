@@ -26,6 +26,9 @@
 #include "../include/heatflow_gb300.h"
 
 #define OR_TINY 1.0e-12                /* mod_constants.f90:17 */
+/* Threads of the loops that run in parallel (or_set_threads): the per-cell loops of the RHS, whose
+ * cells are independent (same bits at any thread count), and the reference's OpenMP SpMV. */
+static int g_threads = 1;
 #define OR_PI 3.141592653589793        /* mod_constants.f90:12 */
 #define OR_STEFBOLTZ 5.670373e-8       /* mod_constants.f90:16 */
 
@@ -301,11 +304,11 @@ void or_boundary(void* h, double* B) {
   if (s->cg[3]) pd[3] = s->t_bath_cg / (s->volume * (double)nx * (double)nz);
   if (s->cg[0]) pd[0] = s->t_bath_cg / (s->volume * (double)ny * (double)nz);
   if (s->cg[1]) pd[1] = s->t_bath_cg / (s->volume * (double)ny * (double)nz);
-  int64_t I = 0;
+#pragma omp parallel for collapse(2) num_threads(g_threads) schedule(static) if (g_threads > 1)
   for (int64_t iz = 1; iz <= nz; ++iz)
     for (int64_t iy = 1; iy <= ny; ++iy)
       for (int64_t ix = 1; ix <= nx; ++ix) {
-        ++I;
+        const int64_t I = ((iz - 1) * ny + (iy - 1)) * nx + ix;
         double kappa = s->kappa[I - 1], kh;
         int64_t c[3] = {ix, iy, iz}, n[3] = {nx, ny, nz};
         for (int a = 0; a < 3; ++a) {
@@ -341,6 +344,7 @@ void or_heater(void* h, int64_t itime, const double* tp, double* Q, double* Qden
   double time_pulse = (double)s->heated_steps * s->time_step;
   double heated_volume = 0.0;
   double L1 = s->len[0], L2 = s->len[1];
+#pragma omp parallel for num_threads(g_threads) schedule(static) if (g_threads > 1)
   for (int64_t ia = 0; ia < na; ++ia) {
     double power = s->power[ia];
     double tau = s->tau_s[ia] * pow(s->time_step, 2.0);
@@ -365,62 +369,80 @@ void or_heater(void* h, int64_t itime, const double* tp, double* Q, double* Qden
     }
     q = q - s->em[ia] * L1 * L2 * OR_STEFBOLTZ * (pow(tp[ia], 4.0) - pow(s->t_bath, 4.0));
     Q[ia] = q;
-    if (s->iheater[ia] > 0) heated_volume = heated_volume + s->volume;
   }
-  for (int64_t ia = 0; ia < na; ++ia) Qdens[ia] = 0.0;
-  if (s->qdens_mode == HF_QDENS_CELL_VOLUME) {
-    for (int64_t ia = 0; ia < na; ++ia) Qdens[ia] = Q[ia] / s->volume;
-  } else if (heated_volume > 0.0) {
-    for (int64_t ia = 0; ia < na; ++ia) Qdens[ia] = Q[ia] / heated_volume;
+  for (int64_t ia = 0; ia < na; ++ia)   /* in cell order, as the reference sums it */
+    if (s->iheater[ia] > 0) heated_volume = heated_volume + s->volume;
+#pragma omp parallel for num_threads(g_threads) schedule(static) if (g_threads > 1)
+  for (int64_t ia = 0; ia < na; ++ia) {
+    double qd = 0.0;
+    if (s->qdens_mode == HF_QDENS_CELL_VOLUME) qd = Q[ia] / s->volume;
+    else if (heated_volume > 0.0) qd = Q[ia] / heated_volume;
+    Qdens[ia] = qd;
   }
 }
 
 /* S_catS, mod_cattaneo.f90:23-42 */
 void or_cattaneo(void* h, const double* tp, const double* tpp, double* scat) {
   or_sys* s = (or_sys*)h;
+#pragma omp parallel for num_threads(g_threads) schedule(static) if (g_threads > 1)
   for (int64_t i = 0; i < s->na; ++i)
     scat[i] = (tpp[i] - 2.0 * tp[i]) * (s->tau_s[i] * s->rhoc[i]);
 }
 
 /* Steps 55-141 of simulate (mod_evolve.f90): B, Q, Qdens, S_CAT, S and the initial guess x.
  * Returns a HF_ENAN_* code if the reference would stop, else 0. */
+/* Any NaN in v (the reference's isnan checks of a whole vector). */
+static int any_nan(const double* v, int64_t n) {
+  int bad = 0;
+#pragma omp parallel for num_threads(g_threads) schedule(static) reduction(| : bad) if (g_threads > 1)
+  for (int64_t i = 0; i < n; ++i) bad |= isnan(v[i]) ? 1 : 0;
+  return bad;
+}
+
 int or_rhs(void* h, int64_t itime, double* B, double* Q, double* Qdens, double* scat, double* S,
            double* x) {
   or_sys* s = (or_sys*)h;
   const int64_t na = s->na;
   const double* tp = s->temp_p;
   const double* tpp = s->temp_pp;
+#pragma omp parallel for num_threads(g_threads) schedule(static) if (g_threads > 1)
   for (int64_t i = 0; i < na; ++i) { B[i] = 0; Q[i] = 0; Qdens[i] = 0; scat[i] = 0; S[i] = 0; }
   or_boundary(h, B);
-  for (int64_t i = 0; i < na; ++i) if (isnan(B[i])) return HF_ENAN_B;
+  if (any_nan(B, na)) return HF_ENAN_B;
   if (s->any_heater) {
     or_heater(h, itime, tp, Q, Qdens);
-    for (int64_t i = 0; i < na; ++i) if (isnan(Q[i])) return HF_ENAN_Q;
-    for (int64_t i = 0; i < na; ++i) if (isnan(Qdens[i])) return HF_ENAN_QDENS;
+    if (any_nan(Q, na)) return HF_ENAN_Q;
+    if (any_nan(Qdens, na)) return HF_ENAN_QDENS;
   }
   if (s->icattaneo == 1) {
     or_cattaneo(h, tp, tpp, scat);
-    for (int64_t i = 0; i < na; ++i) if (isnan(scat[i])) return HF_ENAN_SCAT;
+    if (any_nan(scat, na)) return HF_ENAN_SCAT;
   }
-  if (s->isteady == 0) {
-    for (int64_t i = 0; i < na; ++i) S[i] = -s->inverse_time * tp[i] * s->rhoc[i] - Qdens[i] - B[i];
-    if (s->icattaneo == 1)
-      for (int64_t i = 0; i < na; ++i) S[i] = S[i] + scat[i];
-  } else {
-    for (int64_t i = 0; i < na; ++i) S[i] = -Qdens[i] - B[i];
+  const int cat = s->icattaneo == 1, steady = s->isteady != 0;
+#pragma omp parallel for num_threads(g_threads) schedule(static) if (g_threads > 1)
+  for (int64_t i = 0; i < na; ++i) {
+    if (!steady) {
+      S[i] = -s->inverse_time * tp[i] * s->rhoc[i] - Qdens[i] - B[i];
+      if (cat) S[i] = S[i] + scat[i];
+    } else {
+      S[i] = -Qdens[i] - B[i];
+    }
   }
-  for (int64_t i = 0; i < na; ++i) if (isnan(S[i])) return HF_ENAN_S;
+  if (any_nan(S, na)) return HF_ENAN_S;
   int any = 0;
+#pragma omp parallel for num_threads(g_threads) schedule(static) reduction(| : any) if (g_threads > 1)
   for (int64_t i = 0; i < na; ++i) {
     x[i] = tp[i] + (tp[i] - tpp[i]);
-    if (x[i] - tp[i] < OR_TINY) any = 1;
+    if (x[i] - tp[i] < OR_TINY) any |= 1;
   }
-  if (any) for (int64_t i = 0; i < na; ++i) x[i] = x[i] + OR_TINY;
+  if (any) {
+#pragma omp parallel for num_threads(g_threads) schedule(static) if (g_threads > 1)
+    for (int64_t i = 0; i < na; ++i) x[i] = x[i] + OR_TINY;
+  }
   return 0;
 }
 
 /* ---- solver: module solver, mod_Sparse.f90 ---------------------------------------------- */
-static int g_threads = 1;
 int or_set_threads(int n) {
   g_threads = n > 0 ? n : 1;
 #ifdef _OPENMP
@@ -531,6 +553,35 @@ double or_true_relres(void* h, const double* b, const double* x) {
   for (int64_t i = 0; i < s->na; ++i) { double d = b[i] - y[i]; rr += d * d; bb += b[i] * b[i]; }
   free(y);
   return sqrt(rr) / sqrt(bb);
+}
+
+/* The operator in the geometric form: diag[I] = H_II and the stored slot coupling I with its + x/y/z
+ * neighbour (the first cell of a periodic axis for the last one), with sparse_Hmatrix's drop rule
+ * (|H| < TINY is not stored, mod_setup.f90:137); 0 where there is no such face. */
+void or_geometric(void* h, double* diag, double* cx, double* cy, double* cz) {
+  const or_sys* s = (const or_sys*)h;
+  const int64_t nx = s->nx, ny = s->ny, nz = s->nz;
+  for (int64_t l = 0; l < s->na; ++l) {
+    const int64_t I = l + 1, x = l % nx + 1, y = (l / nx) % ny + 1, z = l / (nx * ny) + 1;
+    double v;
+    diag[l] = hmatrixfunc(s, I, I);
+    v = 0.0;
+    if (x < nx) v = hmatrixfunc(s, I + 1, I);
+    else if (s->periodic[0] && nx > 1) v = hmatrixfunc(s, I, I - (nx - 1));
+    cx[l] = fabs(v) < OR_TINY ? 0.0 : v;
+    v = 0.0;
+    if (ny > 1) {
+      if (y < ny) v = hmatrixfunc(s, I + nx, I);
+      else if (s->periodic[1]) v = hmatrixfunc(s, I, I - (ny - 1) * nx);
+    }
+    cy[l] = fabs(v) < OR_TINY ? 0.0 : v;
+    v = 0.0;
+    if (nz > 1) {
+      if (z < nz) v = hmatrixfunc(s, I + nx * ny, I);
+      else if (s->periodic[2]) v = hmatrixfunc(s, I, I - (nz - 1) * nx * ny);
+    }
+    cz[l] = fabs(v) < OR_TINY ? 0.0 : v;
+  }
 }
 
 /* Jacobi-PCG on the same COO operator (the symmetric specialisation of linbcg: rr == r,

@@ -20,8 +20,8 @@ _lib = None
 
 
 def build(force: bool = False) -> str:
-    if force or not os.path.exists(LIB) or \
-            os.path.getmtime(LIB) < os.path.getmtime(os.path.join(HERE, "hf_oracle.c")):
+    srcs = [os.path.join(HERE, f) for f in ("hf_oracle.c", "cpu_pcg.c", "Makefile")]
+    if force or not os.path.exists(LIB) or any(os.path.getmtime(LIB) < os.path.getmtime(p) for p in srcs):
         subprocess.run(["make", "-s", "-C", HERE], check=True)
     return LIB
 
@@ -60,6 +60,13 @@ def lib():
                                              C.POINTER(C.c_int32)]
         L.or_set_threads.restype = C.c_int
         L.or_set_threads.argtypes = [C.c_int]
+        L.or_geometric.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
+        L.cp_create.restype = C.c_void_p
+        L.cp_create.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.c_int64,
+                                C.POINTER(C.c_int32), C.c_int]
+        L.cp_destroy.argtypes = [C.c_void_p]
+        L.cp_step.restype = C.c_int
+        L.cp_step.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_double, C.c_int64, _ip, _dp]
         _lib = L
     return _lib
 
@@ -196,3 +203,28 @@ class Oracle:
 
 def set_threads(n: int) -> int:
     return lib().or_set_threads(int(n))
+
+
+class CleanPCG:
+    """The clean CPU solver of oracle/cpu_pcg.c (a second CPU baseline, not the reference's
+    algorithm): stencil Jacobi-PCG in FP64 to a true relative residual, OpenMP, on the state of an
+    Oracle, whose RHS it uses."""
+
+    def __init__(self, oracle: "Oracle", threads: int = 0):
+        p = oracle.problem
+        self.o = oracle
+        per = (C.c_int32 * 3)(*[int(v) for v in p.periodic])
+        self.h = lib().cp_create(oracle.h, p.nx, p.ny, p.nz, per, int(threads or os.cpu_count() or 1))
+        if not self.h:
+            raise MemoryError("cp_create failed")
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().cp_destroy(self.h)
+            self.h = None
+
+    def step(self, itime: int, tol: float = 1e-10, itmax: int = 100000):
+        it = C.c_int64()
+        rel = C.c_double()
+        rc = lib().cp_step(self.h, self.o.h, int(itime), float(tol), int(itmax), C.byref(it), C.byref(rel))
+        return rc, it.value, rel.value
