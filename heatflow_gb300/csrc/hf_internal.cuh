@@ -185,6 +185,13 @@ struct DevArrays {
 // solve's last round, step end.
 enum { kStampBegin = 0, kStampRhs, kStampFin, kStampSolve, kStampSolveEnd, kStampEnd, kStamps = 8 };
 
+// Ask L2 for the line holding p (no register, no result): planes a pass streams in its next z
+// steps, so their DRAM latency overlaps the current step's work at the persistent solve's 3 blocks
+// per SM.  Only ever given addresses inside the arrays (planes the task itself reads next).
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 __device__ __forceinline__ unsigned long long gtimer() {
   unsigned long long t;
   asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));

@@ -213,6 +213,11 @@ __device__ __forceinline__ void res_hx_task(const DevArrays& A, double* part, in
 #pragma unroll 4
     for (int z = c.z0; z < c.z1; ++z) {
       const int l = base + z * nxy;
+      if (z + 4 < c.z1) {                       // four planes ahead
+        prefetch_l2(b + l + 4 * nxy);
+        prefetch_l2(yc + l + 4 * nxy);
+        prefetch_l2(yp + l + 4 * nxy);
+      }
       double a = fma(-2.0, yc[l], b[l]);
       a = a + yp[l];
       if (tiny) a = fma(-kTiny, rsum[l], a);
@@ -577,6 +582,7 @@ __device__ __forceinline__ void upd_task(const DevArrays& A, double* part, int64
 __device__ __forceinline__ bool vec4_ok(const InstDesc& d) { return (d.nx & 3) == 0; }
 
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+
 __device__ __forceinline__ void st4(float* p, const float4& v) { *reinterpret_cast<float4*>(p) = v; }
 __device__ __forceinline__ float f4(const float4& v, int i) {
   return i == 0 ? v.x : (i == 1 ? v.y : (i == 2 ? v.z : v.w));
@@ -656,6 +662,11 @@ __device__ __forceinline__ void spmv4_task(const DevArrays& A, double* part, int
         else if (d.pz) ldp(lxy, ru, pou);
       }
       axv = ld4(ax + l); ayv = ld4(ay + l); azv = ld4(az + l);
+      if (z + 1 < zb) {
+        prefetch_l2(ax + l + nxy);
+        prefetch_l2(ay + l + nxy);
+        prefetch_l2(az + l + nxy);
+      }
       if (hn) ldp(l + dn, rn, pon);
       if (hs) { ldp(l + ds, rs, pos); aysv = ld4(ay + l + ds); }
       if (wload && hw) {
