@@ -143,19 +143,7 @@ int main(int argc, char** argv) {
   const int64_t hi[3] = {P.end_ix - 1, P.end_iy - 1, P.end_iz - 1};
   const bool box = hi[0] >= lo[0] && hi[1] >= lo[1] && hi[2] >= lo[2];
   const int64_t nbox = box ? (hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1) : 0;
-  std::vector<double> boxbuf(nbox > 0 ? nbox : 1);
   FILE* log = nullptr;
-  auto log_record = [&](int64_t itime) -> int {
-    if (box) {
-      int64_t ticket = -1;
-      int r = hf_subbox_async(ctx, 0, lo, hi, 1, boxbuf.data(), &ticket);
-      if (r == HF_OK) r = hf_subbox_wait(ctx, ticket);
-      if (r != HF_OK) return r;
-    }
-    const std::string rec = hfhost::format_record((double)(itime - 1) * P.time_step, boxbuf.data(), nbox);
-    std::fwrite(rec.data(), 1, rec.size(), log);
-    return HF_OK;
-  };
   auto final_print = [&]() -> int {
     int r = hf_get_state(ctx, tp.data(), tpp.data());
     if (r != HF_OK) return r;
@@ -166,35 +154,87 @@ int main(int argc, char** argv) {
     }
     return HF_OK;
   };
+  // data_write logs after step 1 and, with _WriteToTxt, every write_every steps (not in test runs)
+  auto logs_after = [&](int64_t it) {
+    if (P.test_run) return false;
+    if (it == 1) return true;
+    return P.write_to_txt && P.write_every > 0 && it % P.write_every == 0;
+  };
+  // Log records in flight: the sub-box is gathered on the device after the step and copied to a
+  // page-locked buffer on the library's second stream while the next steps run; records are
+  // written in order once their copy is done (at most kInFlight at a time).
+  constexpr int kInFlight = 3;
+  struct Pending {
+    int64_t itime = 0, ticket = -1;
+    int slot = 0;
+  };
+  std::vector<std::vector<double>> ring(kInFlight + 1, std::vector<double>(nbox > 0 ? nbox : 1));
+  for (auto& b : ring) hf_host_register(b.data(), b.size() * sizeof(double));   // best effort
+  std::vector<Pending> pending;
+  int next_slot = 0;
+  auto drain = [&](size_t keep) -> int {
+    while (pending.size() > keep) {
+      const Pending p = pending.front();
+      pending.erase(pending.begin());
+      if (box) {
+        const int r = hf_subbox_wait(ctx, p.ticket);
+        if (r != HF_OK) return r;
+      }
+      const std::string rec = hfhost::format_record((double)(p.itime - 1) * P.time_step,
+                                                    ring[p.slot].data(), nbox);
+      std::fwrite(rec.data(), 1, rec.size(), log);
+    }
+    return HF_OK;
+  };
+  auto cleanup = [&]() {
+    for (auto& b : ring) hf_host_unregister(b.data());
+    if (log) std::fclose(log);
+    log = nullptr;
+  };
 
-  for (int64_t itime = 1; itime <= P.ntime; ++itime) {
+  // The steps between two host actions (a log record, a per-step print at IVERB >= 3, the end)
+  // run as one hf_run call: the whole loop as one CUDA graph launch.
+  int64_t itime = 1;
+  while (itime <= P.ntime) {
+    int64_t last = itime;
+    while (last < P.ntime && !logs_after(last) && P.iverb < 3) ++last;
     hf_stats st;
-    rc = hf_step(ctx, itime, &st);
+    rc = hf_run(ctx, itime, last - itime + 1, &st);
     if (rc != HF_OK) {
-      fail_lib(rc, "hf_step");
+      fail_lib(rc, "simulate");
+      cleanup();
       hf_destroy(ctx);
       return 1;
     }
-    // data_write (mod_output.f90:57-146)
-    if (itime == 1 && !P.test_run) {
-      log = std::fopen(hfhost::next_log_name(opt.outputs, P.run_name).c_str(), "w");
-      if (!log) {
-        std::fprintf(stderr, "cannot open the log in %s\n", opt.outputs.c_str());
-        hf_destroy(ctx);
-        return 1;
+    if (logs_after(last)) {
+      if (last == 1) {
+        log = std::fopen(hfhost::next_log_name(opt.outputs, P.run_name).c_str(), "w");
+        if (!log) {
+          std::fprintf(stderr, "cannot open the log in %s\n", opt.outputs.c_str());
+          cleanup();
+          hf_destroy(ctx);
+          return 1;
+        }
       }
-      if ((rc = log_record(itime)) != HF_OK) return fail_lib(rc, "data_write");
-    } else if (!P.test_run && P.write_to_txt && P.write_every > 0 && itime % P.write_every == 0) {
-      if ((rc = log_record(itime)) != HF_OK) return fail_lib(rc, "data_write");
+      Pending p;
+      p.itime = last;
+      p.slot = next_slot;
+      next_slot = (next_slot + 1) % (kInFlight + 1);
+      if (box && (rc = hf_subbox_async(ctx, 0, lo, hi, 1, ring[p.slot].data(), &p.ticket)) != HF_OK)
+        return fail_lib(rc, "data_write");
+      pending.push_back(p);
+      if ((rc = drain(kInFlight - 1)) != HF_OK) return fail_lib(rc, "data_write");
     }
     if (P.iverb >= 3 && (rc = final_print()) != HF_OK) return fail_lib(rc, "final_print");
-    if (itime == P.ntime) {
+    if (last == P.ntime) {
+      if ((rc = drain(0)) != HF_OK) return fail_lib(rc, "data_write");
       if (log) std::fclose(log);
       log = nullptr;
       if ((rc = final_print()) != HF_OK) return fail_lib(rc, "final_print");
     }
+    itime = last + 1;
   }
-  if (log) std::fclose(log);
+  cleanup();
   hf_destroy(ctx);
   const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   std::printf(" time=%12.6f\n", secs);

@@ -46,3 +46,35 @@ def test_driver_runs_the_golden_deck(cuda_lib, golden, tmp_path):
     for k, (t, vals) in enumerate(recs, start=1):
         assert t == float(np.float32((k - 1) * param["time_step"]))
         assert np.allclose(vals, states[k - 1][1], rtol=1e-15, atol=0)
+
+
+def test_driver_chunks_steps_between_records(cuda_lib, golden, tmp_path):
+    """IVERB 1 and write_every 3: the program runs the steps between records as whole-loop graph
+    launches and copies the records while the next steps run; the records (after steps 1, 3, 6,
+    9) and the final fields are those of the per-step path."""
+    build_library()
+    drv = build_driver()
+    param_in = golden["param_in"].replace("IVERB = 6", "IVERB = 1").replace(
+        "write_every = 1", "write_every = 3")
+    work = tmp_path / "run"
+    (work / "inputs").mkdir(parents=True)
+    (work / "inputs" / "param.in").write_text(param_in)
+    (work / "inputs" / "mat.in").write_text(golden["mat_in"])
+    (work / "inputs" / "system.in").write_text(golden["system_in"])
+    r = subprocess.run([drv], cwd=work, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    param, prob = inputs.read_all_files(param_in, golden["mat_in"], golden["system_in"])
+    assert param["write_every"] == 3 and param["IVERB"] == 1
+    with HeatFlow(prob, precision="fp64", criterion="recursive", tol=1e-32) as hf:
+        hf.initial_evolve()
+        states = []
+        for k in range(1, param["ntime"] + 1):
+            hf.run(k, 1)
+            states.append(hf.get_state())
+    recs = parse_records((work / "outputs" / "output_IntRun_00").read_text())
+    marks = [1, 3, 6, 9]
+    assert len(recs) == len(marks)
+    for (t, vals), k in zip(recs, marks):
+        assert t == float(np.float32((k - 1) * param["time_step"]))
+        assert np.array_equal(vals, states[k - 1][1])
+    assert (work / "outputs" / "TempDis.dat").read_text() == inputs.format_temp_file(states[-1][0])
