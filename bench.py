@@ -80,28 +80,70 @@ PHASE_BYTES = {
 }
 
 
-def solve_bytes_per_cell(rounds, precision):
-    """Algorithmic bytes per cell of one persistent-solve launch from its round phases."""
+def round_bytes_per_cell(rounds, precision):
+    """Algorithmic bytes per cell of each round of one persistent-solve launch (its round log)."""
     table = PHASE_BYTES[precision]
-    total, first_cg, first_b, have_y = 0, True, True, False
+    out, first_cg, first_b, have_y = [], True, True, False
     for ph, _ in rounds:
         full, alt = table.get(ph, (0, 0))
+        b = 0
         if ph in ("res_init", "res_init_hx", "res"):
-            total += full
+            b = full
             first_cg = first_b = True
             have_y = False
         elif ph in ("cg_pq", "cg_p"):
-            total += alt if first_cg else full
+            b = alt if first_cg else full
             first_cg = False
         elif ph == "cg_q":
-            total += full
+            b = full
         elif ph == "cg_b":
-            total += alt if first_b else full
+            b = alt if first_b else full
             first_b = False
             have_y = True
         elif ph == "xupd":
-            total += full if have_y else alt
-    return total
+            b = full if have_y else alt
+        out.append(b)
+    return out
+
+
+def solve_bytes_per_cell(rounds, precision):
+    """Algorithmic bytes per cell of one persistent-solve launch from its round phases."""
+    return sum(round_bytes_per_cell(rounds, precision))
+
+
+# FP64 instructions per cell of each round (the rest of the work is FP32/integer): the mixed
+# path's residual sweep 7 FMA + 1 sub (||r||^2 in FP32), its pointwise first residual 1 FMA + 1 add
+# + 1 FMA (TINY) + 1 FMA (||r||^2), the stencil first residual 7 + 1 + 1 FMA, the x update 1 add.
+PHASE_FP64_INSTR = {
+    "mixed": {"res_init_hx": 4, "res_init": 9, "res": 8, "xupd": 1},
+    "fp64": {"res_init_hx": 6, "res_init": 11, "res": 10, "xupd": 1, "cg_p": 1, "cg_q": 8,
+             "cg_b": 4},
+}
+
+
+def solve_floor(rounds, precision, N, hbm_gbs, fp64_tflops):
+    """Each round's floor is the larger of its algorithmic bytes at the measured HBM rate and its
+    FP64 instructions at the measured FP64 issue rate (an FMA's 2 flops per instruction); the
+    launch's floor is their sum, compared with the rounds' measured times (round log)."""
+    instr_rate = fp64_tflops * 1e12 / 2.0
+    table = PHASE_FP64_INSTR[precision]
+    by = {}
+    floor = actual = 0.0
+    for (ph, us), b in zip(rounds, round_bytes_per_cell(rounds, precision)):
+        t_mem = b * N / (hbm_gbs * 1e9) * 1e6
+        t_fp64 = table.get(ph, 0) * N / instr_rate * 1e6
+        f = max(t_mem, t_fp64)
+        floor += f
+        actual += us
+        e = by.setdefault(ph, {"floor_us": 0.0, "us": 0.0, "bound": "fp64" if t_fp64 > t_mem else "hbm"})
+        e["floor_us"] += f
+        e["us"] += us
+    for e in by.values():
+        e["frac"] = e["floor_us"] / e["us"] if e["us"] else None
+    return {"floor_us": floor, "us": actual, "frac": floor / actual if actual else None,
+            "by_phase": by,
+            "note": "per round max(algorithmic bytes / measured HBM, FP64 instructions / measured "
+                    "FP64 rate), summed over the launch's rounds"}
 
 
 def parse():
@@ -483,6 +525,7 @@ def main():
                 "note": "phases' GB/s_upper assume every round of that phase moved its full bytes; "
                         "standalone kernels are timed repeatedly on the same data (partly L2-resident)"}
     if fp_rates:
+        roofline["combined"] = solve_floor(rounds, prec, N, peak, fp_rates["fp64_tflops"])
         roofline["fp64"] = {
             k: {"achieved_tflops": FP64_FLOPS_PER_CELL[k] * N / (kms[k] / 1000.0) / 1e12,
                 "peak_tflops": fp_rates["fp64_tflops"],
