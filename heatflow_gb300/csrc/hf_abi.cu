@@ -1274,7 +1274,7 @@ int hf_autotune(hf_ctx* h, int64_t itime0, int32_t steps, hf_tune_result* result
   if (rc) { cudaFree(sn.t); return rc; }
   const hf_solver_opts base = c.opts;
   const bool mixed = base.precision == HF_PREC_MIXED;
-  const int depths[3] = {8, 16, 32};
+  const int depths[4] = {8, 16, 32, 64};
   const double tols[3] = {1e-4, 1e-5, 1e-6};
   const int ntol = mixed ? 3 : 1;
   std::vector<hf_tune_result> all;
@@ -1287,7 +1287,7 @@ int hf_autotune(hf_ctx* h, int64_t itime0, int32_t steps, hf_tune_result* result
   };
   if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
     return finish(set_err(HF_ECUDA, "cudaEventCreate failed"));
-  for (int di = 0; di < 3; ++di) {
+  for (int di = 0; di < 4; ++di) {
     for (int ti = 0; ti < ntol; ++ti) {
       hf_solver_opts o = base;
       o.task_depth = depths[di];

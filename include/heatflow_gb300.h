@@ -308,7 +308,7 @@ int hf_check_barrier_timeout(hf_ctx* ctx, int32_t wait_ms, int32_t* status, doub
 
 /* ---- autotuner ------------------------------------------------------------------------------
  * No counterpart in the reference.  Chooses the stencil task shape (z-planes per 32 x 8 column
- * tile: 8, 16 or 32) and, on the mixed path, the inner FP32 tolerance (1e-4, 1e-5, 1e-6) for this
+ * tile: 8, 16, 32 or 64) and, on the mixed path, the inner FP32 tolerance (1e-4, 1e-5, 1e-6) for this
  * context's own grids: for every candidate it restores the current state, runs one untimed step
  * and then `steps` steps from step `itime0` timed with CUDA events through the context's step loop
  * (use_graph as set), and keeps the fastest.  On return the options hold the choice and the state,

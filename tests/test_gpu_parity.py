@@ -315,7 +315,7 @@ def test_autotune_leaves_state_and_picks_a_candidate(cuda_lib, precision):
         hf.run(1, 2)
         before = hf.get_state()
         res = hf.autotune(itime0=3, steps=2)
-        assert len(res) == (9 if precision == "mixed" else 3)
+        assert len(res) == (12 if precision == "mixed" else 4)
         assert sum(r["chosen"] for r in res) == 1 and all(r["ms_per_step"] > 0 for r in res)
         best = next(r for r in res if r["chosen"])
         after = hf.get_state()
