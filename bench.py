@@ -272,19 +272,22 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sms)}
 
 
-def cpu_baseline(prob, steps_cap: int, seconds: float, tol: float):
+def cpu_baseline(prob, steps_cap: int, seconds: float, tol: float, warm: int = 0):
     """The oracle port of the reference's step (COO H, Jacobi BiCG with the reference's itol=1
     criterion at `tol`, OpenMP-atomic SpMV as in the reference's Parallel build) on all host
-    cores.  Times whole steps until `steps_cap` steps or `seconds` elapse."""
+    cores.  Runs `warm` untimed steps, then times whole steps until `steps_cap` steps or `seconds`
+    elapse."""
     from oracle.oracle import Oracle, set_threads
     cores = os.cpu_count() or 1
     set_threads(cores)
     o = Oracle(prob)
     o.set_state(*prob.initial_state())
+    for k in range(warm):
+        o.simulate(k + 1, mode=0, tol=tol, itmax=50000)
     times, iters = [], []
     t_all = time.perf_counter()
-    k = 0
-    while k < steps_cap:
+    k = warm
+    while k < warm + steps_cap:
         t0 = time.perf_counter()
         rc, it, _ = o.simulate(k + 1, mode=0, tol=tol, itmax=50000)
         times.append(time.perf_counter() - t0)
@@ -333,11 +336,11 @@ def run_reference(args, rank, world):
         return 0
     from heatflow_gb300.problem import layered_slab
     prob = layered_slab(args.n, icattaneo=0 if args.fourier else 1)
-    warm = 0 if args.warmup < 1 else 1
-    cb = cpu_baseline(prob, args.steps + warm, args.cpu_seconds, args.tol)
+    warm = max(args.warmup, 0)
+    cb = cpu_baseline(prob, max(args.steps, 1), args.cpu_seconds, args.tol, warm=warm)
     line = {
         "metric": METRIC, "value": cb["value"], "unit": UNIT, "impl": "reference",
-        "n_gpus": world, "steps": cb["steps_timed"], "warmup": 0,
+        "n_gpus": world, "steps": cb["steps_timed"], "warmup": warm,
         "ms_per_step": cb["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": workload_config(args, prob),
