@@ -289,6 +289,15 @@ __device__ __forceinline__ void res_task(const DevArrays& A, double* part, int64
     double cxc = 0.0, a = 0.0, bl = 0.0, xwl = 0.0, cxwl = 0.0, xel = 0.0;
     double cyn = 0.0, xyn = 0.0, cys = 0.0, xys = 0.0, czc = 0.0;
     if (act) {
+      if (z + 2 < c.z1) {                    // the plane after next: x, diag, b, cx, cy, cz
+        const int lp = l + 2 * nxy;
+        prefetch_l2(X + lp);
+        prefetch_l2(diag + lp);
+        prefetch_l2(b + lp);
+        prefetch_l2(cx + lp);
+        prefetch_l2(cy + lp);
+        prefetch_l2(cz + lp);
+      }
       cxc = cx[l];
       bl = b[l];
       a = fma(-diag[l], xc, bl);
