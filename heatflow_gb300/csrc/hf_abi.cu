@@ -566,6 +566,8 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
     if (p.nx < 1 || p.ny < 1 || p.nz < 1) return set_err(HF_EARG, "grid dimensions must be >= 1");
     const int64_t n = p.nx * p.ny * p.nz;
     if (n >= (int64_t(1) << 31)) return set_err(HF_EARG, "more than 2^31-1 cells in one grid");
+    if ((p.nx + 3) / 4 * 4 * p.ny * p.nz >= (int64_t(1) << 31))
+      return set_err(HF_EARG, "more than 2^31-1 cells in one grid with rows padded to 4 cells");
     if (p.nx == 1 && n > 1)
       return set_err(HF_EARG, "nx = 1 with more than one cell: the reference's COO assembly "
                               "(sparse_Hmatrix) writes past its capacity for such grids");
@@ -584,7 +586,7 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
   c.own_stream = true;
   c.ninst = count;
   // ---- layout: instances at multiples of kTile cells
-  int64_t off = 0, tiles = 0, hoff = 0;
+  int64_t off = 0, tiles = 0, hoff = 0, off4 = 0;
   std::vector<int32_t> tile_inst;
   c.h_inst.resize(count);
   c.h_bc.resize(count);
@@ -597,6 +599,10 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
     d.off = off;
     d.hoff = hoff;
     hoff += d.n;
+    d.sx = (int32_t)((p.nx + 3) / 4 * 4);
+    d.off4 = off4;
+    const int64_t n4 = (int64_t)d.sx * p.ny * p.nz;
+    off4 += (n4 + kTile - 1) / kTile * kTile;
     d.tile0 = tiles;
     d.ntiles = (int32_t)((d.n + kTile - 1) / kTile);
     for (int t = 0; t < d.ntiles; ++t) tile_inst.push_back((int32_t)i);
@@ -661,6 +667,7 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
   }
   c.ntasks = c.ntasks_cap;
   const size_t N = (size_t)c.ncells;
+  const size_t N4 = (size_t)off4;   // cells of the FP32 inner-solve layout
   // ---- device memory
   DevArrays& A = c.A;
   std::memset(&A, 0, sizeof(A));
@@ -686,7 +693,7 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
   ALLOC(A.diag, N); ALLOC(A.cx, N); ALLOC(A.cy, N); ALLOC(A.cz, N); ALLOC(A.sinv, N);
   ALLOC(A.rsum, N); ALLOC(A.sinv32, N);
   ALLOC(A.a64x, N); ALLOC(A.a64y, N); ALLOC(A.a64z, N);
-  ALLOC(A.a32x, N); ALLOC(A.a32y, N); ALLOC(A.a32z, N);
+  ALLOC(A.a32x, N4); ALLOC(A.a32y, N4); ALLOC(A.a32z, N4);
   ALLOC(A.rhoc, N); ALLOC(A.ccat, N); ALLOC(A.bvec, N); ALLOC(A.tau_s, N);
   ALLOC(c.asm_.kappa, N);
   if (c.any_power) ALLOC(A.power, N);
@@ -696,7 +703,7 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
   ALLOC(A.hx[0], N); ALLOC(A.hx[1], N);
   ALLOC(A.stamps, (size_t)kStamps);
   ALLOC(A.b, N); ALLOC(A.y, N); ALLOC(A.r, N); ALLOC(A.p, N); ALLOC(A.q, N); ALLOC(A.p2, N);
-  ALLOC(A.y32, N); ALLOC(A.r32, N); ALLOC(A.p32, N); ALLOC(A.q32, N); ALLOC(A.p232, N);
+  ALLOC(A.y32, N4); ALLOC(A.r32, N4); ALLOC(A.p32, N4); ALLOC(A.q32, N4); ALLOC(A.p232, N4);
   double *d_rho, *d_hc, *d_tau, *d_em = nullptr;
   ALLOC(d_rho, N); ALLOC(d_hc, N); ALLOC(d_tau, N);
   if (c.any_em) ALLOC(d_em, N);
@@ -716,9 +723,11 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
                   (void*)A.b, (void*)A.y, (void*)A.r, (void*)A.p, (void*)A.q, (void*)A.rsum,
                   (void*)A.p2, (void*)A.hx[0], (void*)A.hx[1]})
     CK(cudaMemsetAsync(p, 0, N * sizeof(double), c.stream));
+  // the padding cells of the FP32 layout stay zero: no kernel writes them anything else
   for (void* p : {(void*)A.a32x, (void*)A.a32y, (void*)A.a32z, (void*)A.y32, (void*)A.r32,
-                  (void*)A.p32, (void*)A.q32, (void*)A.sinv32, (void*)A.p232})
-    CK(cudaMemsetAsync(p, 0, N * sizeof(float), c.stream));
+                  (void*)A.p32, (void*)A.q32, (void*)A.p232})
+    CK(cudaMemsetAsync(p, 0, N4 * sizeof(float), c.stream));
+  CK(cudaMemsetAsync(A.sinv32, 0, N * sizeof(float), c.stream));
   for (int k = 0; k < 4; ++k) CK(cudaMemsetAsync(A.tbuf[k], 0, N * sizeof(double), c.stream));
   if (d_em) CK(cudaMemsetAsync(d_em, 0, N * sizeof(double), c.stream));
   if (A.power) CK(cudaMemsetAsync(A.power, 0, N * sizeof(double), c.stream));

@@ -344,7 +344,8 @@ __global__ void k_scale(DevArrays A) {
   double ay = -A.cy[g] * si * A.sinv[ey];
   double az = -A.cz[g] * si * A.sinv[ez];
   A.a64x[g] = ax; A.a64y[g] = ay; A.a64z[g] = az;
-  A.a32x[g] = (float)ax; A.a32y[g] = (float)ay; A.a32z[g] = (float)az;
+  const int64_t g4 = d.off4 + (z * ny + y) * d.sx + x;   // the FP32 layout (rows of sx cells)
+  A.a32x[g4] = (float)ax; A.a32y[g4] = (float)ay; A.a32z[g4] = (float)az;
   // H*1: the diagonal plus every face of the row
   double rs = A.diag[g];
   if (nx > 1 && (x + 1 < nx || d.px)) rs += A.cx[g];

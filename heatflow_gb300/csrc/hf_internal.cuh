@@ -61,6 +61,12 @@ struct InstDesc {
   int32_t ntask;      // tasks of this instance
   int32_t zc;         // planes per task (the task depth)
   int64_t hoff;       // first cell in the compact host layout (instances back to back, no padding)
+  // The FP32 vectors of the inner solve (a32x/y/z, y32, r32, p32, p232, q32) use their own layout:
+  // rows of sx = nx rounded up to 4 cells (the padding cells hold zeros), so every grid takes the
+  // 16-byte vector passes; instance at off4, a multiple of kTile cells.  sx = nx: the FP64 layout.
+  int64_t off4;
+  int32_t sx;
+  int32_t pad4;
 };
 
 // Per-instance mutable scalars (device memory).
@@ -368,9 +374,12 @@ struct TCell {
   int nx, ny, nz, nxy;
   bool px, py, pz;
   int x0, y, z0, z1, lane;
+  int64_t off4;       // the FP32 vectors' layout (rows of sx cells)
+  int sx, nxy4;
   __device__ int x(int j) const { return x0 + 32 * j + lane; }
   __device__ bool act(int j) const { return x(j) < nx && y < ny; }   // column inside the grid
   __device__ int base(int j) const { return y * nx + x(j); }          // local index of (x, y, 0)
+  __device__ int base4(int j) const { return y * sx + x(j); }         // the same in the FP32 layout
 };
 __device__ __forceinline__ TCell task_cell(const DevArrays& A, int64_t task) {
   const int4 t = A.tasks[task];
@@ -385,6 +394,9 @@ __device__ __forceinline__ TCell task_cell(const DevArrays& A, int64_t task) {
   c.y = t.z + (int)(threadIdx.x >> 5);
   c.z0 = t.w;
   c.z1 = min(t.w + d.zc, d.nz);
+  c.off4 = d.off4;
+  c.sx = d.sx;
+  c.nxy4 = d.sx * d.ny;
   return c;
 }
 

@@ -203,16 +203,18 @@ __device__ __forceinline__ void res_hx_task(const DevArrays& A, double* part, in
   const double* __restrict__ rsum = A.rsum + off;
   const float* __restrict__ sinv32 = A.sinv32 + off;
   const double* __restrict__ sinv = A.sinv + off;
-  TR* R = Vec<TR>::r(A) + off;
+  const bool f32 = sizeof(TR) == 4;           // FP32 g goes into the FP32 layout
+  TR* R = Vec<TR>::r(A) + (f32 ? c.off4 : off);
   const float isig = (float)(1.0 / s.sigma);
   const bool tiny = s.x0flag != 0;            // the residual of x0 + TINY: r(x0) - TINY * H1
   double rr = 0.0, gg64 = 0.0;
   float gg = 0.f;
   if (c.act(0)) {
     const int nxy = c.nxy, base = c.base(0);
+    const int rxy = f32 ? c.nxy4 : nxy, rbase = f32 ? c.base4(0) : base;
 #pragma unroll 4
     for (int z = c.z0; z < c.z1; ++z) {
-      const int l = base + z * nxy;
+      const int l = base + z * nxy, lr = rbase + z * rxy;
       if (z + 4 < c.z1) {                       // four planes ahead
         prefetch_l2(b + l + 4 * nxy);
         prefetch_l2(yc + l + 4 * nxy);
@@ -224,11 +226,11 @@ __device__ __forceinline__ void res_hx_task(const DevArrays& A, double* part, in
       rr = fma(a, a, rr);
       if (sizeof(TR) == 4) {
         const float g = -sinv32[l] * f64_to_f32_trunc(a) * isig;
-        R[l] = (TR)g;
+        R[lr] = (TR)g;
         gg = fmaf(g, g, gg);
       } else {
         const double g = -sinv[l] * a;
-        R[l] = (TR)g;
+        R[lr] = (TR)g;
         gg64 = fma(g, g, gg64);
       }
     }
@@ -265,7 +267,9 @@ __device__ __forceinline__ void res_task(const DevArrays& A, double* part, int64
   const double* __restrict__ rsum = A.rsum + off;
   const float* __restrict__ sinv32 = A.sinv32 + off;
   const double* __restrict__ sinv = A.sinv + off;
-  TR* R = Vec<TR>::r(A) + off;
+  const bool f32 = sizeof(TR) == 4;           // FP32 g goes into the FP32 layout
+  TR* R = Vec<TR>::r(A) + (f32 ? c.off4 : off);
+  const int rxy = f32 ? c.nxy4 : c.nxy, rbase = f32 ? c.base4(0) : c.base(0);
   double* HX = A.hx[1 - s.hx_role] + off;
   const float isig = (float)(1.0 / s.sigma);
   // mixed, after an update: ||r||^2 summed in FP32 over per-thread scaled r (one FP64 instruction
@@ -326,11 +330,11 @@ __device__ __forceinline__ void res_task(const DevArrays& A, double* part, int64
       if (!INIT) HX[l] = bl - a;
       if (sizeof(TR) == 4) {             // mixed: g in FP32, scaled by 1/sigma
         const float g = -sinv32[l] * f64_to_f32_trunc(a) * isig;
-        R[l] = (TR)g;
+        R[rbase + z * rxy] = (TR)g;
         gg = fmaf(g, g, gg);
       } else {                           // FP64 path: sigma = 1
         const double g = -sinv[l] * a;
-        R[l] = (TR)g;
+        R[rbase + z * rxy] = (TR)g;
         gg64 = fma(g, g, gg64);
       }
     }
@@ -358,13 +362,15 @@ __device__ __forceinline__ void xupd_task(const DevArrays& A, double* part, int6
   const int64_t off = c.off;
   const double* XR = A.tbuf[s.role[2]] + off;
   double* XW = A.tbuf[s.role[3]] + off;
-  const TY* Y = Vec<TY>::y(A) + off;
+  const bool f32 = sizeof(TY) == 4;           // FP32 y is read from the FP32 layout
+  const TY* Y = Vec<TY>::y(A) + (f32 ? c.off4 : off);
   const double* __restrict__ sinv = A.sinv + off;
   const float* __restrict__ sinv32 = A.sinv32 + off;
   const bool use_y = s.iter > 0;
   const bool tiny = s.tiny_pending != 0;
   const float sig = (float)s.sigma_prev;
   const int nxy = c.nxy, base = c.base(0);
+  const int yxy = f32 ? c.nxy4 : nxy, ybase = f32 ? c.base4(0) : base;
   for (int z0 = c.z0; z0 < c.z1; z0 += 4) {
     double xv[4], sv[4];
     float sv32[4];
@@ -376,7 +382,7 @@ __device__ __forceinline__ void xupd_task(const DevArrays& A, double* part, int6
       if (z0 + u < c.z1) {
         xv[u] = XR[l];
         if (use_y) {
-          yv[u] = Y[l];
+          yv[u] = Y[ybase + (z0 + u) * yxy];
           if (sizeof(TY) == 8) sv[u] = sinv[l];
           else sv32[u] = sinv32[l];
         }
@@ -577,9 +583,11 @@ __device__ __forceinline__ void upd_task(const DevArrays& A, double* part, int64
 }
 
 // ---- FP32 p + SpMV on 16-byte vectors ---------------------------------------------------------
-// For grids whose rows hold a multiple of 4 cells (every row then starts 16-byte aligned; the
-// instances start at multiples of 1024 cells) each thread owns 4 consecutive x cells and works on
-// float4 vectors: a quarter of the scalar version's instructions per cell.  Block layout over a
+// The FP32 vectors have rows of sx = nx rounded up to 4 cells (every row starts 16-byte aligned;
+// the instances start at multiples of 1024 cells), so each thread owns 4 consecutive x cells and
+// works on float4 vectors: a quarter of the scalar version's instructions per cell.  In a row's
+// last quad the cells past nx are padding: their coefficients and p are zero, q is kept zero, and
+// the last grid cell takes its east neighbour from a load (the periodic wrap) or has none.  Block layout over a
 // 32 x 8 column tile: four z-groups of 64 threads, each marching its quarter of the task's planes;
 // in a group, thread w owns row w / 8 and cells x0 + 4 (w % 8) .. + 3, so a warp holds 4 rows of
 // 8 quads and the x neighbours across quads are shuffles.  Per plane a thread issues its ten
@@ -602,14 +610,15 @@ __device__ __forceinline__ void spmv4_task(const DevArrays& A, double* part, int
                                            const InstScal& s) {
   const int4 tk = A.tasks[task];
   const InstDesc& d = A.inst[tk.x];
-  const int nx = d.nx, ny = d.ny, nz = d.nz, nxy = nx * ny;
-  const int64_t off = d.off;
+  const int nx = d.nx, ny = d.ny, nz = d.nz, sx = d.sx, nxy = sx * ny;
+  const int64_t off = d.off4;
   const int tid = threadIdx.x, grp = tid >> 6, w = tid & 63, row = w >> 3, q = w & 7;
   const int x = tk.y + 4 * q, y = tk.z + row;
   const int z0 = tk.w, z1 = min(z0 + d.zc, nz);
   const int per = (z1 - z0 + 3) >> 2;
   const int za = min(z0 + grp * per, z1), zb = min(za + per, z1);
   const bool act = x < nx && y < ny;
+  const int last = min(3, nx - 1 - x);   // the quad's last grid cell; cells past it are padding
   const int64_t k = s.iter;
   const bool first = !FUSED || k == 0;
   const float beta = (float)s.beta;
@@ -625,15 +634,15 @@ __device__ __forceinline__ void spmv4_task(const DevArrays& A, double* part, int
   bool hn = false, hs = false;
   int dn = 0, ds = 0;
   if (ny > 1) {
-    if (y + 1 < ny) { dn = nx; hn = true; } else if (d.py) { dn = -(ny - 1) * nx; hn = true; }
-    if (y > 0) { ds = -nx; hs = true; } else if (d.py) { ds = (ny - 1) * nx; hs = true; }
+    if (y + 1 < ny) { dn = sx; hn = true; } else if (d.py) { dn = -(ny - 1) * sx; hn = true; }
+    if (y > 0) { ds = -sx; hs = true; } else if (d.py) { ds = (ny - 1) * sx; hs = true; }
   }
   const bool wload = (q == 0 || x == 0);          // west of cell 0 is loaded, not shuffled
-  const bool eload = (q == 7 || x + 4 == nx);     // east of cell 3 is loaded, not shuffled
+  const bool eload = (q == 7 || x + 4 >= nx);     // east of the last cell is loaded, not shuffled
   bool hw = false, he = false;
   int dw = 0, de = 0;
   if (x > 0) { dw = -1; hw = true; } else if (d.px && nx > 1) { dw = nx - 1; hw = true; }
-  if (x + 4 < nx) { de = 4; he = true; } else if (d.px && nx > 1) { de = 4 - nx; he = true; }
+  if (x + 4 < nx) { de = 4; he = true; } else if (d.px && nx > 1) { de = -x; he = true; }
   auto pv = [&](float a, float b) -> float { return first ? a : fmaf(beta, b, a); };
   auto pv4 = [&](const float4& a, const float4& b) -> float4 {
     return make_float4(pv(a.x, b.x), pv(a.y, b.y), pv(a.z, b.z), pv(a.w, b.w));
@@ -642,7 +651,7 @@ __device__ __forceinline__ void spmv4_task(const DevArrays& A, double* part, int
     r = ld4(Src + l);
     po = first ? zero4 : ld4(Po + l);
   };
-  const int lxy = y * nx + x;
+  const int lxy = y * sx + x;
   // plane below the group (za - 1, or the periodic wrap to nz - 1), and the group's first plane
   float4 pm = zero4, azm = zero4, rc = zero4, poc = zero4;
   if (act && za < zb) {
@@ -701,7 +710,7 @@ __device__ __forceinline__ void spmv4_task(const DevArrays& A, double* part, int
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
         const float pc = f4(p, i);
-        const float pe = i < 3 ? f4(p, i + 1) : pe3;
+        const float pe = i < last ? f4(p, i + 1) : pe3;
         const float pw = i > 0 ? f4(p, i - 1) : pw0;
         const float axw = i > 0 ? f4(axv, i - 1) : axw0;
         float acc = pc;
@@ -715,6 +724,7 @@ __device__ __forceinline__ void spmv4_task(const DevArrays& A, double* part, int
           acc = fmaf(f4(azv, i), f4(pu, i), acc);
           acc = fmaf(f4(azm, i), f4(pm, i), acc);
         }
+        if (i > last) acc = 0.f;       // padding: q stays 0 (its p is 0)
         pq = fmaf(pc, acc, pq);
         if (i == 0) qv.x = acc; else if (i == 1) qv.y = acc; else if (i == 2) qv.z = acc; else qv.w = acc;
       }
@@ -750,11 +760,15 @@ __device__ __forceinline__ void stv4(double* p, const V4<double>& v) {
   reinterpret_cast<double2*>(p)[1] = make_double2(v.v[2], v.v[3]);
 }
 
+// A thread's quad.  F32: the pass's vectors are FP32 and live in the FP32 layout (rows of sx
+// cells; voff, nxy, lxy index them); FP64 arrays beside them use the FP64 layout (off, dxy, dlxy).
+// For FP64 vectors (F32 false) both are the FP64 layout.
 struct Quad {
-  int64_t off;
-  int nxy, lxy, za, zb;
-  bool act;
+  int64_t off, voff;
+  int nxy, lxy, dxy, dlxy, za, zb, nx, x;
+  bool act, padded;
 };
+template <bool F32>
 __device__ __forceinline__ Quad quad_cell(const DevArrays& A, int64_t task) {
   const int4 tk = A.tasks[task];
   const InstDesc& d = A.inst[tk.x];
@@ -762,27 +776,45 @@ __device__ __forceinline__ Quad quad_cell(const DevArrays& A, int64_t task) {
   const int x = tk.y + 4 * (w & 7), y = tk.z + (w >> 3);
   const int z1 = min(tk.w + d.zc, d.nz);
   const int per = (z1 - tk.w + 3) >> 2;
+  const int sx = F32 ? d.sx : d.nx;
   Quad c;
   c.off = d.off;
-  c.nxy = d.nx * d.ny;
-  c.lxy = y * d.nx + x;
+  c.voff = F32 ? d.off4 : d.off;
+  c.nxy = sx * d.ny;
+  c.lxy = y * sx + x;
+  c.dxy = d.nx * d.ny;
+  c.dlxy = y * d.nx + x;
+  c.nx = d.nx;
+  c.x = x;
+  c.padded = sx != d.nx;
   c.za = min(tk.w + grp * per, z1);
   c.zb = min(c.za + per, z1);
   c.act = x < d.nx && y < d.ny;
   return c;
 }
 
+// The FP64-layout diagonal of a quad's cells (zeros for padding cells).
+__device__ __forceinline__ V4<double> diag4(const double* __restrict__ diag, const Quad& c, int z) {
+  const int l = c.dlxy + z * c.dxy;
+  if (!c.padded) return ldv4(diag + l);
+  V4<double> v{};
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+    if (c.x + i < c.nx) v.v[i] = diag[l + i];
+  return v;
+}
+
 template <typename T>
 __device__ __forceinline__ void upd4_task(const DevArrays& A, double* part, int64_t task,
                                           const InstScal& s) {
-  const Quad c = quad_cell(A, task);
+  const Quad c = quad_cell<sizeof(T) == 4>(A, task);
   const bool weighted = (A.opts.criterion == HF_STOP_RECURSIVE);
   const T alpha = (T)s.alpha;
   const bool first = (s.iter == 0);
-  T* Y = Vec<T>::y(A) + c.off;
-  T* R = Vec<T>::r(A) + c.off;
-  const T* P = Vec<T>::pb(A, s.iter) + c.off;
-  const T* Q = Vec<T>::q(A) + c.off;
+  T* Y = Vec<T>::y(A) + c.voff;
+  T* R = Vec<T>::r(A) + c.voff;
+  const T* P = Vec<T>::pb(A, s.iter) + c.voff;
+  const T* Q = Vec<T>::q(A) + c.voff;
   const double* __restrict__ diag = A.diag + c.off;
   T rr = T(0);
   double rw = 0.0;
@@ -806,7 +838,7 @@ __device__ __forceinline__ void upd4_task(const DevArrays& A, double* part, int6
         const V4<T>& yv = h ? y1 : y0;
         V4<T> yo, ro;
         V4<double> dg{};
-        if (weighted) dg = ldv4(diag + l);
+        if (weighted) dg = diag4(diag, c, z + h);
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
           yo.v[i] = first ? alpha * pv.v[i] : fma(alpha, pv.v[i], yv.v[i]);
@@ -831,14 +863,14 @@ __device__ __forceinline__ void upd4_task(const DevArrays& A, double* part, int6
 template <typename T>
 __device__ __forceinline__ void cgp4_task(const DevArrays& A, double* part, int64_t task,
                                           const InstScal& s) {
-  const Quad c = quad_cell(A, task);
+  const Quad c = quad_cell<sizeof(T) == 4>(A, task);
   if (!c.act) return;
   const int64_t k = s.iter;
   const bool first = (k == 0);
   const T beta = (T)s.beta;
-  const T* R = Vec<T>::r(A) + c.off;
-  const T* Po = Vec<T>::pb(A, k + 1) + c.off;
-  T* Pn = Vec<T>::pb(A, k) + c.off;
+  const T* R = Vec<T>::r(A) + c.voff;
+  const T* Po = Vec<T>::pb(A, k + 1) + c.voff;
+  T* Pn = Vec<T>::pb(A, k) + c.voff;
   for (int z = c.za; z < c.zb; z += 2) {
     const bool two = z + 1 < c.zb;
     const int l0 = c.lxy + z * c.nxy, l1 = l0 + c.nxy;
@@ -862,11 +894,11 @@ __device__ __forceinline__ void cgp4_task(const DevArrays& A, double* part, int6
 template <typename TY>
 __device__ __forceinline__ void xupd4_task(const DevArrays& A, double* part, int64_t task,
                                            const InstScal& s) {
-  const Quad c = quad_cell(A, task);
+  const Quad c = quad_cell<false>(A, task);   // rows of 4k cells: the two layouts agree in shape
   if (!c.act) return;
   const double* XR = A.tbuf[s.role[2]] + c.off;
   double* XW = A.tbuf[s.role[3]] + c.off;
-  const TY* Y = Vec<TY>::y(A) + c.off;
+  const TY* Y = Vec<TY>::y(A) + (sizeof(TY) == 4 ? A.inst[A.tasks[task].x].off4 : c.off);
   const double* __restrict__ sinv = A.sinv + c.off;
   const float* __restrict__ sinv32 = A.sinv32 + c.off;
   const bool use_y = s.iter > 0;
@@ -911,15 +943,18 @@ __device__ __forceinline__ void xupd4_task(const DevArrays& A, double* part, int
   }
 }
 
-// Dispatch between the vector and the scalar form of a pass (same choice on every path).
+// Dispatch between the vector and the scalar form of a pass (same choice on every path).  The
+// FP32 vectors are padded to rows of 4k cells, so their passes are always vector passes.
 template <typename T>
 __device__ __forceinline__ void upd_any(const DevArrays& A, double* part, int64_t task, const InstScal& s) {
-  if (vec4_ok(A.inst[A.tasks[task].x])) upd4_task<T>(A, part, task, s);
+  if constexpr (sizeof(T) == 4) upd4_task<T>(A, part, task, s);
+  else if (vec4_ok(A.inst[A.tasks[task].x])) upd4_task<T>(A, part, task, s);
   else upd_task<T>(A, part, task, s);
 }
 template <typename T>
 __device__ __forceinline__ void cgp_any(const DevArrays& A, double* part, int64_t task, const InstScal& s) {
-  if (vec4_ok(A.inst[A.tasks[task].x])) cgp4_task<T>(A, part, task, s);
+  if constexpr (sizeof(T) == 4) cgp4_task<T>(A, part, task, s);
+  else if (vec4_ok(A.inst[A.tasks[task].x])) cgp4_task<T>(A, part, task, s);
   else cgp_task<T>(A, part, task, s);
 }
 template <typename TY>
@@ -928,12 +963,11 @@ __device__ __forceinline__ void xupd_any(const DevArrays& A, double* part, int64
   else xupd_task<TY>(A, part, task, s);
 }
 
-// The FP32 p + SpMV pass of one task: vector form where the grid allows it.
+// The FP32 p + SpMV pass of one task (always the vector form: the FP32 layout has rows of 4k).
 template <bool FUSED>
 __device__ __forceinline__ void pq_f32_task(const DevArrays& A, double* part, int64_t task,
                                             const InstScal& s) {
-  if (vec4_ok(A.inst[A.tasks[task].x])) spmv4_task<FUSED>(A, part, task, s);
-  else spmv_task<float, FUSED>(A, part, task, s);
+  spmv4_task<FUSED>(A, part, task, s);
 }
 
 // ---- standalone kernels (host-polled loop, conditional-node graph, kernel timing) --------------
@@ -963,7 +997,7 @@ template <typename T>
 __global__ void __launch_bounds__(kBlock) k_cg_spmv(DevArrays A) {
   const InstScal& s = A.scal[A.tasks[blockIdx.x].x];
   if (!s.inner_active) return;
-  if (sizeof(T) == 4) pq_f32_task<false>(A, A.partials, blockIdx.x, s);
+  if constexpr (sizeof(T) == 4) pq_f32_task<false>(A, A.partials, blockIdx.x, s);
   else spmv_task<T, false>(A, A.partials, blockIdx.x, s);
 }
 
@@ -1430,17 +1464,20 @@ __device__ bool grid_barrier_epilogue(const DevArrays& A, SolveCtl* ctl, unsigne
 template <typename T>
 __device__ __forceinline__ void round_task(const DevArrays& A, double* part, int64_t task,
                                            const InstScal& s) {
-  if (sizeof(T) == 4 && (s.phase == PH_CG_PQ || s.phase == PH_CG_Q)) {
-    if (s.phase == PH_CG_PQ) pq_f32_task<true>(A, part, task, s);
-    else pq_f32_task<false>(A, part, task, s);
-    return;
+  if constexpr (sizeof(T) == 4) {
+    if (s.phase == PH_CG_PQ || s.phase == PH_CG_Q) {
+      if (s.phase == PH_CG_PQ) pq_f32_task<true>(A, part, task, s);
+      else pq_f32_task<false>(A, part, task, s);
+      return;
+    }
+  } else {
+    if (s.phase == PH_CG_Q) { spmv_task<T, false>(A, part, task, s); return; }
+    if (s.phase == PH_CG_PQ) { spmv_task<T, true>(A, part, task, s); return; }
   }
   switch (s.phase) {
     case PH_RES_INIT: res_task<true, T>(A, part, task, s); break;
     case PH_RES: res_task<false, T>(A, part, task, s); break;
     case PH_CG_P: cgp_any<T>(A, part, task, s); break;
-    case PH_CG_Q: spmv_task<T, false>(A, part, task, s); break;
-    case PH_CG_PQ: spmv_task<T, true>(A, part, task, s); break;
     case PH_CG_B: upd_any<T>(A, part, task, s); break;
     case PH_XUPD: xupd_any<T>(A, part, task, s); break;
     default: break;
