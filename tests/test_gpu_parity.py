@@ -371,3 +371,46 @@ def test_vector_paths_match_oracle(cuda_lib, name, g):
     err = np.linalg.norm(T - Tref) / np.linalg.norm(Tref)
     assert err <= 1e-11, (name, err, st)
     assert np.linalg.norm(Tp - Tpref) / np.linalg.norm(Tpref) <= 1e-11
+
+
+def _padded_cases():
+    """Grids whose rows are not a multiple of 4 cells: the mixed path's FP32 vectors then carry
+    padding cells (rows rounded up to 4), and a row's last quad holds 1, 2 or 3 grid cells, with
+    the periodic x wrap taken from a load."""
+    c = {}
+    c["px_5"] = _rng_problem(5, 4, 3, periodic=(1, 1, 0))         # 4k+1, x and y periodic
+    c["px_6"] = _rng_problem(6, 3, 4, periodic=(1, 0, 1))         # 4k+2
+    c["px_7"] = _rng_problem(7, 5, 3, periodic=(1, 0, 0))         # 4k+3
+    c["px_2"] = _rng_problem(2, 3, 4, periodic=(1, 1, 1))         # both x faces join the same pair
+    c["wide_37"] = _rng_problem(37, 9, 6)                         # a second tile of 5 cells
+    c["px_wide_35"] = _rng_problem(35, 4, 5, periodic=(1, 0, 0))  # wrap across two tiles
+    c["neumann_9"] = _rng_problem(9, 5, 4, cg_face=(1, 0, 0, 1, 0, 1), t_bath_cg=2.0)
+    c["heaters_5"] = _rng_problem(5, 5, 5, iheater=np.arange(125, dtype=np.int64) % 9 - 1,
+                                  power_in=2e-6, freq=3.0e11, heated_steps=2, em=0.3, t_bath=280.0)
+    c["single"] = _rng_problem(1, 1, 1)
+    return c
+
+
+PADDED_CASES = _padded_cases()
+
+
+@pytest.mark.parametrize("name", sorted(PADDED_CASES))
+def test_padded_rows_mixed_match_oracle(cuda_lib, name):
+    """Five mixed-precision steps to true rel-res <= 1e-10 on grids with padded FP32 rows, host
+    loop and persistent solve, against the oracle's FP64 PCG to 1e-13: fields within 1e-9
+    relative L2 (the mixed path's tolerance); the two paths give the same bits."""
+    prob = PADDED_CASES[name]
+    assert prob.nx % 4 != 0
+    Tref, _ = _oracle_run(prob, 5, mode=1, tol=1e-13)
+    fields = []
+    for g in (0, 1):
+        with HeatFlow(prob, precision="mixed", criterion="true", tol=1e-10, use_graph=g) as hf:
+            hf.initial_evolve()
+            for k in range(1, 6):
+                st = hf.simulate(k)
+                assert st["unconverged"] == 0
+                assert st["last_true_relres"] <= 1e-10
+            fields.append(hf.get_state()[0])
+    assert np.array_equal(fields[0], fields[1])
+    err = np.linalg.norm(fields[1] - Tref) / np.linalg.norm(Tref)
+    assert err < 1e-9, (name, err)
