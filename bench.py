@@ -11,7 +11,8 @@ One "step" is one implicit time step (RHS, initial guess, solve, state rotation)
 `value` is timed with CUDA events on the library's stream with the state resident in HBM;
 `e2e` is the same metric through the C ABI with host buffers: every step uploads T^n, T^(n-1)
 from pinned host memory and downloads the new T^n into pinned host memory, queued through
-hf_step_host_async (T^(n-1)'s upload overlaps the previous step's download) and ended by
+hf_step_host_async (T^(n-1)'s upload overlaps the previous step's solve, T^n moves in chunks
+behind the previous step's download, and each chunk's RHS runs as it lands) and ended by
 hf_host_sync; `e2e.sync_value` times the same steps through hf_set_state, hf_step, hf_get_state.
 
     python bench.py [--gpus N --steps K --warmup W] [--impl reference]
@@ -607,7 +608,8 @@ def main():
                "timing": "wall clock over K steps queued through hf_step_host_async (every step "
                          "uploads T^n and T^(n-1) from pinned memory and downloads the new T^n "
                          "into pinned memory; T^(n-1)'s upload overlaps the previous step's "
-                         "download), ended by hf_host_sync",
+                         "solve, T^n moves in chunks behind the previous step's download and "
+                         "each chunk's RHS runs as it lands), ended by hf_host_sync",
                "sync_value": world * K / sync_s,
                "sync_timing": "host-synchronous calls per step: hf_set_state, hf_step, "
                               "hf_get_state"}

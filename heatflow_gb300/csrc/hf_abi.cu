@@ -108,16 +108,25 @@ void drop_graph(Ctx& c) {
   if (c.loop_graph) cudaGraphDestroy(c.loop_graph);
   c.loop_exec = nullptr;
   c.loop_graph = nullptr;
+  if (c.post_exec) cudaGraphExecDestroy(c.post_exec);
+  if (c.post_graph) cudaGraphDestroy(c.post_graph);
+  c.post_exec = nullptr;
+  c.post_graph = nullptr;
 }
 
 void free_all(Ctx& c) {
   if (c.stream) cudaStreamSynchronize(c.stream);   // queued host-buffer steps may still run
   drop_graph(c);
-  for (cudaEvent_t* e : {&c.ev_placed, &c.ev_in, &c.ev_out_done}) {
+  if (c.out_stream) cudaStreamSynchronize(c.out_stream);
+  for (cudaEvent_t* e : {&c.ev_placed, &c.ev_out_done, &c.ev_in_pp, &c.ev_gathered}) {
     if (*e) cudaEventDestroy(*e);
     *e = nullptr;
   }
   for (auto& e : c.ev_chunk) {
+    if (e) cudaEventDestroy(e);
+    e = nullptr;
+  }
+  for (auto& e : c.ev_in_chunk) {
     if (e) cudaEventDestroy(e);
     e = nullptr;
   }
@@ -130,6 +139,8 @@ void free_all(Ctx& c) {
   }
   if (c.copy_stream) cudaStreamDestroy(c.copy_stream);
   c.copy_stream = nullptr;
+  if (c.out_stream) cudaStreamDestroy(c.out_stream);
+  c.out_stream = nullptr;
   for (void* p : c.allocs) cudaFree(p);
   c.allocs.clear();
   if (c.h_scal) cudaFreeHost(c.h_scal);
@@ -460,6 +471,93 @@ int build_graph(Ctx& c) {
   c.graph_criterion = c.opts.criterion;
   c.graph_mode = c.opts.use_graph;
   return HF_OK;
+}
+
+// The step after its RHS (RHS finalize, persistent solve, step end, property rebuild) as one
+// graph, for steps whose RHS runs chunk by chunk behind the host upload (hf_step_host_async).
+int build_post_graph(Ctx& c) {
+  if (c.post_exec && c.post_precision == c.opts.precision && c.post_criterion == c.opts.criterion)
+    return HF_OK;
+  if (c.post_exec) cudaGraphExecDestroy(c.post_exec);
+  if (c.post_graph) cudaGraphDestroy(c.post_graph);
+  c.post_exec = nullptr;
+  c.post_graph = nullptr;
+  if (!c.d_ctrl) {
+    int r = dalloc(c, &c.d_ctrl, 1);
+    if (r) return r;
+    CU(cudaMemset(c.d_ctrl, 0, sizeof(CtrlState)));
+  }
+  if (solve_grid_blocks(c, c.opts.precision == HF_PREC_MIXED ? 1 : 0) < 1)
+    return set_err(HF_ECUDA, "no co-resident grid for the persistent solve kernel");
+  cudaStream_t cs = nullptr;
+  CU(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  cudaStream_t saved = c.stream;
+  cudaGraph_t g = nullptr;
+  std::string err;
+  auto chk = [&](cudaError_t e, const char* what) {
+    if (e != cudaSuccess && err.empty()) err = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaSuccess;
+  };
+  if (chk(cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed), "capture")) {
+    c.stream = cs;
+    chk(launch_finalize(c, FIN_RHS, nullptr, 0, 0), "rhs finalize");
+    chk(launch_solve(c), "persistent solve");
+    chk(launch_graph_step_end(c, c.d_ctrl, c.d_sctl), "step end");
+    if (c.tempdep) chk(launch_tempdep(c), "properties");
+    chk(cudaStreamEndCapture(cs, &g), "end capture");
+    if (err.empty()) chk(cudaGraphInstantiate(&c.post_exec, g, 0), "instantiate");
+  }
+  c.stream = saved;
+  cudaStreamDestroy(cs);
+  if (!err.empty()) {
+    if (c.post_exec) cudaGraphExecDestroy(c.post_exec);
+    c.post_exec = nullptr;
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return set_err(HF_ECUDA, "graph capture: " + err);
+  }
+  c.post_graph = g;
+  c.post_precision = c.opts.precision;
+  c.post_criterion = c.opts.criterion;
+  return HF_OK;
+}
+
+// Chunks of the host arrays for hf_step_host_async: whole z-slabs of tasks (instance i, task
+// planes [bz*zc, (bz+1)*zc)), which are contiguous in the compact host layout, in the device
+// layout and in the task table, merged in order into at most kHostChunks chunks of about equal
+// cells.
+void build_host_chunks(Ctx& c) {
+  if (c.host_chunks_depth == c.depth && !c.host_chunks.empty()) return;
+  int64_t total = 0;
+  for (const auto& d : c.h_inst) total += d.n;
+  const int64_t target = (total + Ctx::kHostChunks - 1) / Ctx::kHostChunks;
+  c.host_chunks.clear();
+  Ctx::HostChunk cur{0, 0, 0, 0, 0, 0};
+  bool open = false;
+  for (const auto& d : c.h_inst) {
+    const int64_t nbx = (d.nx + kTX - 1) / kTX, nby = (d.ny + kTY - 1) / kTY;
+    const int64_t nxy = (int64_t)d.nx * d.ny;
+    for (int64_t z0 = 0, bz = 0; z0 < d.nz; z0 += d.zc, ++bz) {
+      const int64_t z1 = std::min<int64_t>(z0 + d.zc, d.nz);
+      const Ctx::HostChunk g{d.hoff + z0 * nxy, d.hoff + z1 * nxy, d.off + z0 * nxy,
+                             d.off + z1 * nxy, d.task0 + bz * nbx * nby,
+                             d.task0 + (bz + 1) * nbx * nby};
+      if (!open) {
+        cur = g;
+        open = true;
+      } else {
+        cur.chi = g.chi;
+        cur.ghi = g.ghi;
+        cur.thi = g.thi;
+      }
+      if (cur.chi - cur.clo >= target && (int)c.host_chunks.size() < Ctx::kHostChunks - 1) {
+        c.host_chunks.push_back(cur);
+        open = false;
+      }
+    }
+  }
+  if (open) c.host_chunks.push_back(cur);
+  c.host_chunks_depth = c.depth;
 }
 
 void fill_stats(Ctx& c, hf_stats* st, int64_t steps, const std::vector<InstScal>& before) {
@@ -979,19 +1077,24 @@ int hf_step_host_async(hf_ctx* h, int64_t itime, const double* tp, const double*
     if ((rc = sync_scal(c))) return rc;
     c.async_before.assign(c.h_scal, c.h_scal + c.ninst);
     c.async_steps = 0;
-    if ((rc = build_graph(c))) return rc;
+    if ((rc = build_post_graph(c))) return rc;
+    build_host_chunks(c);
     if (!c.copy_stream) CU(cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking));
-    for (cudaEvent_t* e : {&c.ev_placed, &c.ev_in, &c.ev_out_done})
+    if (!c.out_stream) CU(cudaStreamCreateWithFlags(&c.out_stream, cudaStreamNonBlocking));
+    for (cudaEvent_t* e : {&c.ev_placed, &c.ev_out_done, &c.ev_in_pp, &c.ev_gathered})
       if (!*e) CU(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
     for (auto& e : c.ev_chunk)
+      if (!e) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    for (auto& e : c.ev_in_chunk)
       if (!e) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     for (double** b : {&c.d_stage_p, &c.d_stage_pp, &c.d_stage_out})
       if (!*b && (rc = dalloc(c, b, (size_t)total))) return rc;
     CU(cudaEventRecord(c.ev_placed, c.stream));
+    CU(cudaEventRecord(c.ev_out_done, c.stream));
     c.last_out = nullptr;
   }
-  const bool loop = c.opts.use_graph == 1 && build_loop_graph(c) == HF_OK;
-  const int64_t chunk = (total + Ctx::kHostChunks - 1) / Ctx::kHostChunks;
+  const std::vector<Ctx::HostChunk>& ch = c.host_chunks;
+  const int nch = (int)ch.size();
   // Copy stream.  The staging buffers are free once the previous step placed its inputs; by then
   // every download older than the previous step's is done too (the main stream is in order).
   // T^(n-1) is normally such an older result, so its upload overlaps the previous step's solve.
@@ -1001,31 +1104,42 @@ int hf_step_host_async(hf_ctx* h, int64_t itime, const double* tp, const double*
   if (tpp == c.last_out) CU(cudaStreamWaitEvent(c.copy_stream, c.ev_out_done, 0));
   CU(cudaMemcpyAsync(c.d_stage_pp, tpp, sizeof(double) * (size_t)total, cudaMemcpyHostToDevice,
                      c.copy_stream));
-  for (int k = 0; k < Ctx::kHostChunks; ++k) {
-    const int64_t lo = k * chunk, n = std::min<int64_t>(chunk, total - lo);
-    if (n <= 0) break;
+  CU(cudaEventRecord(c.ev_in_pp, c.copy_stream));
+  for (int k = 0; k < nch; ++k) {
     if (tp == c.last_out) CU(cudaStreamWaitEvent(c.copy_stream, c.ev_chunk[k], 0));
-    CU(cudaMemcpyAsync(c.d_stage_p + lo, tp + lo, sizeof(double) * (size_t)n, cudaMemcpyHostToDevice,
+    CU(cudaMemcpyAsync(c.d_stage_p + ch[k].clo, tp + ch[k].clo,
+                       sizeof(double) * (size_t)(ch[k].chi - ch[k].clo), cudaMemcpyHostToDevice,
                        c.copy_stream));
+    CU(cudaEventRecord(c.ev_in_chunk[k], c.copy_stream));
   }
-  CU(cudaEventRecord(c.ev_in, c.copy_stream));
-  // Main stream: place the inputs, run the step, gather its result, download it chunk by chunk.
-  CU(cudaStreamWaitEvent(c.stream, c.ev_in, 0));
-  CU(launch_host_in(c, c.d_stage_p, 0, c.stream));
+  // Main stream: place T^(n-1), begin the step, then place each chunk of T^n as it lands and run
+  // the RHS of its tasks (the later chunks are still on the link); then the rest of the step as
+  // one graph and the gather of its result.  The download runs on a stream of its own, chunk by
+  // chunk, so the next step's placements and RHS chunks do not queue behind it.
+  CU(cudaStreamWaitEvent(c.stream, c.ev_in_pp, 0));
   CU(launch_host_in(c, c.d_stage_pp, 1, c.stream));
-  CU(cudaEventRecord(c.ev_placed, c.stream));
   const int64_t per = c.opts.precision == HF_PREC_MIXED ? c.opts.inner_itmax : c.opts.itmax;
   CU(launch_ctrl_init(c, itime, 2 * (int64_t)(c.opts.max_refine + 3) * (per + 3)));
-  CU(cudaGraphLaunch(loop ? c.loop_exec : c.graph_exec, c.stream));
-  CU(launch_host_out(c, c.d_stage_out, c.stream));
-  for (int k = 0; k < Ctx::kHostChunks; ++k) {
-    const int64_t lo = k * chunk, n = std::min<int64_t>(chunk, total - lo);
-    if (n > 0)
-      CU(cudaMemcpyAsync(out + lo, c.d_stage_out + lo, sizeof(double) * (size_t)n,
-                         cudaMemcpyDeviceToHost, c.stream));
-    CU(cudaEventRecord(c.ev_chunk[k], c.stream));
+  // kernels of the step outside the host copies: begin, RHS per chunk, finalize, solve, end
+  CU(launch_graph_step_begin(c, c.d_ctrl, nch + 4 + (c.tempdep ? 4 : 0)));
+  for (int k = 0; k < nch; ++k) {
+    CU(cudaStreamWaitEvent(c.stream, c.ev_in_chunk[k], 0));
+    CU(launch_host_in_range(c, c.d_stage_p, 0, ch[k].glo, ch[k].ghi, c.stream));
+    CU(launch_rhs_range(c, ch[k].tlo, ch[k].thi));
   }
-  CU(cudaEventRecord(c.ev_out_done, c.stream));
+  CU(cudaEventRecord(c.ev_placed, c.stream));
+  CU(cudaGraphLaunch(c.post_exec, c.stream));
+  CU(cudaStreamWaitEvent(c.stream, c.ev_out_done, 0));    // the previous download has left d_stage_out
+  CU(launch_host_out(c, c.d_stage_out, c.stream));
+  CU(cudaEventRecord(c.ev_gathered, c.stream));
+  CU(cudaStreamWaitEvent(c.out_stream, c.ev_gathered, 0));
+  for (int k = 0; k < nch; ++k) {
+    CU(cudaMemcpyAsync(out + ch[k].clo, c.d_stage_out + ch[k].clo,
+                       sizeof(double) * (size_t)(ch[k].chi - ch[k].clo), cudaMemcpyDeviceToHost,
+                       c.out_stream));
+    CU(cudaEventRecord(c.ev_chunk[k], c.out_stream));
+  }
+  CU(cudaEventRecord(c.ev_out_done, c.out_stream));
   c.last_out = out;
   c.async_pending = true;
   c.async_steps += 1;
@@ -1045,9 +1159,12 @@ int hf_host_sync(hf_ctx* h, hf_stats* stats) {
   CU(cudaMemcpyAsync(&cs, c.d_ctrl, sizeof(cs), cudaMemcpyDeviceToHost, c.stream));
   CU(cudaStreamSynchronize(c.stream));
   CU(cudaStreamSynchronize(c.copy_stream));
+  CU(cudaStreamSynchronize(c.out_stream));
   const int64_t steps = c.async_steps;
   c.async_steps = 0;
-  c.launches += cs.launches + 4 * steps;
+  // host copies per step: T^(n-1) placed, T^n placed per chunk, the control reset, the gather
+  const int64_t host_kernels = 3 + (int64_t)c.host_chunks.size();
+  c.launches += cs.launches + host_kernels * steps;
   if (cs.guard_hit & 2)
     return set_err(HF_EDEVICE, "persistent solve: a grid barrier wait reached its time limit");
   if (cs.guard_hit) return set_err(HF_EDEVICE, "captured solve loop reached its iteration bound");
@@ -1055,7 +1172,7 @@ int hf_host_sync(hf_ctx* h, hf_stats* stats) {
   if (rc) return rc;
   if ((rc = diagnose(c))) return rc;
   fill_stats(c, stats, steps, c.async_before);
-  if (stats) stats->kernel_launches = cs.launches + 4 * steps;
+  if (stats) stats->kernel_launches = cs.launches + host_kernels * steps;
   return first_error(c);
 }
 

@@ -67,13 +67,26 @@ struct Ctx {
   // compact staging buffers; kernels place them into (and gather from) the role buffers
   static constexpr int kHostChunks = 8;
   cudaEvent_t ev_placed = nullptr;     // the last queued step's inputs are in their role buffers
-  cudaEvent_t ev_in = nullptr;         // the next step's inputs are in the staging buffers
   cudaEvent_t ev_out_done = nullptr;   // the last queued step's result is on the host
   cudaEvent_t ev_chunk[kHostChunks] = {};   // ... chunk by chunk
   double* d_stage_p = nullptr;         // T^n of the next step (compact layout)
   double* d_stage_pp = nullptr;        // T^(n-1) of the next step
   double* d_stage_out = nullptr;       // the last step's result
   const double* last_out = nullptr;    // host array of the last queued download
+  // T^n moves in chunks of whole task z-slabs: each chunk's RHS tasks run as soon as its cells
+  // are placed, while later chunks are still on the link.  Cells [clo, chi) of the compact host
+  // layout, [glo, ghi) of the device layout, tasks [tlo, thi).
+  struct HostChunk { int64_t clo, chi, glo, ghi, tlo, thi; };
+  std::vector<HostChunk> host_chunks;
+  int host_chunks_depth = -1;           // task depth the chunks were cut for
+  cudaStream_t out_stream = nullptr;    // downloads, so the next step's work need not queue behind them
+  cudaEvent_t ev_gathered = nullptr;    // the last queued step's result is in d_stage_out
+  cudaEvent_t ev_in_pp = nullptr;       // T^(n-1) of the next step is in its staging buffer
+  cudaEvent_t ev_in_chunk[kHostChunks] = {};   // ... T^n, chunk by chunk
+  // the step after its RHS (finalize, persistent solve, step end, property rebuild) as one graph
+  cudaGraphExec_t post_exec = nullptr;
+  cudaGraph_t post_graph = nullptr;
+  int post_precision = -1, post_criterion = -1;
   bool async_pending = false;          // steps queued since the last hf_host_sync
   int64_t async_steps = 0;
   std::vector<InstScal> async_before;  // scalars before the first queued step

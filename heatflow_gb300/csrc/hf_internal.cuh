@@ -407,6 +407,8 @@ cudaError_t launch_coo(Ctx& c, int64_t instance, int64_t* d_counts, int64_t* d_i
                        int64_t* d_jcol, double* d_val, int64_t* d_pos, int phase);
 cudaError_t launch_step_begin(Ctx& c, int64_t itime, int first_of_run);
 cudaError_t launch_rhs(Ctx& c);
+// The RHS of tasks [t0, t1) only (their cells' inputs placed; the finalize still sums all tasks).
+cudaError_t launch_rhs_range(Ctx& c, int64_t t0, int64_t t1);
 cudaError_t launch_task_heat(Ctx& c);
 // Tabulated properties at the current T^n, then the operator rebuilt (4 kernels).
 cudaError_t launch_tempdep(Ctx& c);
@@ -415,6 +417,9 @@ cudaError_t launch_subbox_gather(Ctx& c, int64_t inst, const int64_t* lo, const 
 // Temperature role buffer `which` of every instance <-> a compact device array, on `stream`;
 // host_in drops the stored products H T of an instance whose state it changes.
 cudaError_t launch_host_in(Ctx& c, const double* src, int which, cudaStream_t stream);
+// The same for the device cells [glo, ghi) (whole z-slabs of instances, padding skipped).
+cudaError_t launch_host_in_range(Ctx& c, const double* src, int which, int64_t glo, int64_t ghi,
+                                 cudaStream_t stream);
 cudaError_t launch_host_out(Ctx& c, double* dst, cudaStream_t stream);
 // Control block of a one-step graph launch queued without the host (async host-buffer steps).
 cudaError_t launch_ctrl_init(Ctx& c, int64_t itime, int64_t limit);

@@ -172,8 +172,8 @@ __device__ __forceinline__ void rhs4_task(const DevArrays& A, int64_t task, cons
 // DIAG: count NaNs per vector (failure path only).
 template <bool PARTS, bool DIAG>
 __global__ void __launch_bounds__(kBlock, 4) k_rhs(DevArrays A, double* oB, double* oQ, double* oQd,
-                                                double* oSc) {
-  const int64_t task = blockIdx.x;
+                                                double* oSc, int64_t task_base) {
+  const int64_t task = task_base + blockIdx.x;
   if (!PARTS && !DIAG && task == 0 && threadIdx.x == 0) A.stamps[kStampRhs] = gtimer();
   if (!PARTS && !DIAG) {          // the step's pass: vector form where the rows allow it
     const int inst = A.tasks[task].x;
@@ -291,18 +291,23 @@ __global__ void __launch_bounds__(kBlock, 4) k_rhs(DevArrays A, double* oB, doub
   tile_store<1>(A, task, v);
 }
 
-cudaError_t launch_rhs(Ctx& c) {
-  k_rhs<false, false><<<(unsigned)c.ntasks, kBlock, 0, c.stream>>>(c.A, nullptr, nullptr, nullptr, nullptr);
+cudaError_t launch_rhs(Ctx& c) { return launch_rhs_range(c, 0, c.ntasks); }
+
+cudaError_t launch_rhs_range(Ctx& c, int64_t t0, int64_t t1) {
+  if (t1 <= t0) return cudaSuccess;
+  k_rhs<false, false><<<(unsigned)(t1 - t0), kBlock, 0, c.stream>>>(c.A, nullptr, nullptr, nullptr,
+                                                                    nullptr, t0);
   return cudaGetLastError();
 }
 
 cudaError_t launch_rhs_parts(Ctx& c, double* B, double* Q, double* Qd, double* Sc) {
-  k_rhs<true, false><<<(unsigned)c.ntasks, kBlock, 0, c.stream>>>(c.A, B, Q, Qd, Sc);
+  k_rhs<true, false><<<(unsigned)c.ntasks, kBlock, 0, c.stream>>>(c.A, B, Q, Qd, Sc, 0);
   return cudaGetLastError();
 }
 
 cudaError_t launch_rhs_diagnose(Ctx& c) {
-  k_rhs<false, true><<<(unsigned)c.ntasks, kBlock, 0, c.stream>>>(c.A, nullptr, nullptr, nullptr, nullptr);
+  k_rhs<false, true><<<(unsigned)c.ntasks, kBlock, 0, c.stream>>>(c.A, nullptr, nullptr, nullptr,
+                                                                  nullptr, 0);
   return cudaGetLastError();
 }
 
@@ -453,9 +458,10 @@ cudaError_t launch_subbox_gather(Ctx& c, int64_t inst, const int64_t* lo, const 
 // on the device, so they can be queued behind the step that rotates the roles.  Placing compares
 // bit patterns first: an input that is exactly the state already there (a caller feeding back the
 // results it downloaded) keeps the stored products H T^n, H T^(n-1); any other drops them.
-__global__ void k_host_in(DevArrays A, const double* __restrict__ src, int which) {
+__global__ void k_host_in(DevArrays A, const double* __restrict__ src, int which, int64_t glo,
+                          int64_t ghi) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < A.ncells; g += stride) {
+  for (int64_t g = glo + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < ghi; g += stride) {
     const int inst = A.tile_inst[g / kTile];
     const InstDesc& d = A.inst[inst];
     const int64_t l = g - d.off;
@@ -497,7 +503,14 @@ static unsigned host_copy_blocks(Ctx& c) {
 }
 
 cudaError_t launch_host_in(Ctx& c, const double* src, int which, cudaStream_t stream) {
-  k_host_in<<<host_copy_blocks(c), 256, 0, stream>>>(c.A, src, which);
+  return launch_host_in_range(c, src, which, 0, c.ncells, stream);
+}
+
+cudaError_t launch_host_in_range(Ctx& c, const double* src, int which, int64_t glo, int64_t ghi,
+                                 cudaStream_t stream) {
+  if (ghi <= glo) return cudaSuccess;
+  const unsigned nb = (unsigned)std::max<int64_t>(1, std::min<int64_t>((ghi - glo + 255) / 256, 152 * 8));
+  k_host_in<<<nb, 256, 0, stream>>>(c.A, src, which, glo, ghi);
   return cudaGetLastError();
 }
 

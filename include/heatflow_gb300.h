@@ -210,7 +210,8 @@ int hf_adjoint_accumulate(hf_ctx* ctx, const double* lam, const double* x, int64
  * buffers, whose indices live on the device, and gather the result).  T^(n-1) - normally the
  * result of two calls back - is uploaded on a second stream while the previous step is still
  * solving; T^n - normally the previous call's temp_out - is uploaded chunk by chunk right behind
- * that download, so both directions of the host link run at once.  Any arrays may be passed:
+ * that download, so both directions of the host link run at once, and the right-hand side of
+ * each chunk's cells is computed as soon as the chunk is placed.  Any arrays may be passed:
  * an input that is the previous call's temp_out waits for its download.  Every array
  * holds total_cells doubles (instances back to back) and must stay valid and untouched until
  * hf_host_sync returns.  Needs use_graph 1 or 3.  While steps are queued, every other call that
