@@ -640,6 +640,14 @@ int build_tasks(Ctx& c, int depth) {
   if ((int64_t)tasks.size() > c.ntasks_cap) return set_err(HF_EARG, "task depth below the minimum");
   c.ntasks = (int64_t)tasks.size();
   c.A.ntasks = c.ntasks;
+  std::vector<int32_t> large;
+  for (int64_t i = 0; i < c.ninst; ++i)
+    if (c.h_inst[i].ntask > kWarpSumMax) large.push_back((int32_t)i);
+  c.A.nlarge = (int64_t)large.size();
+  c.A.nsmall = c.ninst - c.A.nlarge;
+  if (!large.empty())
+    CU(cudaMemcpyAsync(const_cast<int32_t*>(c.A.large), large.data(), sizeof(int32_t) * large.size(),
+                       cudaMemcpyHostToDevice, c.stream));
   CU(cudaMemcpyAsync(const_cast<int4*>(c.A.tasks), tasks.data(), sizeof(int4) * tasks.size(),
                      cudaMemcpyHostToDevice, c.stream));
   CU(cudaMemcpyAsync(const_cast<InstDesc*>(c.A.inst), c.h_inst.data(), sizeof(InstDesc) * c.ninst,
@@ -699,6 +707,12 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
     hoff += d.n;
     d.sx = (int32_t)((p.nx + 3) / 4 * 4);
     d.off4 = off4;
+    {
+      const int64_t slots_tile = (p.nx + kTX - 1) / kTX * kTX * ((p.ny + kTY - 1) / kTY * kTY);
+      const int64_t quads = (int64_t)d.sx / 4 * p.ny;            // quads per plane
+      const int64_t slots_lin = (quads + 63) / 64 * 256;
+      d.lin4 = 10 * slots_lin < 9 * slots_tile ? 1 : 0;
+    }
     const int64_t n4 = (int64_t)d.sx * p.ny * p.nz;
     off4 += (n4 + kTile - 1) / kTile * kTile;
     d.tile0 = tiles;
@@ -787,6 +801,9 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
   ALLOC(c.d_sctl, (size_t)1);
   ALLOC(A.counters, (size_t)count);
   ALLOC(c.d_bc, (size_t)count);
+  int32_t* d_large;
+  ALLOC(d_large, (size_t)count);
+  A.large = d_large;
   A.inst = d_inst; A.scal = d_scal; A.tile_inst = d_tile_inst;
   ALLOC(A.diag, N); ALLOC(A.cx, N); ALLOC(A.cy, N); ALLOC(A.cz, N); ALLOC(A.sinv, N);
   ALLOC(A.rsum, N); ALLOC(A.sinv32, N);

@@ -35,6 +35,9 @@ constexpr int kNR = 8;
 // depth (InstDesc::zc planes, an option; kZC by default) along z.  (kXC > 1 trades occupancy for
 // per-thread parallelism; on GB300 kXC = 1 is faster.)
 constexpr int kXC = 1, kTX = 32 * kXC, kTY = 8, kZC = 16;
+// Instances with more tasks than this have their task partials summed by a whole block, the
+// others by one warp.
+constexpr int kWarpSumMax = 512;
 constexpr int kMinTaskDepth = 4;   // task buffers are sized for the shallowest task depth
 // InstScal::status bit: some S was NaN; the failing vector is found by the diagnosis kernel.
 constexpr int kStatusRhsNan = 1 << 16;                       // reduction slots per tile
@@ -66,7 +69,10 @@ struct InstDesc {
   // 16-byte vector passes; instance at off4, a multiple of kTile cells.  sx = nx: the FP64 layout.
   int64_t off4;
   int32_t sx;
-  int32_t pad4;
+  // lin4: the FP32 vector passes give each task 64 consecutive quads of its z-slab's planes (the
+  // task's tile index j takes quads 64j..64j+63 of the plane, rows back to back) instead of its
+  // 8 x 8-quad tile; set where that packs the planes into clearly fewer thread slots
+  int32_t lin4;
 };
 
 // Per-instance mutable scalars (device memory).
@@ -185,6 +191,9 @@ struct DevArrays {
   const int8_t* task_heat;  // per task: some cell holds a heater
   const int4* tasks;        // (instance, x0, y0, z0) per task
   int64_t ncells, ntiles, ninst, ntasks;
+  int64_t nsmall;           // instances with at most kWarpSumMax tasks (their partials: one warp)
+  const int32_t* large;     // the other instances (block sums), nlarge of them
+  int64_t nlarge;
 };
 
 // Slots of DevArrays::stamps: step begin, RHS start, RHS finalize start, solve start, end of the

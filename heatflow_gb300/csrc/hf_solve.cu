@@ -598,6 +598,36 @@ __device__ __forceinline__ void upd_task(const DevArrays& A, double* part, int64
 // cells plane by plane, the same way in both uses.
 __device__ __forceinline__ bool vec4_ok(const InstDesc& d) { return (d.nx & 3) == 0; }
 
+// The quad (4 consecutive x cells) of thread w (0..63) of a z-group.  Tile form: 8 quads x 8 rows
+// of the task's tile.  Linear form (FP32 passes of lin4 instances): quad 64j + w of the plane,
+// j = the task's tile index in its z-slab, rows back to back (rows of sx = 4k cells).  west_lane /
+// east_lane: the neighbouring quad in memory is not in the adjacent lane of this warp.
+struct QuadPos {
+  int x, y;
+  bool act, west_lane, east_lane;
+};
+template <bool LIN_OK>
+__device__ __forceinline__ QuadPos quad_pos(const int4& tk, const InstDesc& d, int w) {
+  QuadPos p;
+  if (LIN_OK && d.lin4) {
+    const int qrow = d.sx >> 2;
+    const int j = (tk.z / kTY) * ((d.nx + kTX - 1) / kTX) + tk.y / kTX;
+    const int g = j * 64 + w;
+    p.act = g < qrow * d.ny;
+    p.y = g / qrow;
+    p.x = (g - p.y * qrow) * 4;
+    p.west_lane = (w & 31) == 0;
+    p.east_lane = (w & 31) == 31;
+  } else {
+    p.x = tk.y + 4 * (w & 7);
+    p.y = tk.z + (w >> 3);
+    p.act = p.x < d.nx && p.y < d.ny;
+    p.west_lane = (w & 7) == 0;
+    p.east_lane = (w & 7) == 7;
+  }
+  return p;
+}
+
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 
 __device__ __forceinline__ void st4(float* p, const float4& v) { *reinterpret_cast<float4*>(p) = v; }
@@ -612,12 +642,13 @@ __device__ __forceinline__ void spmv4_task(const DevArrays& A, double* part, int
   const InstDesc& d = A.inst[tk.x];
   const int nx = d.nx, ny = d.ny, nz = d.nz, sx = d.sx, nxy = sx * ny;
   const int64_t off = d.off4;
-  const int tid = threadIdx.x, grp = tid >> 6, w = tid & 63, row = w >> 3, q = w & 7;
-  const int x = tk.y + 4 * q, y = tk.z + row;
+  const int tid = threadIdx.x, grp = tid >> 6, w = tid & 63;
+  const QuadPos qp = quad_pos<true>(tk, d, w);
+  const int x = qp.x, y = qp.y;
   const int z0 = tk.w, z1 = min(z0 + d.zc, nz);
   const int per = (z1 - z0 + 3) >> 2;
   const int za = min(z0 + grp * per, z1), zb = min(za + per, z1);
-  const bool act = x < nx && y < ny;
+  const bool act = qp.act;
   const int last = min(3, nx - 1 - x);   // the quad's last grid cell; cells past it are padding
   const int64_t k = s.iter;
   const bool first = !FUSED || k == 0;
@@ -637,8 +668,8 @@ __device__ __forceinline__ void spmv4_task(const DevArrays& A, double* part, int
     if (y + 1 < ny) { dn = sx; hn = true; } else if (d.py) { dn = -(ny - 1) * sx; hn = true; }
     if (y > 0) { ds = -sx; hs = true; } else if (d.py) { ds = (ny - 1) * sx; hs = true; }
   }
-  const bool wload = (q == 0 || x == 0);          // west of cell 0 is loaded, not shuffled
-  const bool eload = (q == 7 || x + 4 >= nx);     // east of the last cell is loaded, not shuffled
+  const bool wload = (qp.west_lane || x == 0);     // west of cell 0 is loaded, not shuffled
+  const bool eload = (qp.east_lane || x + 4 >= nx); // east of the last cell is loaded, not shuffled
   bool hw = false, he = false;
   int dw = 0, de = 0;
   if (x > 0) { dw = -1; hw = true; } else if (d.px && nx > 1) { dw = nx - 1; hw = true; }
@@ -773,7 +804,8 @@ __device__ __forceinline__ Quad quad_cell(const DevArrays& A, int64_t task) {
   const int4 tk = A.tasks[task];
   const InstDesc& d = A.inst[tk.x];
   const int tid = threadIdx.x, grp = tid >> 6, w = tid & 63;
-  const int x = tk.y + 4 * (w & 7), y = tk.z + (w >> 3);
+  const QuadPos qp = quad_pos<F32>(tk, d, w);
+  const int x = qp.x, y = qp.y;
   const int z1 = min(tk.w + d.zc, d.nz);
   const int per = (z1 - tk.w + 3) >> 2;
   const int sx = F32 ? d.sx : d.nx;
@@ -789,7 +821,7 @@ __device__ __forceinline__ Quad quad_cell(const DevArrays& A, int64_t task) {
   c.padded = sx != d.nx;
   c.za = min(tk.w + grp * per, z1);
   c.zb = min(c.za + per, z1);
-  c.act = x < d.nx && y < d.ny;
+  c.act = qp.act;
   return c;
 }
 
@@ -1021,7 +1053,6 @@ __global__ void __launch_bounds__(kBlock) k_cg_upd(DevArrays A) {
 // kWarpSumMax tasks the whole block sums (thread-strided, then block_sum), otherwise warp 0 sums
 // (lane-strided, then a shuffle tree).  The result is valid in thread 0.  Partials are read
 // through L2 (written by other blocks of the same persistent launch).
-constexpr int kWarpSumMax = 512;
 template <int NRV>
 __device__ __forceinline__ void warp_instance_sum(const double* part, const InstDesc& d, int lane,
                                                   double (&acc)[NRV]) {
@@ -1375,27 +1406,62 @@ __device__ int instance_epilogue(const DevArrays& A, int64_t inst, const double 
 }
 
 // Epilogues of all instances (the whole last-arriving block).  Large instances (block sums) one
-// after the other, small ones one per warp.  Returns (in every thread) whether any has work left.
+// after the other.  Small ones kBlock at a time: each warp sums the partials of its instances
+// (per instance exactly warp_instance_sum's order, as in the finalize kernels), kEpiUnroll
+// instances' loads in flight at once, into shared memory; then one thread per instance runs the
+// epilogues side by side (with many instances, one lane running them in turn set the round's
+// length).  Returns (in every thread) whether any instance has work left.
+constexpr int kEpiUnroll = 4;
+constexpr int kPhaseCache = 1024;   // instances whose phases a solve block keeps in shared memory
 template <typename T>
 __device__ int all_epilogues(const DevArrays& A, double* red) {
+  __shared__ double s_acc[kBlock][2];
+  __shared__ int32_t s_ph[kBlock];
   int act = 0;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int64_t i = 0; i < A.ninst; ++i) {
+  for (int64_t k = 0; k < A.nlarge; ++k) {     // a list: no serial walk over every instance
+    const int64_t i = A.large[k];
     const InstDesc& d = A.inst[i];
-    if (d.ntask <= kWarpSumMax) continue;
     const int32_t ph = __ldcg(&A.scal[i].phase);
     double acc[2] = {0.0, 0.0};
     if (phase_partials(ph) > 0) instance_sum<2>(A.partials, d, acc, red);
     if (threadIdx.x == 0) act |= instance_epilogue<T>(A, i, acc);
     __syncthreads();
   }
-  for (int64_t i = warp; i < A.ninst; i += kBlock / 32) {
-    const InstDesc& d = A.inst[i];
-    if (d.ntask > kWarpSumMax) continue;
-    const int32_t ph = __ldcg(&A.scal[i].phase);
-    double acc[2] = {0.0, 0.0};
-    if (phase_partials(ph) > 0) warp_instance_sum<2>(A.partials, d, lane, acc);
-    if (lane == 0) act |= instance_epilogue<T>(A, i, acc);
+  for (int64_t base = 0; A.nsmall > 0 && base < A.ninst; base += kBlock) {
+    const int nb = (int)(A.ninst - base < kBlock ? A.ninst - base : kBlock);
+    if ((int)threadIdx.x < nb) s_ph[threadIdx.x] = __ldcg(&A.scal[base + threadIdx.x].phase);
+    __syncthreads();
+    for (int j0 = warp * kEpiUnroll; j0 < nb; j0 += (kBlock / 32) * kEpiUnroll) {
+      double acc[kEpiUnroll][2];
+#pragma unroll
+      for (int u = 0; u < kEpiUnroll; ++u) {
+        acc[u][0] = 0.0;
+        acc[u][1] = 0.0;
+        const int j = j0 + u;
+        if (j >= nb) continue;
+        const InstDesc& d = A.inst[base + j];
+        if (d.ntask > kWarpSumMax || phase_partials(s_ph[j]) == 0) continue;
+        for (int64_t t = lane; t < d.ntask; t += 32) {
+          acc[u][0] += __ldcg(&A.partials[(d.task0 + t) * kNR + 0]);
+          acc[u][1] += __ldcg(&A.partials[(d.task0 + t) * kNR + 1]);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kEpiUnroll; ++u) {
+        const double v0 = warp_sum(acc[u][0]), v1 = warp_sum(acc[u][1]);
+        if (lane == 0 && j0 + u < nb) {
+          s_acc[j0 + u][0] = v0;
+          s_acc[j0 + u][1] = v1;
+        }
+      }
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < nb && A.inst[base + threadIdx.x].ntask <= kWarpSumMax) {
+      const double acc[2] = {s_acc[threadIdx.x][0], s_acc[threadIdx.x][1]};
+      act |= instance_epilogue<T>(A, base + threadIdx.x, acc);
+    }
+    __syncthreads();
   }
   return __syncthreads_or(act);
 }
@@ -1490,8 +1556,12 @@ __global__ void __launch_bounds__(kBlock, 3)
     k_solve(DevArrays A, SolveCtl* ctl, int64_t limit, unsigned long long wait_ns, int leaver) {
   __shared__ InstScal sh;
   __shared__ double red[32 * 2];
+  __shared__ int32_t s_phase[kPhaseCache];
   const unsigned G = gridDim.x;
   const unsigned nt = (unsigned)A.ntasks;
+  // several instances: every round starts with all their phases in shared memory, so tasks of
+  // instances without work this round are passed over without reading their scalars
+  const bool cache = A.ninst > 1 && A.ninst <= kPhaseCache;
   if (blockIdx.x == 0 && threadIdx.x == 0) A.stamps[kStampSolve] = ctl->t_start = gtimer();
   for (int64_t r = 0;; ++r) {
     if (r >= limit) {
@@ -1501,10 +1571,15 @@ __global__ void __launch_bounds__(kBlock, 3)
     // odd rounds walk the tasks backwards, so a round starts on the data the previous round wrote
     // last, which is still in L2 (the partial sums have fixed slots: the order changes no bits)
     int cur = -1;
+    if (cache) {
+      for (int i = threadIdx.x; i < (int)A.ninst; i += kBlock) s_phase[i] = __ldcg(&A.scal[i].phase);
+      __syncthreads();
+    }
     const unsigned cnt = blockIdx.x < nt ? (nt - 1 - blockIdx.x) / G + 1 : 0u;
     for (unsigned k = 0; k < cnt; ++k) {
       const unsigned t = blockIdx.x + G * ((r & 1) ? cnt - 1 - k : k);
       const int inst = A.tasks[t].x;
+      if (cache && s_phase[inst] == PH_IDLE) continue;
       if (inst != cur) {                     // this instance's scalars, through L2
         __syncthreads();
         if ((int)threadIdx.x < kScalWords)
