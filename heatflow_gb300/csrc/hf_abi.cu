@@ -707,12 +707,6 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
     hoff += d.n;
     d.sx = (int32_t)((p.nx + 3) / 4 * 4);
     d.off4 = off4;
-    {
-      const int64_t slots_tile = (p.nx + kTX - 1) / kTX * kTX * ((p.ny + kTY - 1) / kTY * kTY);
-      const int64_t quads = (int64_t)d.sx / 4 * p.ny;            // quads per plane
-      const int64_t slots_lin = (quads + 63) / 64 * 256;
-      d.lin4 = 10 * slots_lin < 9 * slots_tile ? 1 : 0;
-    }
     const int64_t n4 = (int64_t)d.sx * p.ny * p.nz;
     off4 += (n4 + kTile - 1) / kTile * kTile;
     d.tile0 = tiles;

@@ -69,10 +69,7 @@ struct InstDesc {
   // 16-byte vector passes; instance at off4, a multiple of kTile cells.  sx = nx: the FP64 layout.
   int64_t off4;
   int32_t sx;
-  // lin4: the FP32 vector passes give each task 64 consecutive quads of its z-slab's planes (the
-  // task's tile index j takes quads 64j..64j+63 of the plane, rows back to back) instead of its
-  // 8 x 8-quad tile; set where that packs the planes into clearly fewer thread slots
-  int32_t lin4;
+  int32_t pad4;
 };
 
 // Per-instance mutable scalars (device memory).

@@ -598,33 +598,20 @@ __device__ __forceinline__ void upd_task(const DevArrays& A, double* part, int64
 // cells plane by plane, the same way in both uses.
 __device__ __forceinline__ bool vec4_ok(const InstDesc& d) { return (d.nx & 3) == 0; }
 
-// The quad (4 consecutive x cells) of thread w (0..63) of a z-group.  Tile form: 8 quads x 8 rows
-// of the task's tile.  Linear form (FP32 passes of lin4 instances): quad 64j + w of the plane,
-// j = the task's tile index in its z-slab, rows back to back (rows of sx = 4k cells).  west_lane /
-// east_lane: the neighbouring quad in memory is not in the adjacent lane of this warp.
+// The quad (4 consecutive x cells) of thread w (0..63) of a z-group: 8 quads x 8 rows of the
+// task's tile.  west_lane / east_lane: the neighbouring quad of the row is not in the adjacent
+// lane of this warp.
 struct QuadPos {
   int x, y;
   bool act, west_lane, east_lane;
 };
-template <bool LIN_OK>
 __device__ __forceinline__ QuadPos quad_pos(const int4& tk, const InstDesc& d, int w) {
   QuadPos p;
-  if (LIN_OK && d.lin4) {
-    const int qrow = d.sx >> 2;
-    const int j = (tk.z / kTY) * ((d.nx + kTX - 1) / kTX) + tk.y / kTX;
-    const int g = j * 64 + w;
-    p.act = g < qrow * d.ny;
-    p.y = g / qrow;
-    p.x = (g - p.y * qrow) * 4;
-    p.west_lane = (w & 31) == 0;
-    p.east_lane = (w & 31) == 31;
-  } else {
-    p.x = tk.y + 4 * (w & 7);
-    p.y = tk.z + (w >> 3);
-    p.act = p.x < d.nx && p.y < d.ny;
-    p.west_lane = (w & 7) == 0;
-    p.east_lane = (w & 7) == 7;
-  }
+  p.x = tk.y + 4 * (w & 7);
+  p.y = tk.z + (w >> 3);
+  p.act = p.x < d.nx && p.y < d.ny;
+  p.west_lane = (w & 7) == 0;
+  p.east_lane = (w & 7) == 7;
   return p;
 }
 
@@ -643,7 +630,7 @@ __device__ __forceinline__ void spmv4_task(const DevArrays& A, double* part, int
   const int nx = d.nx, ny = d.ny, nz = d.nz, sx = d.sx, nxy = sx * ny;
   const int64_t off = d.off4;
   const int tid = threadIdx.x, grp = tid >> 6, w = tid & 63;
-  const QuadPos qp = quad_pos<true>(tk, d, w);
+  const QuadPos qp = quad_pos(tk, d, w);
   const int x = qp.x, y = qp.y;
   const int z0 = tk.w, z1 = min(z0 + d.zc, nz);
   const int per = (z1 - z0 + 3) >> 2;
@@ -804,7 +791,7 @@ __device__ __forceinline__ Quad quad_cell(const DevArrays& A, int64_t task) {
   const int4 tk = A.tasks[task];
   const InstDesc& d = A.inst[tk.x];
   const int tid = threadIdx.x, grp = tid >> 6, w = tid & 63;
-  const QuadPos qp = quad_pos<F32>(tk, d, w);
+  const QuadPos qp = quad_pos(tk, d, w);
   const int x = qp.x, y = qp.y;
   const int z1 = min(tk.w + d.zc, d.nz);
   const int per = (z1 - tk.w + 3) >> 2;

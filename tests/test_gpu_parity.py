@@ -376,9 +376,7 @@ def test_vector_paths_match_oracle(cuda_lib, name, g):
 def _padded_cases():
     """Grids whose rows are not a multiple of 4 cells: the mixed path's FP32 vectors then carry
     padding cells (rows rounded up to 4), and a row's last quad holds 1, 2 or 3 grid cells, with
-    the periodic x wrap taken from a load.  The lin_* grids (and wide_37, px_wide_35) have planes
-    that the FP32 passes cover in runs of 64 consecutive quads rather than 8 x 8-quad tiles, so
-    rows straddle warps and x neighbours cross lanes 31 / 0 by loads."""
+    the periodic x wrap taken from a load; several grids are more than one tile wide."""
     c = {}
     c["px_5"] = _rng_problem(5, 4, 3, periodic=(1, 1, 0))         # 4k+1, x and y periodic
     c["px_6"] = _rng_problem(6, 3, 4, periodic=(1, 0, 1))         # 4k+2
@@ -390,8 +388,8 @@ def _padded_cases():
     c["heaters_5"] = _rng_problem(5, 5, 5, iheater=np.arange(125, dtype=np.int64) % 9 - 1,
                                   power_in=2e-6, freq=3.0e11, heated_steps=2, em=0.3, t_bath=280.0)
     c["single"] = _rng_problem(1, 1, 1)
-    c["lin_px_50"] = _rng_problem(50, 20, 6, periodic=(1, 1, 0))
-    c["lin_20"] = _rng_problem(20, 30, 5)                          # rows of 4k cells, linear quads
+    c["px_50"] = _rng_problem(50, 20, 6, periodic=(1, 1, 0))       # wrap across two tiles
+    c["rows_20"] = _rng_problem(20, 30, 5)                         # rows of 4k cells, no padding
     return c
 
 
