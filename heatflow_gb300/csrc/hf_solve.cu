@@ -245,6 +245,11 @@ __device__ __forceinline__ void res_hx_task(const DevArrays& A, double* part, in
   }
 }
 
+__device__ __forceinline__ bool vec4_ok(const InstDesc& d);
+template <typename TR>
+__device__ __forceinline__ void res_hx4_task(const DevArrays& A, double* part, int64_t task,
+                                             const InstScal& s);
+
 // FP64 true residual of one task: r = S - H x with x in the x-read buffer (INIT: x0 from the RHS
 // kernel) or, after an update, in the x-write buffer (the epilogue then swaps the roles).  Writes
 // g = -S^-1 r / sigma into the inner residual (type TR).  FP64 work per cell: 7 FMA for S - Hx,
@@ -253,7 +258,8 @@ template <bool INIT, typename TR>
 __device__ __forceinline__ void res_task(const DevArrays& A, double* part, int64_t task,
                                           const InstScal& s) {
   if (INIT && s.hx_ok >= 2) {
-    res_hx_task<TR>(A, part, task, s);
+    if (vec4_ok(A.inst[A.tasks[task].x])) res_hx4_task<TR>(A, part, task, s);
+    else res_hx_task<TR>(A, part, task, s);
     return;
   }
   const TCell c = task_cell(A, task);
@@ -959,6 +965,66 @@ __device__ __forceinline__ void xupd4_task(const DevArrays& A, double* part, int
       }
       stv4(XW + (h ? l1 : l0), xv);
     }
+  }
+}
+
+// The step's first residual from the stored products (res_hx_task) on 4-cell vectors, for rows of
+// 4k cells: the same per-cell arithmetic; ||r||^2 and ||g||^2 summed per thread plane by plane,
+// cells in x order.  A quarter of the scalar form's load instructions keeps more bytes in flight
+// on this FP64-bound round.
+template <typename TR>
+__device__ __forceinline__ void res_hx4_task(const DevArrays& A, double* part, int64_t task,
+                                             const InstScal& s) {
+  const Quad c = quad_cell<false>(A, task);   // rows of 4k cells: the two layouts agree in shape
+  const int64_t off = c.off;
+  const double* __restrict__ b = A.b + off;
+  const double* __restrict__ yc = A.hx[s.hx_role] + off;
+  const double* __restrict__ yp = A.hx[1 - s.hx_role] + off;
+  const double* __restrict__ rsum = A.rsum + off;
+  const float* __restrict__ sinv32 = A.sinv32 + off;
+  const double* __restrict__ sinv = A.sinv + off;
+  const bool f32 = sizeof(TR) == 4;
+  TR* R = Vec<TR>::r(A) + (f32 ? A.inst[A.tasks[task].x].off4 : off);
+  const float isig = (float)(1.0 / s.sigma);
+  const bool tiny = s.x0flag != 0;            // the residual of x0 + TINY: r(x0) - TINY * H1
+  double rr = 0.0, gg64 = 0.0;
+  float gg = 0.f;
+  if (c.act) {
+    for (int z = c.za; z < c.zb; ++z) {
+      const int l = c.lxy + z * c.nxy;
+      const V4<double> bv = ldv4(b + l), cv = ldv4(yc + l), pv = ldv4(yp + l);
+      V4<double> rs{}, s64{};
+      V4<float> s32{};
+      if (tiny) rs = ldv4(rsum + l);
+      if (f32) s32 = ldv4(sinv32 + l);
+      else s64 = ldv4(sinv + l);
+      V4<TR> g4;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        double a = fma(-2.0, cv.v[i], bv.v[i]);
+        a = a + pv.v[i];
+        if (tiny) a = fma(-kTiny, rs.v[i], a);
+        rr = fma(a, a, rr);
+        if (f32) {
+          const float g = -s32.v[i] * f64_to_f32_trunc(a) * isig;
+          g4.v[i] = (TR)g;
+          gg = fmaf(g, g, gg);
+        } else {
+          const double g = -s64.v[i] * a;
+          g4.v[i] = (TR)g;
+          gg64 = fma(g, g, gg64);
+        }
+      }
+      stv4(R + l, g4);
+    }
+  }
+  if (sizeof(TR) == 4) {
+    task_store_f(part + task * kNR, 1, gg);
+    const double v[1] = {rr};
+    tile_store<1>(part + task * kNR, v);
+  } else {
+    const double v[2] = {rr, gg64};
+    tile_store<2>(part + task * kNR, v);
   }
 }
 
