@@ -9,7 +9,7 @@ import numpy as np
 import pytest
 
 from heatflow_gb300 import abi
-from heatflow_gb300.problem import layered_slab, point_source_cube
+from heatflow_gb300.problem import layered_slab, point_source_cube, random_instance
 from heatflow_gb300.solver import HeatFlow
 
 pytestmark = pytest.mark.gpu
@@ -102,6 +102,32 @@ def test_async_batch_registered(cuda_lib):
     finally:
         for b in bufs:
             lib.hf_host_unregister(b.ctypes.data_as(C.c_void_p))
+
+
+@pytest.mark.parametrize("use_graph", [1, 3])
+def test_async_batch_many_chunks(cuda_lib, use_graph):
+    """Uneven grids whose z-slabs of tasks fill the 8 upload chunks unevenly: chunks that hold
+    several grids and a tall grid spread over several chunks.  Each chunk's RHS runs as it lands;
+    the result is the uninterrupted run's, bit for bit."""
+    rng = np.random.default_rng(11)
+    probs = [random_instance(rng, lo=6, hi=40) for _ in range(12)]
+    probs.append(layered_slab(40, nz=70, layer=7))
+    kw = dict(KW, use_graph=use_graph)
+    with HeatFlow(probs, **kw) as hf:
+        hf.initial_evolve()
+        hf.run(1, 2)
+        tp, tpp = hf.get_state()
+    with HeatFlow(probs, **kw) as hf:
+        hf.set_state(tp, tpp)
+        hf.run(3, 4)
+        T_ref, Tp_ref = hf.get_state()
+    bufs = [_pinned(tp.size, 0.0) for _ in range(3)]
+    bufs[0][:] = tp
+    bufs[1][:] = tpp
+    with HeatFlow(probs, **kw) as hf:
+        st, (cur, prev, _) = _run_async(hf, bufs, 3, 4)
+    assert st["unconverged"] == 0
+    assert np.array_equal(bufs[cur], T_ref) and np.array_equal(bufs[prev], Tp_ref)
 
 
 def test_pageable_arrays_refused(cuda_lib):
