@@ -130,6 +130,28 @@ def test_async_batch_many_chunks(cuda_lib, use_graph):
     assert np.array_equal(bufs[cur], T_ref) and np.array_equal(bufs[prev], Tp_ref)
 
 
+def test_async_nan_input_reported(cuda_lib):
+    """A NaN in the T^n handed to the second queued step: hf_host_sync reports the reference's
+    Cattaneo NaN error (mod_evolve.f90 stops there) and the state is left unrotated, as a
+    synchronous step leaves it."""
+    prob = point_source_cube(6, icattaneo=1)
+    tp, tpp = _initial(prob)
+    bufs = [_pinned(prob.ncells, 0.0) for _ in range(4)]
+    bufs[0][:] = tp
+    bufs[1][:] = tpp
+    bad = bufs[3]
+    bad[:] = tp
+    bad[7] = np.nan
+    with HeatFlow(prob, **KW) as hf:
+        hf.step_host_async(3, bufs[0], bufs[1], bufs[2])
+        hf.step_host_async(4, bad, bufs[2], bufs[1])
+        with pytest.raises(abi.HeatFlowError) as e:
+            hf.host_sync()
+        assert e.value.code == abi.HF_ENAN_SCAT
+        after, _ = hf.get_state()
+    assert np.isnan(after[7]) and np.isfinite(np.delete(after, 7)).all()
+
+
 def test_pageable_arrays_refused(cuda_lib):
     prob = point_source_cube(8)
     with HeatFlow(prob, **KW) as hf:
