@@ -144,6 +144,7 @@ struct SolveCtl {
   int32_t err;             // a barrier wait gave up (time limit): the launch was abandoned
   int32_t guard_hit;       // the round bound was reached
   int32_t pad;
+  unsigned next_task[2];   // tasks handed out in the current round (by round parity)
   int64_t rounds;          // rounds run
   unsigned long long t_start;                 // %globaltimer at kernel start (ns)
   unsigned long long t_round[kRoundLog];      // %globaltimer when round r's barrier opened

@@ -1546,6 +1546,7 @@ __device__ bool grid_barrier_epilogue(const DevArrays& A, SolveCtl* ctl, unsigne
     }
     const int act = all_epilogues<T>(A, red);
     if (threadIdx.x == 0) {
+      ctl->next_task[round & 1] = 0u;     // every block is done taking this round's tasks
       ctl->result[(g + 1) & 1] = act ? 1u : 0u;
       const unsigned long long t = gtimer();
       if (round < kRoundLog) ctl->t_round[round] = t;
@@ -1610,6 +1611,7 @@ __global__ void __launch_bounds__(kBlock, 3)
   __shared__ InstScal sh;
   __shared__ double red[32 * 2];
   __shared__ int32_t s_phase[kPhaseCache];
+  __shared__ unsigned s_next;
   const unsigned G = gridDim.x;
   const unsigned nt = (unsigned)A.ntasks;
   // several instances: every round starts with all their phases in shared memory, so tasks of
@@ -1626,22 +1628,31 @@ __global__ void __launch_bounds__(kBlock, 3)
     int cur = -1;
     if (cache) {
       for (int i = threadIdx.x; i < (int)A.ninst; i += kBlock) s_phase[i] = __ldcg(&A.scal[i].phase);
-      __syncthreads();
     }
-    const unsigned cnt = blockIdx.x < nt ? (nt - 1 - blockIdx.x) / G + 1 : 0u;
-    for (unsigned k = 0; k < cnt; ++k) {
-      const unsigned t = blockIdx.x + G * ((r & 1) ? cnt - 1 - k : k);
+    // tasks are handed out one at a time from a counter, so a block on a busier SM takes fewer
+    // (every SM holds the same number of blocks, but a round lasts as long as its slowest SM);
+    // each block asks for its next task while it runs the current one
+    if (threadIdx.x == 0) s_next = atomicAdd(&ctl->next_task[r & 1], 1u);
+    __syncthreads();
+    for (unsigned k = s_next; k < nt;) {
+      __syncthreads();                       // every thread has read s_next
+      if (threadIdx.x == 0) s_next = atomicAdd(&ctl->next_task[r & 1], 1u);
+      const unsigned t = (r & 1) ? nt - 1 - k : k;
       const int inst = A.tasks[t].x;
-      if (cache && s_phase[inst] == PH_IDLE) continue;
-      if (inst != cur) {                     // this instance's scalars, through L2
-        __syncthreads();
-        if ((int)threadIdx.x < kScalWords)
-          reinterpret_cast<unsigned long long*>(&sh)[threadIdx.x] =
-              __ldcg(reinterpret_cast<const unsigned long long*>(A.scal + inst) + threadIdx.x);
-        __syncthreads();
-        cur = inst;
+      const bool skip = cache && s_phase[inst] == PH_IDLE;
+      if (!skip) {
+        if (inst != cur) {                   // this instance's scalars, through L2
+          __syncthreads();
+          if ((int)threadIdx.x < kScalWords)
+            reinterpret_cast<unsigned long long*>(&sh)[threadIdx.x] =
+                __ldcg(reinterpret_cast<const unsigned long long*>(A.scal + inst) + threadIdx.x);
+          __syncthreads();
+          cur = inst;
+        }
+        if (sh.phase != PH_IDLE) round_task<T>(A, A.partials, t, sh);
       }
-      if (sh.phase != PH_IDLE) round_task<T>(A, A.partials, t, sh);
+      __syncthreads();                       // s_next holds the block's next task
+      k = s_next;
     }
     unsigned any = 0;
     // failure-path check only (leaver >= 0): that block leaves without arriving, so the others'
@@ -1661,13 +1672,11 @@ int solve_grid_blocks(Ctx& c, int fp32) {
                        : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve<double>, kBlock, 0);
   if (e != cudaSuccess) return -1;
   if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c.device) != cudaSuccess) return -1;
+  // every SM holds the same number of blocks; tasks are handed out one at a time, so the blocks
+  // of busier SMs take fewer of them
   int64_t g = (int64_t)per_sm * nsm;
   if (g > c.ntasks) g = c.ntasks;
   if (g < 1) return -1;
-  // every round lasts as long as the busiest block: with r = ceil(tasks / grid) tasks on some
-  // block, a grid of ceil(tasks / r) blocks has the same r and no partly idle blocks
-  const int64_t r = (c.ntasks + g - 1) / g;
-  g = (c.ntasks + r - 1) / r;
   cached = (int)g;
   return cached;
 }
