@@ -34,7 +34,7 @@ constexpr int kNR = 8;
 // instance (one warp per row; lane L holds columns x0 + L + 32 j, j < kXC) and marches the task
 // depth (InstDesc::zc planes, an option; kZC by default) along z.  (kXC > 1 trades occupancy for
 // per-thread parallelism; on GB300 kXC = 1 is faster.)
-constexpr int kXC = 1, kTX = 32 * kXC, kTY = 8, kZC = 16;
+constexpr int kXC = 1, kTX = 32 * kXC, kTY = 8, kZC = 32;
 // Instances with more tasks than this have their task partials summed by a whole block, the
 // others by one warp.
 constexpr int kWarpSumMax = 512;
