@@ -176,9 +176,16 @@ int validate_opts(const hf_solver_opts& o) {
   return HF_OK;
 }
 
+// Calls that read or change a context's device state while host-buffer steps are queued
+// (hf_step_host_async) are refused until hf_host_sync has collected them.
+int refuse_queued(const Ctx& c) {
+  return c.async_pending
+             ? set_err(HF_ESTATE, "host-buffer steps are queued: call hf_host_sync first")
+             : HF_OK;
+}
+
 int sync_scal(Ctx& c) {
-  if (c.async_pending)
-    return set_err(HF_ESTATE, "host-buffer steps are queued: call hf_host_sync first");
+  if (int r = refuse_queued(c)) return r;
   CU(cudaMemcpyAsync(c.h_scal, c.A.scal, sizeof(InstScal) * c.ninst, cudaMemcpyDeviceToHost,
                      c.stream));
   CU(cudaStreamSynchronize(c.stream));
@@ -975,6 +982,7 @@ int64_t hf_instance_cells(const hf_ctx* h, int64_t i) {
 int hf_set_stream(hf_ctx* h, void* stream) {
   if (!h) return set_err(HF_EARG, "null context");
   Ctx& c = h->c;
+  if (int r_ = refuse_queued(c)) return r_;
   CU(cudaStreamSynchronize(c.stream));
   if (stream) {
     if (c.own_stream) cudaStreamDestroy(c.stream);
@@ -1294,6 +1302,7 @@ int hf_set_property_tables(hf_ctx* h, int32_t ntables, const int32_t* offsets, c
   if (!h || ntables < 0 || (ntables > 0 && (!offsets || !rows || !cell_table)))
     return set_err(HF_EARG, "bad arguments");
   Ctx& c = h->c;
+  if (int r_ = refuse_queued(c)) return r_;
   if (ntables == 0) {                         // back to fixed properties
     c.tempdep = false;
     drop_graph(c);
@@ -1353,6 +1362,7 @@ int hf_subbox_async(hf_ctx* h, int64_t inst, const int64_t* lo, const int64_t* h
   if (!h || !lo || !hi || !host || !ticket || (which != 0 && which != 1))
     return set_err(HF_EARG, "bad arguments");
   Ctx& c = h->c;
+  if (int r_ = refuse_queued(c)) return r_;
   if (inst < 0 || inst >= c.ninst) return set_err(HF_EARG, "instance out of range");
   const InstDesc& d = c.h_inst[inst];
   const int64_t dims[3] = {d.nx, d.ny, d.nz};
@@ -1568,6 +1578,7 @@ int hf_check_barrier_timeout(hf_ctx* h, int32_t wait_ms, int32_t* status, double
 int hf_step_timeline(hf_ctx* h, double* us) {
   if (!h || !us) return set_err(HF_EARG, "null argument");
   Ctx& c = h->c;
+  if (int r_ = refuse_queued(c)) return r_;
   unsigned long long t[kStamps];
   CU(cudaStreamSynchronize(c.stream));
   CU(cudaMemcpy(t, c.A.stamps, sizeof(t), cudaMemcpyDeviceToHost));
@@ -1583,6 +1594,7 @@ int hf_solve_profile(hf_ctx* h, int64_t cap, int64_t* rounds, int32_t* phases, d
   if (!h || !rounds || cap < 0 || (cap > 0 && (!phases || !round_us)))
     return set_err(HF_EARG, "bad arguments");
   Ctx& c = h->c;
+  if (int r_ = refuse_queued(c)) return r_;
   SolveCtl sc;
   CU(cudaStreamSynchronize(c.stream));
   CU(cudaMemcpy(&sc, c.d_sctl, sizeof(sc), cudaMemcpyDeviceToHost));
@@ -1646,6 +1658,7 @@ int hf_time_kernel(hf_ctx* h, int which, int reps, double* ms) {
 int hf_get_operator(hf_ctx* h, double* diag, double* cx, double* cy, double* cz) {
   if (!h) return set_err(HF_EARG, "null context");
   Ctx& c = h->c;
+  if (int r_ = refuse_queued(c)) return r_;
   int rc;
   if (diag && (rc = download_padded(c, diag, c.A.diag))) return rc;
   if (cx && (rc = download_padded(c, cx, c.A.cx))) return rc;
@@ -1658,6 +1671,7 @@ int hf_get_operator(hf_ctx* h, double* diag, double* cx, double* cy, double* cz)
 int hf_apply_operator(hf_ctx* h, const double* x, double* y) {
   if (!h || !x || !y) return set_err(HF_EARG, "null argument");
   Ctx& c = h->c;
+  if (int r_ = refuse_queued(c)) return r_;
   int rc;
   if ((rc = upload_padded(c, c.A.p, x))) return rc;   // p and q are free outside a step
   CU(launch_apply(c, c.A.p, c.A.q));
@@ -1827,6 +1841,7 @@ int hf_solve_device(hf_ctx* h, const double* b, double* x, hf_stats* stats) {
 int hf_adjoint_rhs(hf_ctx* h, const double* g, const double* l1, const double* l2, double* out) {
   if (!h || !g || !l1 || !l2 || !out) return set_err(HF_EARG, "null argument");
   Ctx& c = h->c;
+  if (int r_ = refuse_queued(c)) return r_;
   if (c.ninst != 1) return set_err(HF_EARG, "the adjoint takes single-grid contexts");
   CU(launch_adj_rhs(c, g, l1, l2, out));
   CU(cudaStreamSynchronize(c.stream));
@@ -1837,6 +1852,7 @@ int hf_adjoint_accumulate(hf_ctx* h, const double* lam, const double* x, int64_t
                           double* grad_logk, double* grad_src) {
   if (!h || !lam || !x || !grad_logk) return set_err(HF_EARG, "null argument");
   Ctx& c = h->c;
+  if (int r_ = refuse_queued(c)) return r_;
   if (c.ninst != 1) return set_err(HF_EARG, "the adjoint takes single-grid contexts");
   for (int f = 0; f < 6; ++f)
     if (c.h_bc[0].cg[f]) return set_err(HF_EARG, "the adjoint does not differentiate Neumann (CG) faces");
@@ -1850,6 +1866,7 @@ int hf_assemble_coo(hf_ctx* h, int64_t inst, int64_t cap, int64_t* irow, int64_t
                     int64_t* len, int64_t* count) {
   if (!h) return set_err(HF_EARG, "null context");
   Ctx& c = h->c;
+  if (int r_ = refuse_queued(c)) return r_;
   if (inst < 0 || inst >= c.ninst) return set_err(HF_EARG, "instance out of range");
   const InstDesc& d = c.h_inst[inst];
   const int64_t nx = d.nx, ny = d.ny, nz = d.nz;

@@ -166,9 +166,12 @@ def test_calls_refused_while_queued(cuda_lib):
     bufs = [_pinned(prob.ncells, 300.0) for _ in range(3)]
     with HeatFlow(prob, **KW) as hf:
         hf.step_host_async(1, bufs[0], bufs[1], bufs[2])
-        with pytest.raises(abi.HeatFlowError) as e:
-            hf.get_state()
-        assert e.value.code == abi.HF_ESTATE
+        table = np.array([[250.0, 100.0, 2000.0, 700.0], [350.0, 120.0, 2000.0, 700.0]])
+        for call in (hf.get_state, hf.operator, hf.step_timeline, hf.solve_profile,
+                     lambda: hf.set_property_tables([table], np.zeros(prob.ncells, np.int32))):
+            with pytest.raises(abi.HeatFlowError) as e:
+                call()
+            assert e.value.code == abi.HF_ESTATE
         st = hf.host_sync()
         assert st["steps"] == 1
         T, Tp = hf.get_state()
