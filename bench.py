@@ -147,6 +147,47 @@ def solve_floor(rounds, precision, N, hbm_gbs, fp64_tflops):
                     "FP64 rate), summed over the launch's rounds"}
 
 
+def phase_table(rounds, precision, N):
+    """Per phase of one persistent-solve launch: rounds, microseconds, upper GB/s (full bytes)."""
+    out = {}
+    for ph, us in rounds:
+        e = out.setdefault(ph, {"rounds": 0, "us": 0.0})
+        e["rounds"] += 1
+        e["us"] += us
+    for ph, e in out.items():
+        full, _ = PHASE_BYTES[precision].get(ph, (0, 0))
+        e["us_per_round"] = e["us"] / e["rounds"]
+        e["GB/s_upper"] = full * N / (e["us_per_round"] * 1e-6) / 1e9 if full else None
+    return out
+
+
+def kernel_table(kms, N, peak, fp_rates):
+    """Standalone kernel times -> GB/s, fraction of HBM and, for the FP64-pipe kernels, TFLOP/s."""
+    out = {}
+    for k, v in kms.items():
+        gbs = BYTES_PER_CELL[k] * N / (v / 1000.0) / 1e9
+        e = {"ms": v, "GB/s": gbs, "frac": gbs / peak}
+        if fp_rates and k in FP64_FLOPS_PER_CELL:
+            tf = FP64_FLOPS_PER_CELL[k] * N / (v / 1000.0) / 1e12
+            e["fp64_tflops"] = tf
+            e["fp64_frac"] = tf / fp_rates["fp64_tflops"]
+        out[k] = e
+    return out
+
+
+def compact(obj, digits=5):
+    """Floats rounded to `digits` significant digits (the line stays short enough to be kept whole)."""
+    if isinstance(obj, float):
+        if obj != obj or obj in (float("inf"), float("-inf")) or obj == 0.0:
+            return obj
+        return float(f"{obj:.{digits}g}")
+    if isinstance(obj, dict):
+        return {k: compact(v, digits) for k, v in obj.items()}
+    if isinstance(obj, (list, tuple)):
+        return [compact(v, digits) for v in obj]
+    return obj
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -169,6 +210,8 @@ def parse():
                          "see the kernels)")
     ap.add_argument("--host-loop", action="store_true",
                     help="drive the solve loop from the host instead of the captured graph")
+    ap.add_argument("--detail", default=None,
+                    help="also write per-phase and standalone-kernel timings to this JSON file")
     ap.add_argument("--cpu-seconds", type=float, default=90.0,
                     help="wall-clock bound of the reference arm's timed steps")
     return ap.parse_args()
@@ -327,9 +370,9 @@ def cpu_clean_pcg(prob, steps_cap: int, seconds: float, tol: float):
     ms = 1000.0 * float(np.mean(times)) if times else float("nan")
     return {"value": 1000.0 / ms, "unit": UNIT, "cores": cores, "kind": "clean CPU solver",
             "ms_per_step": ms, "steps_timed": len(times), "cg_iters_per_step": iters,
-            "sample": f"{len(times)} step(s) of the same {prob.nx}^3 workload after one untimed: "
-                      f"7-point stencil Jacobi-PCG in FP64 to true rel-res {tol:g}, OpenMP "
-                      f"{cores} threads (oracle/cpu_pcg.c; not the reference's algorithm)"}
+            "sample": f"{len(times)} step(s) of the {prob.nx}^3 workload after one untimed: "
+                      f"stencil Jacobi-PCG, FP64, true rel-res {tol:g}, {cores} threads "
+                      f"(oracle/cpu_pcg.c, not the reference's algorithm)"}
 
 
 def run_reference(args, rank, world):
@@ -350,7 +393,7 @@ def run_reference(args, rank, world):
         "notes": "reference Fortran not buildable on either machine (no Fortran compiler); "
                  "the oracle port restates it statement by statement",
     }
-    print(json.dumps(line), flush=True)
+    print(json.dumps(compact(line), separators=(",", ":")), flush=True)
     return 0
 
 
@@ -482,31 +525,14 @@ def main():
     cell_iters_per_s = world * cell_iters / (ms / 1000.0)
 
     # ---- kernel roofline.  The dominant kernel is the persistent solve (k_solve: the whole
-    # refinement loop of a step in one cooperative launch); it and the RHS kernel are timed alone
-    # with CUDA events on the library's stream.  The solve's algorithmic bytes come from the phase
-    # of every grid-wide round of the timed launches (the kernel's own round log).
+    # refinement loop of a step in one cooperative launch); it is timed alone with CUDA events on
+    # the library's stream.  Its algorithmic bytes come from the phase of every grid-wide round of
+    # the timed launches (the kernel's own round log).
     peak, peak_kind = measured_peak()
     prec = "mixed"
     solve_ms = hf.time_kernel(abi.HF_KERNEL_SOLVE, reps=10)
     rounds, nrounds = hf.solve_profile()
     solve_bpc = solve_bytes_per_cell(rounds, prec)
-    rhs_ms = hf.time_kernel(abi.HF_KERNEL_RHS, reps=10)
-    phases = {}
-    for ph, us in rounds:
-        e = phases.setdefault(ph, {"rounds": 0, "us": 0.0})
-        e["rounds"] += 1
-        e["us"] += us
-    for ph, e in phases.items():
-        full, alt = PHASE_BYTES[prec].get(ph, (0, 0))
-        e["us_per_round"] = e["us"] / e["rounds"]
-        e["GB/s_upper"] = full * N / (e["us_per_round"] * 1e-6) / 1e9 if full else None
-    kernels = {"cg_p_fp32": abi.HF_KERNEL_CG_P, "cg_spmv_fp32": abi.HF_KERNEL_CG_SPMV,
-               "cg_pq_fp32": abi.HF_KERNEL_CG_PQ, "cg_update_fp32": abi.HF_KERNEL_CG_UPDATE,
-               "xupdate_mixed": abi.HF_KERNEL_XUPDATE,
-               "residual_init_hx_mixed": abi.HF_KERNEL_RESIDUAL_INIT,   # before the sweep below,
-               "residual_mixed": abi.HF_KERNEL_RESIDUAL}                # which rewrites H x
-    kms = {name: hf.time_kernel(k, reps=10) for name, k in kernels.items()}
-    kms["rhs"] = rhs_ms
     f64 = C.c_double()
     f32 = C.c_double()
     rc = abi.load_library().hf_measure_fp_rates(C.byref(f64), C.byref(f32))
@@ -517,24 +543,31 @@ def main():
                 "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_kind": f"of {peak_kind}",
                 "traffic": ratio * solve_bpc * N if ratio else None,
-                "traffic_source": "ncu DRAM read+write per algorithmic byte of the k_solve launches "
-                                  "this bench times (256^3, profiles/solve_kernel_layered_slab_"
-                                  "256cube_dram.md), times this launch's algorithmic bytes",
+                "traffic_source": "ncu DRAM read+write per algorithmic byte (profiles/solve_kernel_"
+                                  "layered_slab_256cube_dram.md) x this launch's algorithmic bytes",
                 "algorithmic_bytes_per_launch": solve_bpc * N, "ms_per_launch": solve_ms,
-                "rounds_per_launch": nrounds, "share_of_step": solve_ms / (ms / K),
-                "phases": phases,
-                "kernels": {k: {"ms": kms[k], "GB/s": BYTES_PER_CELL[k] * N / (kms[k] / 1000.0) / 1e9,
-                                "frac": BYTES_PER_CELL[k] * N / (kms[k] / 1000.0) / 1e9 / peak}
-                            for k in kms},
-                "note": "phases' GB/s_upper assume every round of that phase moved its full bytes; "
-                        "standalone kernels are timed repeatedly on the same data (partly L2-resident)"}
+                "rounds_per_launch": nrounds, "share_of_step": solve_ms / (ms / K)}
+    rhs_ms = hf.time_kernel(abi.HF_KERNEL_RHS, reps=10)
+    roofline["k_rhs"] = {"ms": rhs_ms, "GB/s": BYTES_PER_CELL["rhs"] * N / (rhs_ms / 1000.0) / 1e9,
+                         "share_of_step": rhs_ms / (ms / K)}
+    detail = {"phases": phase_table(rounds, prec, N)}
     if fp_rates:
-        roofline["combined"] = solve_floor(rounds, prec, N, peak, fp_rates["fp64_tflops"])
-        roofline["fp64"] = {
-            k: {"achieved_tflops": FP64_FLOPS_PER_CELL[k] * N / (kms[k] / 1000.0) / 1e12,
-                "peak_tflops": fp_rates["fp64_tflops"],
-                "frac": FP64_FLOPS_PER_CELL[k] * N / (kms[k] / 1000.0) / 1e12 / fp_rates["fp64_tflops"]}
-            for k in kms if k in FP64_FLOPS_PER_CELL}
+        comb = solve_floor(rounds, prec, N, peak, fp_rates["fp64_tflops"])
+        roofline["combined"] = {"floor_us": comb["floor_us"], "us": comb["us"], "frac": comb["frac"],
+                                "by_phase": {ph: [e["us"], e["frac"], e["bound"]]
+                                             for ph, e in comb["by_phase"].items()},
+                                "note": "per round max(bytes / measured HBM, FP64 instructions / "
+                                        "measured FP64 rate); by_phase: [us, frac, bound]"}
+    if args.detail:
+        # standalone kernels (timed repeatedly on the same data, partly L2-resident)
+        kernels = {"cg_p_fp32": abi.HF_KERNEL_CG_P, "cg_spmv_fp32": abi.HF_KERNEL_CG_SPMV,
+                   "cg_pq_fp32": abi.HF_KERNEL_CG_PQ, "cg_update_fp32": abi.HF_KERNEL_CG_UPDATE,
+                   "xupdate_mixed": abi.HF_KERNEL_XUPDATE,
+                   "residual_init_hx_mixed": abi.HF_KERNEL_RESIDUAL_INIT,   # before the sweep
+                   "residual_mixed": abi.HF_KERNEL_RESIDUAL}                # that rewrites H x
+        kms = {name: hf.time_kernel(k, reps=10) for name, k in kernels.items()}
+        kms["rhs"] = rhs_ms
+        detail["kernels"] = kernel_table(kms, N, peak, fp_rates)
     hf.close()
 
     # ---- plain FP64 GPU path at the same residual
@@ -554,19 +587,20 @@ def main():
         ms64 = max_over_ranks(ms64)
         solve64 = h2.time_kernel(abi.HF_KERNEL_SOLVE, 10)
         r64, n64 = h2.solve_profile()
-        k64 = {"residual_fp64": h2.time_kernel(abi.HF_KERNEL_RESIDUAL, 10),
-               "xupdate_fp64": h2.time_kernel(abi.HF_KERNEL_XUPDATE, 10),
-               "cg_spmv_fp64": h2.time_kernel(abi.HF_KERNEL_CG_SPMV, 10),
-               "cg_update_fp64": h2.time_kernel(abi.HF_KERNEL_CG_UPDATE, 10),
-               "cg_p_fp64": h2.time_kernel(abi.HF_KERNEL_CG_P, 10)}
         fp64 = {"steps_per_s": aggregate_rate(world, K, ms64), "ms_per_step": ms64 / K,
                 "iterations_per_step": st64["iterations"] / K,
                 "refinements_per_step": st64["refinements"] / K,
                 "last_true_relres": st64["last_true_relres"],
-                "solve": {"ms": solve64, "rounds": n64,
-                          "GB/s": solve_bytes_per_cell(r64, "fp64") * N / (solve64 / 1000.0) / 1e9},
-                "kernels": {k: {"ms": v, "GB/s": BYTES_PER_CELL[k] * N / (v / 1000.0) / 1e9}
-                            for k, v in k64.items()}}
+                "solve_ms": solve64, "solve_rounds": n64,
+                "solve_GB/s": solve_bytes_per_cell(r64, "fp64") * N / (solve64 / 1000.0) / 1e9}
+        if args.detail:
+            k64 = {"residual_fp64": h2.time_kernel(abi.HF_KERNEL_RESIDUAL, 10),
+                   "xupdate_fp64": h2.time_kernel(abi.HF_KERNEL_XUPDATE, 10),
+                   "cg_spmv_fp64": h2.time_kernel(abi.HF_KERNEL_CG_SPMV, 10),
+                   "cg_update_fp64": h2.time_kernel(abi.HF_KERNEL_CG_UPDATE, 10),
+                   "cg_p_fp64": h2.time_kernel(abi.HF_KERNEL_CG_P, 10)}
+            detail["fp64_kernels"] = kernel_table(k64, N, peak, fp_rates)
+            detail["fp64_phases"] = phase_table(r64, "fp64", N)
         h2.close()
 
     # ---- end to end through the C ABI with host buffers
@@ -605,14 +639,10 @@ def main():
         sync_s = max_over_ranks(time.perf_counter() - t0)
         e2e = {"value": world * K / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 2 * 8 * N,
                "d2h_bytes_per_step": 8 * N,
-               "timing": "wall clock over K steps queued through hf_step_host_async (every step "
-                         "uploads T^n and T^(n-1) from pinned memory and downloads the new T^n "
-                         "into pinned memory; T^(n-1)'s upload overlaps the previous step's "
-                         "solve, T^n moves in chunks behind the previous step's download and "
-                         "each chunk's RHS runs as it lands), ended by hf_host_sync",
+               "timing": "wall clock, K steps through hf_step_host_async from/to pinned host "
+                         "memory (T^n, T^(n-1) up, new T^n down every step), then hf_host_sync",
                "sync_value": world * K / sync_s,
-               "sync_timing": "host-synchronous calls per step: hf_set_state, hf_step, "
-                              "hf_get_state"}
+               "sync_timing": "hf_set_state + hf_step + hf_get_state per step"}
         h3.close()
 
     cb = clean = None
@@ -623,22 +653,29 @@ def main():
         clean = {k: clean[k] for k in ("value", "unit", "cores", "kind", "ms_per_step", "sample")}
 
     if rank == 0:
+        mixed_over_fp64 = (steps_per_s / fp64["steps_per_s"]) if fp64 else None
+        # the contract keys first, the large sub-objects next, and the spec comparison
+        # (mixed vs FP64 GPU at the same true residual) last, so it closes the line
         line = {
             "metric": METRIC, "value": steps_per_s, "unit": UNIT, "n_gpus": world, "steps": K,
             "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
             "config": dict(workload_config(args, prob), autotuned=tuned),
+            "gpu_launches": st["kernel_launches"],
+            "roofline": roofline, "fp_rates_measured": fp_rates,
+            "cpu_baseline": cb, "cpu_clean_pcg": clean, "clocks": clocks, "e2e": e2e,
             "cell_iters_per_s": cell_iters_per_s,
             "iterations_per_step": {"fp32_cg": st["inner_iterations"] / K,
                                     "fp64_refinement_sweeps": st["refinements"] / K},
             "last_true_relres": st["last_true_relres"],
             "fp64_gpu": fp64,
-            "mixed_over_fp64": (steps_per_s / fp64["steps_per_s"]) if fp64 else None,
-            "roofline": roofline, "fp_rates_measured": fp_rates,
-            "cpu_baseline": cb, "cpu_clean_pcg": clean, "clocks": clocks, "e2e": e2e,
-            "gpu_launches": st["kernel_launches"],
+            "mixed_over_fp64": mixed_over_fp64,
         }
-        print(json.dumps(line), flush=True)
+        line = compact(line)
+        if args.detail:
+            with open(args.detail, "w") as f:
+                json.dump(compact(dict(detail, line=line)), f, indent=1)
+        print(json.dumps(line, separators=(",", ":")), flush=True)
     if dist is not None:
         dist.destroy_process_group()
     return 0

@@ -118,13 +118,18 @@ void free_all(Ctx& c) {
   if (c.stream) cudaStreamSynchronize(c.stream);   // queued host-buffer steps may still run
   drop_graph(c);
   if (c.out_stream) cudaStreamSynchronize(c.out_stream);
-  for (cudaEvent_t* e : {&c.ev_placed, &c.ev_out_done, &c.ev_in_pp, &c.ev_gathered}) {
+  for (cudaEvent_t* e : {&c.ev_placed, &c.ev_in_pp, &c.ev_gathered}) {
     if (*e) cudaEventDestroy(*e);
     *e = nullptr;
   }
-  for (auto& e : c.ev_chunk) {
-    if (e) cudaEventDestroy(e);
-    e = nullptr;
+  for (auto& o : c.outs) {
+    if (o.done) cudaEventDestroy(o.done);
+    o.done = nullptr;
+    for (auto& e : o.chunk) {
+      if (e) cudaEventDestroy(e);
+      e = nullptr;
+    }
+    o.ptr = nullptr;
   }
   for (auto& e : c.ev_in_chunk) {
     if (e) cudaEventDestroy(e);
@@ -1100,32 +1105,41 @@ int hf_step_host_async(hf_ctx* h, int64_t itime, const double* tp, const double*
     build_host_chunks(c);
     if (!c.copy_stream) CU(cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking));
     if (!c.out_stream) CU(cudaStreamCreateWithFlags(&c.out_stream, cudaStreamNonBlocking));
-    for (cudaEvent_t* e : {&c.ev_placed, &c.ev_out_done, &c.ev_in_pp, &c.ev_gathered})
+    for (cudaEvent_t* e : {&c.ev_placed, &c.ev_in_pp, &c.ev_gathered})
       if (!*e) CU(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
-    for (auto& e : c.ev_chunk)
-      if (!e) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    for (auto& o : c.outs) {
+      if (!o.done) CU(cudaEventCreateWithFlags(&o.done, cudaEventDisableTiming));
+      for (auto& e : o.chunk)
+        if (!e) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
     for (auto& e : c.ev_in_chunk)
       if (!e) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     for (double** b : {&c.d_stage_p, &c.d_stage_pp, &c.d_stage_out})
       if (!*b && (rc = dalloc(c, b, (size_t)total))) return rc;
     CU(cudaEventRecord(c.ev_placed, c.stream));
-    CU(cudaEventRecord(c.ev_out_done, c.stream));
-    c.last_out = nullptr;
+    for (auto& o : c.outs) {
+      CU(cudaEventRecord(o.done, c.stream));
+      o.ptr = nullptr;
+    }
   }
   const std::vector<Ctx::HostChunk>& ch = c.host_chunks;
   const int nch = (int)ch.size();
   // Copy stream.  The staging buffers are free once the previous step placed its inputs; by then
-  // every download older than the previous step's is done too (the main stream is in order).
-  // T^(n-1) is normally such an older result, so its upload overlaps the previous step's solve.
-  // T^n is normally the previous step's result: each chunk follows that chunk's download, so the
-  // two directions of the link run at once.
+  // every download older than the last two queued ones is done too (the previous step's main
+  // stream waited for the download before it).  An input that is the destination of one of the
+  // last two downloads waits for it: T^(n-1), normally the result of two steps back, as a whole
+  // (its upload then overlaps the previous step's solve); T^n, normally the previous step's
+  // result, chunk by chunk behind that chunk's download, so both directions of the link run at
+  // once.
   CU(cudaStreamWaitEvent(c.copy_stream, c.ev_placed, 0));
-  if (tpp == c.last_out) CU(cudaStreamWaitEvent(c.copy_stream, c.ev_out_done, 0));
+  for (const auto& o : c.outs)
+    if (o.ptr && tpp == o.ptr) CU(cudaStreamWaitEvent(c.copy_stream, o.done, 0));
   CU(cudaMemcpyAsync(c.d_stage_pp, tpp, sizeof(double) * (size_t)total, cudaMemcpyHostToDevice,
                      c.copy_stream));
   CU(cudaEventRecord(c.ev_in_pp, c.copy_stream));
   for (int k = 0; k < nch; ++k) {
-    if (tp == c.last_out) CU(cudaStreamWaitEvent(c.copy_stream, c.ev_chunk[k], 0));
+    for (const auto& o : c.outs)
+      if (o.ptr && tp == o.ptr) CU(cudaStreamWaitEvent(c.copy_stream, o.chunk[k], 0));
     CU(cudaMemcpyAsync(c.d_stage_p + ch[k].clo, tp + ch[k].clo,
                        sizeof(double) * (size_t)(ch[k].chi - ch[k].clo), cudaMemcpyHostToDevice,
                        c.copy_stream));
@@ -1148,18 +1162,21 @@ int hf_step_host_async(hf_ctx* h, int64_t itime, const double* tp, const double*
   }
   CU(cudaEventRecord(c.ev_placed, c.stream));
   CU(cudaGraphLaunch(c.post_exec, c.stream));
-  CU(cudaStreamWaitEvent(c.stream, c.ev_out_done, 0));    // the previous download has left d_stage_out
+  // the previous download has left d_stage_out
+  CU(cudaStreamWaitEvent(c.stream, c.outs[c.out_last].done, 0));
   CU(launch_host_out(c, c.d_stage_out, c.stream));
   CU(cudaEventRecord(c.ev_gathered, c.stream));
   CU(cudaStreamWaitEvent(c.out_stream, c.ev_gathered, 0));
+  Ctx::HostOut& o = c.outs[c.out_last ^ 1];   // replaces the download of two steps back
   for (int k = 0; k < nch; ++k) {
     CU(cudaMemcpyAsync(out + ch[k].clo, c.d_stage_out + ch[k].clo,
                        sizeof(double) * (size_t)(ch[k].chi - ch[k].clo), cudaMemcpyDeviceToHost,
                        c.out_stream));
-    CU(cudaEventRecord(c.ev_chunk[k], c.out_stream));
+    CU(cudaEventRecord(o.chunk[k], c.out_stream));
   }
-  CU(cudaEventRecord(c.ev_out_done, c.out_stream));
-  c.last_out = out;
+  CU(cudaEventRecord(o.done, c.out_stream));
+  o.ptr = out;
+  c.out_last ^= 1;
   c.async_pending = true;
   c.async_steps += 1;
   c.state_set = true;

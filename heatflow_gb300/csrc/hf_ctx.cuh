@@ -67,12 +67,19 @@ struct Ctx {
   // compact staging buffers; kernels place them into (and gather from) the role buffers
   static constexpr int kHostChunks = 8;
   cudaEvent_t ev_placed = nullptr;     // the last queued step's inputs are in their role buffers
-  cudaEvent_t ev_out_done = nullptr;   // the last queued step's result is on the host
-  cudaEvent_t ev_chunk[kHostChunks] = {};   // ... chunk by chunk
+  // Downloads of the last two queued steps (older ones are covered by ev_placed): the host array
+  // each writes, with events for the whole download and chunk by chunk.  An upload from one of
+  // these arrays waits for its download, whatever order the caller passes the arrays in.
+  struct HostOut {
+    const double* ptr = nullptr;
+    cudaEvent_t done = nullptr;
+    cudaEvent_t chunk[kHostChunks] = {};
+  };
+  HostOut outs[2];
+  int out_last = 0;                    // outs[out_last]: the last queued download
   double* d_stage_p = nullptr;         // T^n of the next step (compact layout)
   double* d_stage_pp = nullptr;        // T^(n-1) of the next step
   double* d_stage_out = nullptr;       // the last step's result
-  const double* last_out = nullptr;    // host array of the last queued download
   // T^n moves in chunks of whole task z-slabs: each chunk's RHS tasks run as soon as its cells
   // are placed, while later chunks are still on the link.  Cells [clo, chi) of the compact host
   // layout, [glo, ghi) of the device layout, tasks [tlo, thi).

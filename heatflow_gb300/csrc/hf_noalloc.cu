@@ -8,7 +8,10 @@
 // norms - in a file-scope static device array, so it allocates nothing.
 //
 // The first call on a device looks up the array's device address with cudaGetSymbolAddress, so
-// it belongs before any stream capture begins.
+// it belongs before any stream capture begins.  The address is kept per device together with the
+// id of the CUDA context it was looked up in; a call that finds another context current (the
+// device was reset with cudaDeviceReset, which unloads the array with the old context) looks the
+// address up again instead of handing the kernel a stale one.
 // The static array is created when the library is loaded on a device and stays resident until
 // the process exits (kNoAllocScratchBytes per device that loads the library).  Every call shares
 // it and it keeps the last call's contents; calls whose kernels overlap on the GPU (two streams,
@@ -36,9 +39,29 @@ static_assert(kNoAllocScratchBytes == 256 * 1024, "the header states 256 KiB of 
 
 static __device__ __align__(256) double g_noalloc_scratch[2 * kNaMaxBlocks];
 
-// Device address of g_noalloc_scratch on each device (the host-side symbol is only a stand-in).
+// Device address of g_noalloc_scratch on each device (the host-side symbol is only a stand-in),
+// with the id of the context it belongs to.
 std::mutex g_mu;
-double* g_scratch_ptr[128] = {nullptr};
+struct ScratchSlot {
+  double* ptr = nullptr;
+  unsigned long long ctx_id = 0;
+};
+ScratchSlot g_scratch[128];
+
+// cuCtxGetId through the runtime's driver entry point (no link against the driver library): the
+// id of the current context, unique for the life of the process.  False if no context is current.
+using CtxIdFn = int (*)(void* ctx, unsigned long long* id);
+bool current_ctx_id(unsigned long long* id) {
+  static CtxIdFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<CtxIdFn>(p);
+  }();
+  return fn && fn(nullptr, id) == 0;
+}
 
 struct Grid {
   int nx, ny, nz;
@@ -131,17 +154,20 @@ int scratch_for_current_device(double** out) {
     return HF_ECUDA;
   }
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_scratch_ptr[dev]) {
+  ScratchSlot& slot = g_scratch[dev];
+  unsigned long long id = 0;
+  if (!slot.ptr || !current_ctx_id(&id) || id != slot.ctx_id) {
     void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);   // makes the device's context current
     if (e != cudaSuccess || !p) {
       hf::set_last_error(std::string("hf_residual_noalloc: cudaGetSymbolAddress failed: ") +
                          cudaGetErrorString(e));
       return HF_ECUDA;
     }
-    g_scratch_ptr[dev] = static_cast<double*>(p);
+    slot.ptr = static_cast<double*>(p);
+    slot.ctx_id = current_ctx_id(&id) ? id : 0;
   }
-  *out = g_scratch_ptr[dev];
+  *out = slot.ptr;
   return HF_OK;
 }
 
@@ -155,13 +181,17 @@ extern "C" int hf_residual_noalloc(int64_t nx, int64_t ny, int64_t nz, const int
     hf::set_last_error("hf_residual_noalloc: dimensions must be >= 1 and every pointer non-null");
     return HF_EARG;
   }
-  const int64_t n = nx * ny * nz;
-  if (n > HF_NOALLOC_MAX_CELLS) {
-    hf::set_last_error("hf_residual_noalloc: " + std::to_string(n) + " cells exceed the static "
-                       "scratch limit HF_NOALLOC_MAX_CELLS = " +
-                       std::to_string((long long)HF_NOALLOC_MAX_CELLS));
+  // the cell count is formed only once it cannot overflow: each factor and each partial product
+  // is held to the limit first
+  const int64_t lim = HF_NOALLOC_MAX_CELLS;
+  if (nx > lim || ny > lim / nx || nz > lim / (nx * ny)) {
+    hf::set_last_error("hf_residual_noalloc: a grid of " + std::to_string((long long)nx) + " x " +
+                       std::to_string((long long)ny) + " x " + std::to_string((long long)nz) +
+                       " cells exceeds the static scratch limit HF_NOALLOC_MAX_CELLS = " +
+                       std::to_string((long long)lim));
     return HF_EARG;
   }
+  const int64_t n = nx * ny * nz;
   double* scratch = nullptr;
   int rc = scratch_for_current_device(&scratch);
   if (rc) return rc;

@@ -1390,14 +1390,14 @@ __global__ void k_ctrl_select(DevArrays A, CtrlState* ctrl, cudaGraphConditional
 // of instance_sum (the order the finalize kernels use, so every path obtains the same bits) and
 // updates the instance's scalars (alpha, beta, convergence test, next phase) in device memory --
 // and only then opens the barrier.  Blocks read the scalars of the instances they work on through
-// L2 at the start of each round.  Tasks are assigned statically (task t to block t mod grid).
-// The kernel returns when the last epilogue reports that no instance has work left.
+// L2 at the start of each round.  Tasks are handed out one at a time from a per-round counter
+// (SolveCtl::next_task), so blocks on busier SMs take fewer of them.  The kernel returns when the
+// last epilogue reports that no instance has work left.
 //
 // Termination: every barrier wait is bounded in time (wait_ns, 4 s by default) and in polls; a block that
 // gives up records SolveCtl::err and returns, and the blocks still waiting see the flag and return
 // too.  The number of rounds is bounded by `limit`.  Co-residency of all blocks, which the barrier
 // needs, is guaranteed by the cooperative launch (the grid never exceeds the occupancy bound).
-constexpr unsigned long long kBarrierWaitNs = 4000000000ull;   // default barrier time limit
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
   unsigned v;

@@ -485,6 +485,13 @@ std::string next_log_name(const std::string& outdir, const std::string& run_name
   }
 }
 
+int records_after(const Param& p, int64_t itime) {
+  if (p.test_run) return 0;
+  int n = itime == 1 ? 1 : 0;
+  if (p.write_to_txt && p.write_every > 0 && itime % p.write_every == 0) ++n;
+  return n;
+}
+
 std::string problem_json(const Deck& d) {
   const Param& p = d.param;
   const hf_problem& q = d.prob;

@@ -77,6 +77,12 @@ std::string format_record(double time, const double* v, int64_t n);
 // First ./outputs/output_<RunName>_NN (NN from 00) that does not exist (last_log, :187-201).
 std::string next_log_name(const std::string& outdir, const std::string& run_name);
 
+// Records data_write appends to the sub-box log after step `itime` (mod_output.f90:79-113): one
+// when the log is opened at itime = 1, and one more whenever _WriteToTxt is set and
+// mod(itime, write_every) = 0 -- so with write_every = 1, step 1 is logged twice.  Test runs log
+// nothing.
+int records_after(const Param& p, int64_t itime);
+
 // The deck's problem as JSON (parsed values; the per-cell arrays as lists), for comparisons.
 std::string problem_json(const Deck& deck);
 

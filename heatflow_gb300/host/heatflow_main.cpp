@@ -7,11 +7,12 @@
 //
 //   heatflow_gb300 [--inputs DIR] [--outputs DIR] [--restart DIR]
 //                  [--precision fp64|mixed] [--criterion recursive|true] [--tol X]
-//                  [--graph 0|1|2|3] [--dump-problem]
+//                  [--graph 0|1|2|3] [--dump-problem] [--dump-log-schedule]
 //
 // Defaults follow the reference: FP64 with linbcg's stopping rule (recursive residual, tol 1e-32),
 // the whole step loop as CUDA graphs.  --dump-problem prints the parsed deck as JSON and stops
-// before any GPU call.  A fatal condition prints the reference's message and exits with status 1
+// before any GPU call; --dump-log-schedule prints, as JSON, the steps after which the sub-box log
+// gets records and how many ([itime, records] pairs), and stops before any GPU call too.  A fatal condition prints the reference's message and exits with status 1
 // (`stop 1`).
 #include <chrono>
 #include <cstdio>
@@ -30,13 +31,13 @@ struct Options {
   std::string inputs = "./inputs", outputs = "./outputs", restart = "./restart";
   int precision = HF_PREC_FP64, criterion = HF_STOP_RECURSIVE, use_graph = 1;
   double tol = -1.0;
-  bool dump_problem = false;
+  bool dump_problem = false, dump_log_schedule = false;
 };
 
 [[noreturn]] void usage(const char* msg) {
   std::fprintf(stderr, "%s\nusage: heatflow_gb300 [--inputs DIR] [--outputs DIR] [--restart DIR] "
                        "[--precision fp64|mixed] [--criterion recursive|true] [--tol X] "
-                       "[--graph 0|1|2|3] [--dump-problem]\n", msg);
+                       "[--graph 0|1|2|3] [--dump-problem] [--dump-log-schedule]\n", msg);
   std::exit(2);
 }
 
@@ -64,6 +65,7 @@ Options parse_args(int argc, char** argv) {
     } else if (a == "--tol") o.tol = std::atof(next().c_str());
     else if (a == "--graph") o.use_graph = std::atoi(next().c_str());
     else if (a == "--dump-problem") o.dump_problem = true;
+    else if (a == "--dump-log-schedule") o.dump_log_schedule = true;
     else usage(("unknown argument " + a).c_str());
   }
   return o;
@@ -105,6 +107,19 @@ int main(int argc, char** argv) {
   }
   const hfhost::Param& P = deck.param;
   const int64_t n = deck.ncells();
+  if (opt.dump_log_schedule) {
+    std::printf("[");
+    const char* sep = "";
+    for (int64_t it = 1; it <= P.ntime; ++it) {
+      const int k = hfhost::records_after(P, it);
+      if (k > 0) {
+        std::printf("%s[%lld, %d]", sep, (long long)it, k);
+        sep = ", ";
+      }
+    }
+    std::printf("]\n");
+    return 0;
+  }
 
   hf_solver_opts so;
   hf_default_opts(&so);
@@ -135,7 +150,11 @@ int main(int argc, char** argv) {
     hf_destroy(ctx);
     return 1;
   }
-  if ((rc = hf_set_state(ctx, tp.data(), tpp.data())) != HF_OK) return fail_lib(rc, "hf_set_state");
+  if ((rc = hf_set_state(ctx, tp.data(), tpp.data())) != HF_OK) {
+    fail_lib(rc, "hf_set_state");
+    hf_destroy(ctx);
+    return 1;
+  }
 
   mkdir(opt.outputs.c_str(), 0755);
   // sub-box of the log (1-based inclusive bounds of param.in; an empty box logs the time only)
@@ -154,19 +173,16 @@ int main(int argc, char** argv) {
     }
     return HF_OK;
   };
-  // data_write logs after step 1 and, with _WriteToTxt, every write_every steps (not in test runs)
-  auto logs_after = [&](int64_t it) {
-    if (P.test_run) return false;
-    if (it == 1) return true;
-    return P.write_to_txt && P.write_every > 0 && it % P.write_every == 0;
-  };
+  // data_write logs after step 1 and, with _WriteToTxt, every write_every steps (not in test
+  // runs); step 1 gets two records when both rules apply (hfhost::records_after)
+  auto logs_after = [&](int64_t it) { return hfhost::records_after(P, it) > 0; };
   // Log records in flight: the sub-box is gathered on the device after the step and copied to a
   // page-locked buffer on the library's second stream while the next steps run; records are
   // written in order once their copy is done (at most kInFlight at a time).
   constexpr int kInFlight = 3;
   struct Pending {
     int64_t itime = 0, ticket = -1;
-    int slot = 0;
+    int slot = 0, copies = 1;   // the same record written `copies` times in a row
   };
   std::vector<std::vector<double>> ring(kInFlight + 1, std::vector<double>(nbox > 0 ? nbox : 1));
   for (auto& b : ring) hf_host_register(b.data(), b.size() * sizeof(double));   // best effort
@@ -182,7 +198,7 @@ int main(int argc, char** argv) {
       }
       const std::string rec = hfhost::format_record((double)(p.itime - 1) * P.time_step,
                                                     ring[p.slot].data(), nbox);
-      std::fwrite(rec.data(), 1, rec.size(), log);
+      for (int k = 0; k < p.copies; ++k) std::fwrite(rec.data(), 1, rec.size(), log);
     }
     return HF_OK;
   };
@@ -190,6 +206,13 @@ int main(int argc, char** argv) {
     for (auto& b : ring) hf_host_unregister(b.data());
     if (log) std::fclose(log);
     log = nullptr;
+  };
+  // a library error after set-up: the reference's message, then the buffers and the context go
+  auto fail_run = [&](int r, const char* where) {
+    fail_lib(r, where);
+    cleanup();
+    hf_destroy(ctx);
+    return 1;
   };
 
   // The steps between two host actions (a log record, a per-step print at IVERB >= 3, the end)
@@ -200,12 +223,7 @@ int main(int argc, char** argv) {
     while (last < P.ntime && !logs_after(last) && P.iverb < 3) ++last;
     hf_stats st;
     rc = hf_run(ctx, itime, last - itime + 1, &st);
-    if (rc != HF_OK) {
-      fail_lib(rc, "simulate");
-      cleanup();
-      hf_destroy(ctx);
-      return 1;
-    }
+    if (rc != HF_OK) return fail_run(rc, "simulate");
     if (logs_after(last)) {
       if (last == 1) {
         log = std::fopen(hfhost::next_log_name(opt.outputs, P.run_name).c_str(), "w");
@@ -219,18 +237,22 @@ int main(int argc, char** argv) {
       Pending p;
       p.itime = last;
       p.slot = next_slot;
+      p.copies = hfhost::records_after(P, last);
       next_slot = (next_slot + 1) % (kInFlight + 1);
+      // the _WriteToTxt record's message (mod_output.f90:110)
+      if (P.write_to_txt && P.write_every > 0 && last % P.write_every == 0)
+        std::printf(" Writing Temperature difference to file\n");
       if (box && (rc = hf_subbox_async(ctx, 0, lo, hi, 1, ring[p.slot].data(), &p.ticket)) != HF_OK)
-        return fail_lib(rc, "data_write");
+        return fail_run(rc, "data_write");
       pending.push_back(p);
-      if ((rc = drain(kInFlight - 1)) != HF_OK) return fail_lib(rc, "data_write");
+      if ((rc = drain(kInFlight - 1)) != HF_OK) return fail_run(rc, "data_write");
     }
-    if (P.iverb >= 3 && (rc = final_print()) != HF_OK) return fail_lib(rc, "final_print");
+    if (P.iverb >= 3 && (rc = final_print()) != HF_OK) return fail_run(rc, "final_print");
     if (last == P.ntime) {
-      if ((rc = drain(0)) != HF_OK) return fail_lib(rc, "data_write");
+      if ((rc = drain(0)) != HF_OK) return fail_run(rc, "data_write");
       if (log) std::fclose(log);
       log = nullptr;
-      if ((rc = final_print()) != HF_OK) return fail_lib(rc, "final_print");
+      if ((rc = final_print()) != HF_OK) return fail_run(rc, "final_print");
     }
     itime = last + 1;
   }

@@ -212,7 +212,8 @@ int hf_adjoint_accumulate(hf_ctx* ctx, const double* lam, const double* x, int64
  * solving; T^n - normally the previous call's temp_out - is uploaded chunk by chunk right behind
  * that download, so both directions of the host link run at once, and the right-hand side of
  * each chunk's cells is computed as soon as the chunk is placed.  Any arrays may be passed:
- * an input that is the previous call's temp_out waits for its download.  Every array
+ * an input that is the temp_out of one of the queued calls waits for that download, in
+ * whatever order the arrays rotate.  Every array
  * holds total_cells doubles (instances back to back) and must stay valid and untouched until
  * hf_host_sync returns.  Needs use_graph 1 or 3.  While steps are queued, every other call that
  * reads or changes the state returns HF_ESTATE. */
@@ -334,7 +335,8 @@ int hf_autotune(hf_ctx* ctx, int64_t itime0, int32_t steps, hf_tune_result* resu
  * allocates nothing: its reduction scratch is a static device array of 256 KiB that every device
  * loading the library holds until the process exits, which limits grids to
  * HF_NOALLOC_MAX_CELLS cells (larger grids return HF_EARG).  The first call on a device looks up
- * that array's device address (cudaGetSymbolAddress), so make it before any stream capture.
+ * that array's device address (cudaGetSymbolAddress), so make it before any stream capture; so
+ * does the first call after the device's context was reset (cudaDeviceReset).
  * Calls share the scratch and keep the last call's partial sums: calls whose kernels overlap on
  * the GPU race and must be serialised by the caller.  Asynchronous: results are ready when the
  * stream reaches them. */

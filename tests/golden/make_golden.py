@@ -3,9 +3,9 @@
 Reads the reference's test/data/{param.in, mat.in, system.in, TempDis.dat} (a 25x25x1 Fourier
 run of 10 steps whose final Temp_p the reference wrote with final_print) and stores them in
 tempdis_25x25.json: the three input decks verbatim (they are the run's inputs) and the 625
-golden temperatures.  Run from the repository root:
+golden temperatures.  Run from the repository root with the reference's checkout as argument:
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path to the HeatFlow checkout>
 """
 import json
 import os
@@ -32,4 +32,6 @@ def main(ref_root: str):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <path to the HeatFlow checkout>")
+    main(sys.argv[1])

@@ -1,6 +1,7 @@
 """The C++ host program runs the reference's test deck end to end on the GPU: ./inputs read,
 10 steps, ./outputs/TempDis.dat and TempDisTPD.dat in final_print's layout, and the sub-box log
-output_<RunName>_00 with one record after step 1 and one every write_every steps."""
+output_<RunName>_00 with data_write's records: one when the log opens after step 1 and, with
+_WriteToTxt, one every write_every steps (mod_output.f90:79-113), so step 1 twice at write_every 1."""
 import os
 import subprocess
 
@@ -40,10 +41,13 @@ def test_driver_runs_the_golden_deck(cuda_lib, golden, tmp_path):
     Tp, Tpp = states[-1]
     assert (work / "outputs" / "TempDis.dat").read_text() == inputs.format_temp_file(Tp)
     assert (work / "outputs" / "TempDisTPD.dat").read_text() == inputs.format_temp_file(Tpp)
-    # the log: T^(n-1) after each logged step over the 25 x 25 x 1 box, at time (itime-1) dt
+    # the log: T^(n-1) after each logged step over the 25 x 25 x 1 box, at time (itime-1) dt;
+    # write_every = 1 with _WriteToTxt: step 1 is logged twice, then every step
     recs = parse_records((work / "outputs" / "output_IntRun_00").read_text())
-    assert len(recs) == param["ntime"]
-    for k, (t, vals) in enumerate(recs, start=1):
+    marks = [1] + list(range(1, param["ntime"] + 1))
+    assert len(recs) == param["ntime"] + 1 == 11
+    assert r.stdout.count("Writing Temperature difference to file") == param["ntime"]
+    for k, (t, vals) in zip(marks, recs):
         assert t == float(np.float32((k - 1) * param["time_step"]))
         assert np.allclose(vals, states[k - 1][1], rtol=1e-15, atol=0)
 
