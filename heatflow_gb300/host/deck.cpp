@@ -485,6 +485,47 @@ std::string next_log_name(const std::string& outdir, const std::string& run_name
   }
 }
 
+std::vector<double> parse_property_table(const std::string& text, const std::string& name) {
+  std::vector<double> rows;
+  for (const std::string& line : split_lines(text)) {
+    const std::vector<std::string> t = split_ws(line);
+    if (t.empty()) continue;
+    if (t.size() != 4)
+      throw InputError("Error: " + name + ": each row needs 4 values (T, kappa, rho, c), got " +
+                       std::to_string(t.size()));
+    for (const std::string& v : t) rows.push_back(fortran_real(v));
+    const size_t r = rows.size() / 4;
+    if (r > 1 && !(rows[4 * (r - 1)] > rows[4 * (r - 2)]))
+      throw InputError("Error: " + name + ": temperatures must ascend");
+  }
+  if (rows.size() < 8) throw InputError("Error: " + name + ": a table needs at least two rows");
+  return rows;
+}
+
+PropertyTables load_material_tables(const std::string& inputs_dir, const System& sys) {
+  PropertyTables pt;
+  const int64_t n = sys.nx * sys.ny * sys.nz;
+  std::map<int64_t, int32_t> index;              // material -> table, -1 without a file
+  for (int64_t I = 0; I < n; ++I) index.emplace(sys.imaterial[I], -1);
+  pt.offsets.push_back(0);
+  for (auto& kv : index) {                       // ascending material index
+    std::string path = inputs_dir;
+    if (!path.empty() && path.back() != '/') path += '/';
+    path += "MatTable" + std::to_string((long long)kv.first);
+    struct stat st;
+    if (stat(path.c_str(), &st) != 0) continue;  // no file: fixed properties
+    const std::vector<double> rows =
+        parse_property_table(read_text_file(path, "Error cannot find file: " + path), path);
+    kv.second = pt.ntables();
+    pt.materials.push_back(kv.first);
+    pt.rows.insert(pt.rows.end(), rows.begin(), rows.end());
+    pt.offsets.push_back((int32_t)(pt.rows.size() / 4));
+  }
+  pt.cell_table.resize(n);
+  for (int64_t I = 0; I < n; ++I) pt.cell_table[I] = index[sys.imaterial[I]];
+  return pt;
+}
+
 int records_after(const Param& p, int64_t itime) {
   if (p.test_run) return 0;
   int n = itime == 1 ? 1 : 0;
@@ -530,7 +571,21 @@ std::string problem_json(const Deck& d) {
     << ", \"input_temp_dis\": " << (p.input_temp_dis ? 1 : 0)
     << ", \"full_restart\": " << (p.full_restart ? 1 : 0)
     << ", \"test_run\": " << (p.test_run ? 1 : 0)
-    << ", \"write_to_txt\": " << (p.write_to_txt ? 1 : 0) << "}";
+    << ", \"write_to_txt\": " << (p.write_to_txt ? 1 : 0)
+    << ", \"temp_dep_prop\": " << p.temp_dep_prop;
+  if (d.tables.ntables() > 0) {
+    const PropertyTables& t = d.tables;
+    o << ", \"property_tables\": {\"materials\": [";
+    for (size_t k = 0; k < t.materials.size(); ++k) o << (k ? ", " : "") << t.materials[k];
+    o << "], \"offsets\": [";
+    for (size_t k = 0; k < t.offsets.size(); ++k) o << (k ? ", " : "") << t.offsets[k];
+    o << "], ";
+    append_json_array(o, "rows", t.rows.data(), (int64_t)t.rows.size());
+    o << ", \"cell_table\": [";
+    for (size_t k = 0; k < t.cell_table.size(); ++k) o << (k ? ", " : "") << t.cell_table[k];
+    o << "]}";
+  }
+  o << "}";
   return o.str();
 }
 

@@ -53,6 +53,25 @@ std::vector<Material> read_mat(const std::string& text);
 System read_system(const std::string& text);
 Material material(int64_t imaterial, const std::vector<Material>& mats);
 
+// Temperature tables of the materials (TempDepProp = 1): the per-material file
+// ./inputs/MatTable<imaterial> that ChangeProp looks for (mod_tempdep.f90:44-55), in the format of
+// the reference's test/data/tempdep.in -- one row per line, four numbers: T (ascending), kappa,
+// rho, heat capacity.  Laid out for hf_set_property_tables: table k is rows[4*offsets[k] ..
+// 4*offsets[k+1]), materials[k] its material index, cell_table the table of each cell or -1.
+struct PropertyTables {
+  std::vector<int64_t> materials;
+  std::vector<int32_t> offsets;
+  std::vector<double> rows;
+  std::vector<int32_t> cell_table;
+  int32_t ntables() const { return offsets.empty() ? 0 : (int32_t)offsets.size() - 1; }
+};
+// One table's rows (4 values each); InputError on a ragged row, fewer than two rows, or
+// temperatures that do not ascend.
+std::vector<double> parse_property_table(const std::string& text, const std::string& name);
+// Tables of every material of the grid that has a MatTable<imaterial> file in inputs_dir
+// (materials in ascending index order); materials without a file keep fixed properties.
+PropertyTables load_material_tables(const std::string& inputs_dir, const System& sys);
+
 // A deck's problem: per-cell arrays owned here, `prob` points into them.
 struct Deck {
   Param param;
@@ -60,6 +79,7 @@ struct Deck {
   System sys;
   std::vector<double> kappa, rho, heat_capacity, tau, em;
   hf_problem prob{};
+  PropertyTables tables;   // loaded when TempDepProp = 1
   int64_t ncells() const { return sys.nx * sys.ny * sys.nz; }
 };
 // read_all_files on in-memory decks (mod_inputs.f90:116-196) + set_global_variables' per-cell part

@@ -97,6 +97,9 @@ int main(int argc, char** argv) {
     const std::string mat = hfhost::read_text_file(opt.inputs + "/mat.in", "Error cannot find file: mat.in");
     const std::string sys = hfhost::read_text_file(opt.inputs + "/system.in", "Error cannot find file: system.in");
     hfhost::build_deck(deck, param, mat, sys);
+    // TempDepProp = 1: ChangeProp's per-material tables (mod_tempdep.f90:44-55), re-evaluated
+    // after every step (mod_evolve.f90:172-174)
+    if (deck.param.temp_dep_prop == 1) deck.tables = hfhost::load_material_tables(opt.inputs, deck.sys);
   } catch (const hfhost::InputError& e) {
     std::printf(" %s\n", e.what());
     return 1;
@@ -130,6 +133,15 @@ int main(int argc, char** argv) {
   hf_ctx* ctx = nullptr;
   int rc = hf_create(&deck.prob, &so, &ctx);
   if (rc != HF_OK) return fail_lib(rc, "hf_create");
+  if (deck.tables.ntables() > 0) {
+    const hfhost::PropertyTables& t = deck.tables;
+    if ((rc = hf_set_property_tables(ctx, t.ntables(), t.offsets.data(), t.rows.data(),
+                                     t.cell_table.data())) != HF_OK) {
+      fail_lib(rc, "hf_set_property_tables");
+      hf_destroy(ctx);
+      return 1;
+    }
+  }
   std::printf(" Setup complete, running simulation\n");
 
   // initial_evolve

@@ -305,6 +305,45 @@ def read_input_dir(path: str):
     return read_all_files(rd("param.in"), rd("mat.in"), rd("system.in"))
 
 
+# ---- temperature tables (TempDepProp = 1, mod_tempdep.f90) ------------------------------------
+def parse_property_table(text: str, name: str = "table") -> np.ndarray:
+    """One material's table in the format of the reference's test/data/tempdep.in: one row per
+    line, T (ascending), kappa, rho, heat capacity.  Returns a (rows, 4) array."""
+    rows = []
+    for line in text.splitlines():
+        t = line.split()
+        if not t:
+            continue
+        if len(t) != 4:
+            raise InputError(f"Error: {name}: each row needs 4 values (T, kappa, rho, c), got {len(t)}")
+        rows.append([_fortran_real(v) for v in t])
+        if len(rows) > 1 and not rows[-1][0] > rows[-2][0]:
+            raise InputError(f"Error: {name}: temperatures must ascend")
+    if len(rows) < 2:
+        raise InputError(f"Error: {name}: a table needs at least two rows")
+    return np.asarray(rows, dtype=np.float64)
+
+
+def material_tables(inputs_dir: str, imaterial) -> tuple[list, np.ndarray]:
+    """ChangeProp's lookup (mod_tempdep.f90:44-55): every material of the grid that has a file
+    <inputs_dir>/MatTable<imaterial> gets that table (materials in ascending index order); the
+    others keep fixed properties.  Returns (tables, cell_table) for HeatFlow.set_property_tables
+    (cell_table: the table of each cell, or -1).  The reference builds the name with
+    char(imaterial), the character whose code is the index -- evidently meant as the decimal
+    index, which is what is used here."""
+    imaterial = np.asarray(imaterial, dtype=np.int64)
+    tables, index = [], {}
+    for m in sorted(set(int(v) for v in np.unique(imaterial))):
+        path = os.path.join(inputs_dir, f"MatTable{m}")
+        index[m] = -1
+        if os.path.exists(path):
+            with open(path) as f:
+                tables.append(parse_property_table(f.read(), path))
+            index[m] = len(tables) - 1
+    cell_table = np.array([index[int(v)] for v in imaterial], dtype=np.int32)
+    return tables, cell_table
+
+
 # ---- restart / output formats (mod_output.f90:225-237, mod_init_evolve.f90:66-140) ----------
 def format_temp_file(values) -> str:
     """final_print's layout: 6 values per line, ES16.8 with 1X separators, two blank lines."""

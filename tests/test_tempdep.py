@@ -156,3 +156,120 @@ def test_oracle_one_cell_periodic_axis_has_zero_diagonal():
     from oracle.oracle import Oracle
     prob, _, _ = periodic_problem(6, 1, 4, (0, 1, 0))
     assert np.all(np.diag(Oracle(prob).dense()) == 0.0)
+
+
+# ---- the reference's table format and per-material lookup (mod_tempdep.f90:44-55) ---------------
+def _reference_table_text():
+    import json
+    import os
+    here = os.path.dirname(os.path.abspath(__file__))
+    with open(os.path.join(here, "golden", "tempdep_table.json")) as f:
+        return json.load(f)["text"]
+
+
+def _tempdep_deck(golden, d, with_table=True):
+    """The reference's test deck with TempDepProp = 1 and, for its material 1, the reference's
+    table test/data/tempdep.in as ./inputs/MatTable1."""
+    d.mkdir(parents=True, exist_ok=True)
+    param = golden["param_in"].replace("TempDepProp = 0", "TempDepProp = 1")
+    assert "TempDepProp = 1" in param
+    (d / "param.in").write_text(param)
+    (d / "mat.in").write_text(golden["mat_in"])
+    (d / "system.in").write_text(golden["system_in"])
+    if with_table:
+        (d / "MatTable1").write_text(_reference_table_text())
+    return param
+
+
+def test_reference_table_parses():
+    from heatflow_gb300.inputs import parse_property_table
+    text = _reference_table_text()
+    rows = parse_property_table(text)
+    assert rows.shape == (24, 4)
+    assert np.all(np.diff(rows[:, 0]) > 0)
+    want = np.array([[float(v) for v in line.split()] for line in text.splitlines() if line.split()])
+    assert np.array_equal(rows, want)
+
+
+@pytest.mark.parametrize("bad", ["300 1 2\n", "300 1 2 3\n290 1 2 3\n", "300 1 2 3\n"])
+def test_bad_tables_refused(bad):
+    from heatflow_gb300.inputs import InputError, parse_property_table
+    with pytest.raises(InputError):
+        parse_property_table(bad)
+
+
+def test_host_program_reads_material_tables(golden, tmp_path):
+    """The C++ host program and the Python readers find the same MatTable<imaterial> files and
+    read the same rows (--dump-problem stops before any GPU call)."""
+    import json
+    import subprocess
+    from heatflow_gb300 import inputs
+    from heatflow_gb300.build import build_driver, build_library
+    build_library()
+    drv = build_driver()
+    d = tmp_path / "inputs"
+    _tempdep_deck(golden, d)
+    r = subprocess.run([drv, "--inputs", str(d), "--dump-problem"], capture_output=True, text=True,
+                       timeout=60)
+    assert r.returncode == 0, r.stdout + r.stderr
+    js = json.loads(next(l for l in r.stdout.splitlines() if l.startswith("{")))
+    assert js["temp_dep_prop"] == 1
+    sysd = inputs.read_system(golden["system_in"])
+    tables, ct = inputs.material_tables(str(d), sysd.imaterial)
+    pt = js["property_tables"]
+    assert pt["materials"] == [1] and pt["offsets"] == [0, 24]
+    assert np.array_equal(np.asarray(pt["rows"]).reshape(-1, 4), tables[0])
+    assert np.array_equal(np.asarray(pt["cell_table"]), ct) and np.all(ct == 0)
+    # without a MatTable file the material keeps fixed properties (the reference's `continue`)
+    (d / "MatTable1").unlink()
+    r = subprocess.run([drv, "--inputs", str(d), "--dump-problem"], capture_output=True, text=True,
+                       timeout=60)
+    js = json.loads(next(l for l in r.stdout.splitlines() if l.startswith("{")))
+    assert "property_tables" not in js
+    assert inputs.material_tables(str(d), sysd.imaterial)[0] == []
+    # a malformed table stops the program with a message, as input errors do
+    (d / "MatTable1").write_text("300 1 2\n")
+    r = subprocess.run([drv, "--inputs", str(d), "--dump-problem"], capture_output=True, text=True,
+                       timeout=60)
+    assert r.returncode == 1 and "MatTable1" in r.stdout
+
+
+@pytest.mark.gpu
+def test_reference_table_deck_on_gpu(cuda_lib, golden, tmp_path):
+    """The reference's test deck with TempDepProp = 1 and its table file: the C++ host program
+    runs it end to end; its TempDis.dat equals the Python path's (same library) byte for byte,
+    and that field is within 1e-10 of the oracle run with the same tables."""
+    import subprocess
+    from oracle.oracle import Oracle
+    from heatflow_gb300 import inputs
+    from heatflow_gb300.build import build_driver, build_library
+    from heatflow_gb300.solver import HeatFlow
+    build_library()
+    drv = build_driver()
+    work = tmp_path / "run"
+    param_text = _tempdep_deck(golden, work / "inputs")
+    r = subprocess.run([drv], cwd=work, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    param, prob = inputs.read_all_files(param_text, golden["mat_in"], golden["system_in"])
+    sysd = inputs.read_system(golden["system_in"])
+    tables, ct = inputs.material_tables(str(work / "inputs"), sysd.imaterial)
+    nt = param["ntime"]
+    o = Oracle(prob)
+    o.set_property_tables(tables, ct)
+    o.set_state(*prob.initial_state())
+    rc, _ = o.run(nt, itime0=1, mode=0, tol=1e-32, itmax=50000)
+    assert rc == 0
+    Tref, _ = o.get_state()
+    o0 = Oracle(prob)                                    # the same deck without the table
+    o0.set_state(*prob.initial_state())
+    o0.run(nt, itime0=1, mode=0, tol=1e-32, itmax=50000)
+    assert np.linalg.norm(o0.get_state()[0] - Tref) / np.linalg.norm(Tref) > 1e-6
+    with HeatFlow(prob, precision="fp64", criterion="recursive", tol=1e-32) as hf:
+        hf.set_property_tables(tables, ct)
+        hf.initial_evolve()
+        for k in range(1, nt + 1):
+            hf.run(k, 1)
+        Tp, Tpp = hf.get_state()
+    assert np.linalg.norm(Tp - Tref) / np.linalg.norm(Tref) <= 1e-10
+    assert (work / "outputs" / "TempDis.dat").read_text() == inputs.format_temp_file(Tp)
+    assert (work / "outputs" / "TempDisTPD.dat").read_text() == inputs.format_temp_file(Tpp)
