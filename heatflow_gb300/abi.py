@@ -139,6 +139,7 @@ _SIGNATURES = {
     "hf_adjoint_rhs": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "hf_adjoint_accumulate": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
                                         C.c_void_p]),
+    "hf_index_checks": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int64)]),
 }
 HF_KERNEL_RHS, HF_KERNEL_RESIDUAL, HF_KERNEL_CG_P, HF_KERNEL_CG_SPMV, HF_KERNEL_CG_UPDATE = 0, 1, 2, 3, 4
 HF_KERNEL_XUPDATE, HF_KERNEL_SOLVE, HF_KERNEL_CG_PQ, HF_KERNEL_RESIDUAL_INIT = 5, 6, 7, 8
@@ -149,14 +150,18 @@ PHASE_NAMES = {HF_PHASE_IDLE: "idle", HF_PHASE_START: "start", HF_PHASE_RES_INIT
                HF_PHASE_CG_B: "cg_b", HF_PHASE_XUPD: "xupd", HF_PHASE_RES: "res",
                HF_PHASE_RES_INIT_HX: "res_init_hx"}
 
-_lib = None
+# the index-checked build of the same library (tests only; built by build_library(checked=True))
+CHECKED_LIB_PATH = os.path.join(HERE, "_build", "checked", "libheatflow_gb300_checked.so")
+_libs: dict = {}
 
 
-def load_library(path: str = LIB_PATH):
-    """Load libheatflow_gb300.so and declare its signatures.  Raises if it is missing."""
-    global _lib
-    if _lib is not None:
-        return _lib
+def load_library(path: str = LIB_PATH, checked: bool = False):
+    """Load libheatflow_gb300.so (or, with checked=True, its index-checked build) and declare its
+    signatures.  Raises if it is missing."""
+    if checked:
+        path = CHECKED_LIB_PATH
+    if path in _libs:
+        return _libs[path]
     if not os.path.exists(path):
         raise RuntimeError(
             f"heatflow_gb300: CUDA library not built ({path}); run "
@@ -168,7 +173,7 @@ def load_library(path: str = LIB_PATH):
             continue
         fn.restype = res
         fn.argtypes = args
-    _lib = lib
+    _libs[path] = lib
     return lib
 
 
@@ -182,8 +187,9 @@ class HeatFlowError(RuntimeError):
         super().__init__(f"{where}: {msg}" + (f" ({detail})" if detail else ""))
 
 
-def check(code: int, where: str):
+def check(code: int, where: str, lib=None):
+    """Raise HeatFlowError for a failed call; `lib` is the library that made it (its last error)."""
     if code != HF_OK:
-        lib = load_library()
+        lib = lib or load_library()
         detail = lib.hf_last_error()
         raise HeatFlowError(code, where, detail.decode() if detail else "")

@@ -2,6 +2,8 @@
 
 Translation units compile in parallel; the set-up and RHS kernels are compiled with -fmad=false
 (they restate the reference's arithmetic bit for bit), the solver kernels with FMA.
+build_library(checked=True) builds the index-checked variant (-DHF_CHECKED, every global access
+of the step kernels checked against its array's extent) into _build/checked/, for tests.
 """
 from __future__ import annotations
 
@@ -14,6 +16,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libheatflow_gb300.so")
+OUT_CHECKED = os.path.join(OUT, "checked")
+LIB_CHECKED = os.path.join(OUT_CHECKED, "libheatflow_gb300_checked.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
@@ -36,9 +40,9 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found")
 
 
-def _compile(unit: str, flags: list[str], verbose: bool) -> str:
+def _compile(unit: str, flags: list[str], verbose: bool, out: str = OUT) -> str:
     src = os.path.join(CSRC, unit)
-    obj = os.path.join(OUT, unit.replace(".cu", ".o"))
+    obj = os.path.join(out, unit.replace(".cu", ".o"))
     cmd = [nvcc(), *ARCH, *COMMON, *flags, "-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
@@ -50,10 +54,10 @@ def _compile(unit: str, flags: list[str], verbose: bool) -> str:
     return obj
 
 
-def _stale() -> bool:
-    if not os.path.exists(LIB):
+def _stale(lib: str = LIB) -> bool:
+    if not os.path.exists(lib):
         return True
-    t = os.path.getmtime(LIB)
+    t = os.path.getmtime(lib)
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
     deps.append(os.path.join(os.path.dirname(HERE), "include", "heatflow_gb300.h"))
     deps.append(__file__)
@@ -84,21 +88,24 @@ def build_driver(force: bool = False) -> str:
     return DRIVER
 
 
-def build_library(force: bool = False, verbose: bool = False) -> str:
-    if not force and not _stale():
-        return LIB
-    os.makedirs(OUT, exist_ok=True)
+def build_library(force: bool = False, verbose: bool = False, checked: bool = False) -> str:
+    lib, out = (LIB_CHECKED, OUT_CHECKED) if checked else (LIB, OUT)
+    extra = ["-DHF_CHECKED"] if checked else []
+    if not force and not _stale(lib):
+        return lib
+    os.makedirs(out, exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
-        objs = list(ex.map(lambda kv: _compile(kv[0], kv[1], verbose), UNITS.items()))
-    tmp = LIB + ".tmp"
+        objs = list(ex.map(lambda kv: _compile(kv[0], kv[1] + extra, verbose, out), UNITS.items()))
+    tmp = lib + ".tmp"
     cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":
     print(build_library(force=True, verbose=False))
+    print(build_library(force=True, verbose=False, checked=True))
     print(build_driver(force=True))

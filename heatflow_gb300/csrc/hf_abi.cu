@@ -11,6 +11,8 @@
 
 #include "hf_ctx.cuh"
 
+#define HF_FILE_ID 1   // index-check sites of the checked build: 100000 * file + line
+
 namespace hf {
 cudaError_t launch_props(Ctx& c, const double* rho, const double* hc, const double* tau,
                          const double* em);
@@ -596,7 +598,27 @@ void fill_stats(Ctx& c, hf_stats* st, int64_t steps, const std::vector<InstScal>
   }
 }
 
+// The index-check record of the checked build: HF_EDEVICE with the first failed check's site.
+int check_record(Ctx& c) {
+#ifdef HF_CHECKED
+  unsigned long long rec[4] = {0, 0, 0, 0};
+  CU(cudaMemcpyAsync(rec, c.A.check, sizeof(rec), cudaMemcpyDeviceToHost, c.stream));
+  CU(cudaStreamSynchronize(c.stream));
+  if (rec[0])
+    return set_err(HF_EDEVICE, "index check failed " + std::to_string(rec[0]) + " time(s); first at "
+                               "site " + std::to_string(rec[1]) + " (file " +
+                               std::to_string(rec[1] / 100000) + ", line " +
+                               std::to_string(rec[1] % 100000) + "): index " +
+                               std::to_string((long long)rec[2]) + " outside [0, " +
+                               std::to_string(rec[3]) + ")");
+#else
+  (void)c;
+#endif
+  return HF_OK;
+}
+
 int first_error(Ctx& c) {
+  if (int r = check_record(c)) return r;
   for (int64_t i = 0; i < c.ninst; ++i) {
     if (c.h_scal[i].status) return status_code(c.h_scal[i].status);
     if (c.h_scal[i].devcheck)
@@ -823,6 +845,7 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
   for (int k = 0; k < 4; ++k) ALLOC(A.tbuf[k], N);
   ALLOC(A.hx[0], N); ALLOC(A.hx[1], N);
   ALLOC(A.stamps, (size_t)kStamps);
+  ALLOC(A.check, (size_t)4);
   ALLOC(A.b, N); ALLOC(A.y, N); ALLOC(A.r, N); ALLOC(A.p, N); ALLOC(A.q, N); ALLOC(A.p2, N);
   ALLOC(A.y32, N4); ALLOC(A.r32, N4); ALLOC(A.p32, N4); ALLOC(A.q32, N4); ALLOC(A.p232, N4);
   double *d_rho, *d_hc, *d_tau, *d_em = nullptr;
@@ -838,6 +861,7 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
   CK(cudaMemsetAsync(d_scal, 0, sizeof(InstScal) * count, c.stream));
   CK(cudaMemsetAsync(c.d_sctl, 0, sizeof(SolveCtl), c.stream));
   CK(cudaMemsetAsync(A.stamps, 0, sizeof(unsigned long long) * kStamps, c.stream));
+  CK(cudaMemsetAsync(A.check, 0, sizeof(unsigned long long) * 4, c.stream));
   for (void* p : {(void*)A.diag, (void*)A.cx, (void*)A.cy, (void*)A.cz, (void*)c.asm_.kappa,
                   (void*)d_rho, (void*)d_hc, (void*)d_tau, (void*)A.rhoc, (void*)A.ccat,
                   (void*)A.bvec, (void*)A.tau_s, (void*)A.a64x, (void*)A.a64y, (void*)A.a64z,
@@ -1623,6 +1647,29 @@ int hf_solve_profile(hf_ctx* h, int64_t cap, int64_t* rounds, int32_t* phases, d
     round_us[r] = (double)(sc.t_round[r] - prev) * 1e-3;
     prev = sc.t_round[r];
   }
+  return HF_OK;
+}
+
+int hf_index_checks(hf_ctx* h, int32_t probe, int32_t* enabled, int64_t* record) {
+  if (!h || !enabled) return set_err(HF_EARG, "null argument");
+  Ctx& c = h->c;
+  if (int r = refuse_queued(c)) return r;
+#ifdef HF_CHECKED
+  *enabled = 1;
+  if (probe) {
+    CU(launch_check_probe(c));
+    CU(cudaStreamSynchronize(c.stream));
+  }
+#else
+  *enabled = 0;
+  (void)probe;
+#endif
+  unsigned long long rec[4] = {0, 0, 0, 0};
+  CU(cudaMemcpyAsync(rec, c.A.check, sizeof(rec), cudaMemcpyDeviceToHost, c.stream));
+  CU(cudaMemsetAsync(c.A.check, 0, sizeof(rec), c.stream));
+  CU(cudaStreamSynchronize(c.stream));
+  if (record)
+    for (int k = 0; k < 4; ++k) record[k] = (int64_t)rec[k];
   return HF_OK;
 }
 

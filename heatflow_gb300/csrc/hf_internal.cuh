@@ -192,7 +192,41 @@ struct DevArrays {
   int64_t nsmall;           // instances with at most kWarpSumMax tasks (their partials: one warp)
   const int32_t* large;     // the other instances (block sums), nlarge of them
   int64_t nlarge;
+  // index-check record of the checked build (HF_CHECKED): [0] failed checks, [1] site of the
+  // first, [2] its index, [3] the extent it was checked against
+  unsigned long long* check;
 };
+
+// ---- index checks of the checked build ----------------------------------------------------------
+// Compiled with -DHF_CHECKED (build_library(checked=True): a separate library for tests), every
+// global load and store of the step kernels takes its index through HF_IX (one cell) or HF_IX4 (a
+// 4-cell vector, which must also start on a multiple of 4 cells: a 16-byte boundary for FP32, two
+// for FP64).  An index outside [0, n) -- n the extent of that array in the instance's layout -- is
+// recorded in DevArrays::check and replaced by 0, so the access stays inside the array and the
+// kernel goes on: no trap, no fault.  The host reports a record as HF_EDEVICE (the site is
+// 100000 * file + line).  In the normal build both macros are the index itself.
+#ifdef HF_CHECKED
+__device__ __noinline__ inline long long hf_check_ix(unsigned long long* rec, int site, long long i,
+                                                     long long n, int vec) {
+  const bool ok = i >= 0 && i + vec <= n && (vec == 1 || (i & (vec - 1)) == 0);
+  if (ok) return i;
+  if (rec) {
+    const unsigned long long k = atomicAdd(rec, 1ull);
+    if (k == 0ull) {
+      rec[1] = (unsigned long long)site;
+      rec[2] = (unsigned long long)i;
+      rec[3] = (unsigned long long)n;
+    }
+  }
+  return 0;
+}
+#define HF_SITE (HF_FILE_ID * 100000 + __LINE__)
+#define HF_IX(A, i, n) ((int)hf_check_ix((A).check, HF_SITE, (long long)(i), (long long)(n), 1))
+#define HF_IX4(A, i, n) ((int)hf_check_ix((A).check, HF_SITE, (long long)(i), (long long)(n), 4))
+#else
+#define HF_IX(A, i, n) (i)
+#define HF_IX4(A, i, n) (i)
+#endif
 
 // Slots of DevArrays::stamps: step begin, RHS start, RHS finalize start, solve start, end of the
 // solve's last round, step end.
@@ -387,6 +421,8 @@ struct TCell {
   __device__ bool act(int j) const { return x(j) < nx && y < ny; }   // column inside the grid
   __device__ int base(int j) const { return y * nx + x(j); }          // local index of (x, y, 0)
   __device__ int base4(int j) const { return y * sx + x(j); }         // the same in the FP32 layout
+  __device__ int n() const { return nxy * nz; }                       // cells of the instance
+  __device__ int n4() const { return nxy4 * nz; }                     // ... in the FP32 layout
 };
 __device__ __forceinline__ TCell task_cell(const DevArrays& A, int64_t task) {
   const int4 t = A.tasks[task];
@@ -456,5 +492,8 @@ cudaError_t launch_ctrl_select(Ctx& c, CtrlState* ctrl, cudaGraphConditionalHand
 enum { FIN_RHS = 0, FIN_RHS_DIAG, FIN_RES_INIT, FIN_RES, FIN_SPMV, FIN_UPD };
 cudaError_t launch_finalize(Ctx& c, int kind, CtrlState* ctrl, cudaGraphConditionalHandle hw,
                             int graph);
+#ifdef HF_CHECKED
+cudaError_t launch_check_probe(Ctx& c);   // one failed index check, no memory access
+#endif
 
 }  // namespace hf

@@ -13,6 +13,8 @@
 
 #include "hf_ctx.cuh"
 
+#define HF_FILE_ID 2   // index-check sites of the checked build: 100000 * file + line
+
 namespace hf {
 
 // Heat of one cell for heater case cs at step itime (mod_heating.f90:59-117).
@@ -70,6 +72,7 @@ __device__ __noinline__ double rhs_qdens(const DevArrays& A, const InstDesc& d, 
                                          int64_t off, int l, double tp) {
   double q = 0.0, qd = 0.0;
   {
+    l = HF_IX(A, l, d.n);
     const int cs = A.icase[off + l];
     if (cs > 0 && cs < 7) {
       const double P = r.has_power ? A.power[off + l] : r.power_in;
@@ -133,7 +136,7 @@ __device__ __forceinline__ void rhs4_task(const DevArrays& A, int64_t task, cons
   int flag = 0;
   if (act) {
     for (int z = za; z < zb; ++z) {
-      const int l = lxy + z * nxy;
+      const int l = HF_IX4(A, lxy + z * nxy, d.n);
       const double2* tp2 = reinterpret_cast<const double2*>(Tp + l);
       const double2* tq2 = reinterpret_cast<const double2*>(Tpp + l);
       const double2* rc2 = reinterpret_cast<const double2*>(rhoc + l);
@@ -225,7 +228,7 @@ __global__ void __launch_bounds__(kBlock, 4) k_rhs(DevArrays A, double* oB, doub
 #pragma unroll
     for (int j = 0; j < kXC; ++j) {
       if (!c.act(j)) continue;
-      const int l = c.base(j) + z * c.nxy;
+      const int l = HF_IX(A, c.base(j) + z * c.nxy, c.n());
       const double tp = Tp[l], tpp = Tpp[l];
       double q = 0.0, qd = 0.0;
       if (heater) {

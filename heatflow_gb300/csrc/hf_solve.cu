@@ -25,6 +25,8 @@
 
 #include "hf_ctx.cuh"
 
+#define HF_FILE_ID 3   // index-check sites of the checked build: 100000 * file + line
+
 namespace hf {
 
 template <typename T> struct Vec;
@@ -106,8 +108,8 @@ constexpr unsigned kFull = 0xffffffffu;
 
 // Value and z-face of plane z0-1 of chunk j (zeros at a non-periodic bottom face).
 template <typename T, typename C, class V>
-__device__ __forceinline__ void plane_below(const TCell& c, int j, V v, const C* __restrict__ cz,
-                                            T& vm, C& czm) {
+__device__ __forceinline__ void plane_below(const DevArrays& A, const TCell& c, int j, V v,
+                                            const C* __restrict__ cz, T& vm, C& czm) {
   vm = T(0);
   czm = C(0);
   if (!c.act(j) || c.nz < 2) return;
@@ -116,7 +118,7 @@ __device__ __forceinline__ void plane_below(const TCell& c, int j, V v, const C*
   else if (c.pz) l = c.base(j) + (c.nz - 1) * c.nxy;
   else return;
   vm = v(l);
-  czm = cz[l];
+  czm = cz[HF_IX(A, l, c.n())];
 }
 
 template <typename T, class V>
@@ -220,17 +222,18 @@ __device__ __forceinline__ void res_hx_task(const DevArrays& A, double* part, in
         prefetch_l2(yc + l + 4 * nxy);
         prefetch_l2(yp + l + 4 * nxy);
       }
-      double a = fma(-2.0, yc[l], b[l]);
-      a = a + yp[l];
-      if (tiny) a = fma(-kTiny, rsum[l], a);
+      const int lc = HF_IX(A, l, c.n());
+      double a = fma(-2.0, yc[lc], b[lc]);
+      a = a + yp[lc];
+      if (tiny) a = fma(-kTiny, rsum[lc], a);
       rr = fma(a, a, rr);
       if (sizeof(TR) == 4) {
-        const float g = -sinv32[l] * f64_to_f32_trunc(a) * isig;
-        R[lr] = (TR)g;
+        const float g = -sinv32[lc] * f64_to_f32_trunc(a) * isig;
+        R[HF_IX(A, lr, c.n4())] = (TR)g;
         gg = fmaf(g, g, gg);
       } else {
-        const double g = -sinv[l] * a;
-        R[lr] = (TR)g;
+        const double g = -sinv[lc] * a;
+        R[HF_IX(A, lr, c.n())] = (TR)g;
         gg64 = fma(g, g, gg64);
       }
     }
@@ -287,10 +290,11 @@ __device__ __forceinline__ void res_task(const DevArrays& A, double* part, int64
   const int nz = c.nz, nxy = c.nxy, base = c.base(0);
   const XEdge xe = x_edges(c);
   const int yn = y_north(c), ys = y_south(c);
-  auto xval = [&](int m) -> double { return X[m]; };
+  const int n = c.n();
+  auto xval = [&](int m) -> double { return X[HF_IX(A, m, n)]; };
   double xm, czm;
-  plane_below<double>(c, 0, xval, cz, xm, czm);
-  double xc = act ? X[base + c.z0 * nxy] : 0.0;
+  plane_below<double>(A, c, 0, xval, cz, xm, czm);
+  double xc = act ? xval(base + c.z0 * nxy) : 0.0;
   double rr = 0.0, gg64 = 0.0;
   float gg = 0.f;
   for (int z = c.z0; z < c.z1; ++z) {
@@ -308,15 +312,16 @@ __device__ __forceinline__ void res_task(const DevArrays& A, double* part, int64
         prefetch_l2(cy + lp);
         prefetch_l2(cz + lp);
       }
-      cxc = cx[l];
-      bl = b[l];
-      a = fma(-diag[l], xc, bl);
-      if (tiny) a = fma(-kTiny, rsum[l], a);
-      if (xe.w != kNoNbr) { xwl = X[l + xe.w]; cxwl = cx[l + xe.w]; }
-      if (xe.e != kNoNbr) xel = X[l + xe.e];
-      if (yn != kNoNbr) { cyn = cy[l]; xyn = X[l + yn]; }
-      if (ys != kNoNbr) { cys = cy[l + ys]; xys = X[l + ys]; }
-      czc = cz[l];
+      const int lc = HF_IX(A, l, n);
+      cxc = cx[lc];
+      bl = b[lc];
+      a = fma(-diag[lc], xc, bl);
+      if (tiny) a = fma(-kTiny, rsum[lc], a);
+      if (xe.w != kNoNbr) { xwl = xval(l + xe.w); cxwl = cx[HF_IX(A, l + xe.w, n)]; }
+      if (xe.e != kNoNbr) xel = xval(l + xe.e);
+      if (yn != kNoNbr) { cyn = cy[lc]; xyn = xval(l + yn); }
+      if (ys != kNoNbr) { cys = cy[HF_IX(A, l + ys, n)]; xys = xval(l + ys); }
+      czc = cz[lc];
     }
     const double up = __shfl_up_sync(kFull, xc, 1), cup = __shfl_up_sync(kFull, cxc, 1);
     const double dn = __shfl_down_sync(kFull, xc, 1);
@@ -333,14 +338,15 @@ __device__ __forceinline__ void res_task(const DevArrays& A, double* part, int64
       }
       if (INIT || sizeof(TR) == 8) rr = fma(a, a, rr);
       else rq.add(a);
-      if (!INIT) HX[l] = bl - a;
+      const int lc = HF_IX(A, l, n);
+      if (!INIT) HX[lc] = bl - a;
       if (sizeof(TR) == 4) {             // mixed: g in FP32, scaled by 1/sigma
-        const float g = -sinv32[l] * f64_to_f32_trunc(a) * isig;
-        R[rbase + z * rxy] = (TR)g;
+        const float g = -sinv32[lc] * f64_to_f32_trunc(a) * isig;
+        R[HF_IX(A, rbase + z * rxy, c.n4())] = (TR)g;
         gg = fmaf(g, g, gg);
       } else {                           // FP64 path: sigma = 1
-        const double g = -sinv[l] * a;
-        R[rbase + z * rxy] = (TR)g;
+        const double g = -sinv[lc] * a;
+        R[HF_IX(A, rbase + z * rxy, n)] = (TR)g;
         gg64 = fma(g, g, gg64);
       }
     }
@@ -386,11 +392,12 @@ __device__ __forceinline__ void xupd_task(const DevArrays& A, double* part, int6
       const int l = base + (z0 + u) * nxy;
       xv[u] = 0.0; yv[u] = TY(0); sv[u] = 0.0; sv32[u] = 0.f;
       if (z0 + u < c.z1) {
-        xv[u] = XR[l];
+        const int lc = HF_IX(A, l, c.n());
+        xv[u] = XR[lc];
         if (use_y) {
-          yv[u] = Y[ybase + (z0 + u) * yxy];
-          if (sizeof(TY) == 8) sv[u] = sinv[l];
-          else sv32[u] = sinv32[l];
+          yv[u] = Y[HF_IX(A, ybase + (z0 + u) * yxy, f32 ? c.n4() : c.n())];
+          if (sizeof(TY) == 8) sv[u] = sinv[lc];
+          else sv32[u] = sinv32[lc];
         }
       }
     }
@@ -404,7 +411,7 @@ __device__ __forceinline__ void xupd_task(const DevArrays& A, double* part, int6
         if (sizeof(TY) == 8) x = fma(sv[u], (double)yv[u], x);   // sigma = 1 on the FP64 path
         else x = x + f32_to_f64(sig * sv32[u] * (float)yv[u]);
       }
-      XW[l] = x;
+      XW[HF_IX(A, l, c.n())] = x;
     }
   }
 }
@@ -426,9 +433,9 @@ __device__ __forceinline__ void cgp_task(const DevArrays& A, double* part, int64
     T rv[4], pv[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-      const int l = base + (z0 + u) * nxy;
       rv[u] = T(0); pv[u] = T(0);
       if (z0 + u < c.z1) {
+        const int l = HF_IX(A, base + (z0 + u) * nxy, c.n());
         rv[u] = R[l];
         if (!first) pv[u] = Po[l];
       }
@@ -436,7 +443,7 @@ __device__ __forceinline__ void cgp_task(const DevArrays& A, double* part, int64
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       if (z0 + u >= c.z1) continue;
-      Pn[base + (z0 + u) * nxy] = first ? rv[u] : fma(beta, pv[u], rv[u]);
+      Pn[HF_IX(A, base + (z0 + u) * nxy, c.n())] = first ? rv[u] : fma(beta, pv[u], rv[u]);
     }
   }
 }
@@ -468,7 +475,11 @@ __device__ __forceinline__ void spmv_task(const DevArrays& A, double* part, int6
   const bool east_shfl = act && (c.x(0) + 1 < nx) && c.lane < 31;
   // raw operands of one direction value: p = first ? a : beta * b + a
   struct RP { T a, b; };
-  auto ld = [&](int m) -> RP { return RP{Src[m], first ? T(0) : Po[m]}; };
+  const int n = c.n();
+  auto ld = [&](int m) -> RP {
+    const int mc = HF_IX(A, m, n);
+    return RP{Src[mc], first ? T(0) : Po[mc]};
+  };
   auto pval = [&](const RP& v) -> T { return first ? v.a : fma(beta, v.b, v.a); };
   struct Plane { RP own, n, s, w, e; T axc, ayc, azc, ays, axw; };
   const RP z0v{T(0), T(0)};
@@ -480,12 +491,12 @@ __device__ __forceinline__ void spmv_task(const DevArrays& A, double* part, int6
       if (c.pz && nz > 1) o.own = ld(base);
       return;
     }
-    const int l = base + z * nxy;
+    const int l = base + z * nxy, lc = HF_IX(A, l, n);
     o.own = ld(l);
-    o.axc = ax[l]; o.ayc = ay[l]; o.azc = az[l];
+    o.axc = ax[lc]; o.ayc = ay[lc]; o.azc = az[lc];
     if (yn != kNoNbr) o.n = ld(l + yn);
-    if (ys != kNoNbr) { o.s = ld(l + ys); o.ays = ay[l + ys]; }
-    if (xe.w != kNoNbr) { o.w = ld(l + xe.w); o.axw = ax[l + xe.w]; }
+    if (ys != kNoNbr) { o.s = ld(l + ys); o.ays = ay[HF_IX(A, l + ys, n)]; }
+    if (xe.w != kNoNbr) { o.w = ld(l + xe.w); o.axw = ax[HF_IX(A, l + xe.w, n)]; }
     if (xe.e != kNoNbr) o.e = ld(l + xe.e);
   };
   // plane below the task (z0 - 1, or the periodic wrap to nz - 1)
@@ -494,7 +505,7 @@ __device__ __forceinline__ void spmv_task(const DevArrays& A, double* part, int6
     int lb = -1;
     if (c.z0 > 0) lb = base + (c.z0 - 1) * nxy;
     else if (c.pz) lb = base + (nz - 1) * nxy;
-    if (lb >= 0) { pm = pval(ld(lb)); azm = az[lb]; }
+    if (lb >= 0) { pm = pval(ld(lb)); azm = az[HF_IX(A, lb, n)]; }
   }
   Plane cur, nxt;
   load(c.z0, cur);
@@ -522,8 +533,9 @@ __device__ __forceinline__ void spmv_task(const DevArrays& A, double* part, int6
         acc = fma(cur.azc, pval(nxt.own), acc);
         acc = fma(azm, pm, acc);
       }
-      if (FUSED) Pn[l] = pc;
-      Q[l] = acc;
+      const int lc = HF_IX(A, l, n);
+      if (FUSED) Pn[lc] = pc;
+      Q[lc] = acc;
       pq = fma(pc, acc, pq);
     }
     pm = pc; azm = cur.azc;
@@ -561,9 +573,9 @@ __device__ __forceinline__ void upd_task(const DevArrays& A, double* part, int64
       T pv[4], qv[4], rv[4], yv[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        const int l = base + (z0 + u) * nxy;
         pv[u] = T(0); qv[u] = T(0); rv[u] = T(0); yv[u] = T(0);
         if (z0 + u < c.z1) {
+          const int l = HF_IX(A, base + (z0 + u) * nxy, c.n());
           pv[u] = P[l]; qv[u] = Q[l]; rv[u] = R[l];
           if (!first) yv[u] = Y[l];
         }
@@ -571,7 +583,7 @@ __device__ __forceinline__ void upd_task(const DevArrays& A, double* part, int64
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         if (z0 + u >= c.z1) continue;
-        const int l = base + (z0 + u) * nxy;
+        const int l = HF_IX(A, base + (z0 + u) * nxy, c.n());
         Y[l] = first ? alpha * pv[u] : fma(alpha, pv[u], yv[u]);
         const T r = fma(-alpha, qv[u], rv[u]);
         R[l] = r;
@@ -671,9 +683,11 @@ __device__ __forceinline__ void spmv4_task(const DevArrays& A, double* part, int
   auto pv4 = [&](const float4& a, const float4& b) -> float4 {
     return make_float4(pv(a.x, b.x), pv(a.y, b.y), pv(a.z, b.z), pv(a.w, b.w));
   };
+  const int n4 = nxy * nz;               // the instance's cells in the FP32 layout
   auto ldp = [&](int l, float4& r, float4& po) {
-    r = ld4(Src + l);
-    po = first ? zero4 : ld4(Po + l);
+    const int lc = HF_IX4(A, l, n4);
+    r = ld4(Src + lc);
+    po = first ? zero4 : ld4(Po + lc);
   };
   const int lxy = y * sx + x;
   // plane below the group (za - 1, or the periodic wrap to nz - 1), and the group's first plane
@@ -687,7 +701,7 @@ __device__ __forceinline__ void spmv4_task(const DevArrays& A, double* part, int
         float4 rb, pob;
         ldp(lb, rb, pob);
         pm = pv4(rb, pob);
-        azm = ld4(az + lb);
+        azm = ld4(az + HF_IX4(A, lb, n4));
       }
     }
     ldp(lxy + za * nxy, rc, poc);
@@ -703,22 +717,25 @@ __device__ __forceinline__ void spmv4_task(const DevArrays& A, double* part, int
         if (z + 1 < nz) ldp(l + nxy, ru, pou);
         else if (d.pz) ldp(lxy, ru, pou);
       }
-      axv = ld4(ax + l); ayv = ld4(ay + l); azv = ld4(az + l);
+      const int lc = HF_IX4(A, l, n4);
+      axv = ld4(ax + lc); ayv = ld4(ay + lc); azv = ld4(az + lc);
       if (z + 1 < zb) {
         prefetch_l2(ax + l + nxy);
         prefetch_l2(ay + l + nxy);
         prefetch_l2(az + l + nxy);
       }
       if (hn) ldp(l + dn, rn, pon);
-      if (hs) { ldp(l + ds, rs, pos); aysv = ld4(ay + l + ds); }
+      if (hs) { ldp(l + ds, rs, pos); aysv = ld4(ay + HF_IX4(A, l + ds, n4)); }
       if (wload && hw) {
-        rw = Src[l + dw];
-        pow_ = first ? 0.f : Po[l + dw];
-        axwl = ax[l + dw];
+        const int lw = HF_IX(A, l + dw, n4);
+        rw = Src[lw];
+        pow_ = first ? 0.f : Po[lw];
+        axwl = ax[lw];
       }
       if (eload && he) {
-        re = Src[l + de];
-        poe = first ? 0.f : Po[l + de];
+        const int le = HF_IX(A, l + de, n4);
+        re = Src[le];
+        poe = first ? 0.f : Po[le];
       }
     }
     const float4 p = pv4(rc, poc);
@@ -752,8 +769,9 @@ __device__ __forceinline__ void spmv4_task(const DevArrays& A, double* part, int
         pq = fmaf(pc, acc, pq);
         if (i == 0) qv.x = acc; else if (i == 1) qv.y = acc; else if (i == 2) qv.z = acc; else qv.w = acc;
       }
-      if (FUSED) st4(Pn + l, p);
-      st4(Q + l, qv);
+      const int ls = HF_IX4(A, l, n4);
+      if (FUSED) st4(Pn + ls, p);
+      st4(Q + ls, qv);
       pm = p;
       azm = azv;
       rc = ru;
@@ -790,6 +808,7 @@ __device__ __forceinline__ void stv4(double* p, const V4<double>& v) {
 struct Quad {
   int64_t off, voff;
   int nxy, lxy, dxy, dlxy, za, zb, nx, x;
+  int vn, dn;        // cells of the instance in the vectors' layout and in the FP64 layout
   bool act, padded;
 };
 template <bool F32>
@@ -815,17 +834,20 @@ __device__ __forceinline__ Quad quad_cell(const DevArrays& A, int64_t task) {
   c.za = min(tk.w + grp * per, z1);
   c.zb = min(c.za + per, z1);
   c.act = qp.act;
+  c.vn = c.nxy * d.nz;
+  c.dn = c.dxy * d.nz;
   return c;
 }
 
 // The FP64-layout diagonal of a quad's cells (zeros for padding cells).
-__device__ __forceinline__ V4<double> diag4(const double* __restrict__ diag, const Quad& c, int z) {
+__device__ __forceinline__ V4<double> diag4(const DevArrays& A, const double* __restrict__ diag,
+                                            const Quad& c, int z) {
   const int l = c.dlxy + z * c.dxy;
-  if (!c.padded) return ldv4(diag + l);
+  if (!c.padded) return ldv4(diag + HF_IX4(A, l, c.dn));
   V4<double> v{};
 #pragma unroll
   for (int i = 0; i < 4; ++i)
-    if (c.x + i < c.nx) v.v[i] = diag[l + i];
+    if (c.x + i < c.nx) v.v[i] = diag[HF_IX(A, l + i, c.dn)];
   return v;
 }
 
@@ -846,7 +868,8 @@ __device__ __forceinline__ void upd4_task(const DevArrays& A, double* part, int6
   if (c.act) {
     for (int z = c.za; z < c.zb; z += 2) {
       const bool two = z + 1 < c.zb;
-      const int l0 = c.lxy + z * c.nxy, l1 = l0 + c.nxy;
+      const int l0 = HF_IX4(A, c.lxy + z * c.nxy, c.vn);
+      const int l1 = two ? HF_IX4(A, l0 + c.nxy, c.vn) : 0;
       V4<T> p0 = ldv4(P + l0), q0 = ldv4(Q + l0), r0 = ldv4(R + l0), y0{}, p1{}, q1{}, r1{}, y1{};
       if (!first) y0 = ldv4(Y + l0);
       if (two) {
@@ -863,7 +886,7 @@ __device__ __forceinline__ void upd4_task(const DevArrays& A, double* part, int6
         const V4<T>& yv = h ? y1 : y0;
         V4<T> yo, ro;
         V4<double> dg{};
-        if (weighted) dg = diag4(diag, c, z + h);
+        if (weighted) dg = diag4(A, diag, c, z + h);
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
           yo.v[i] = first ? alpha * pv.v[i] : fma(alpha, pv.v[i], yv.v[i]);
@@ -898,7 +921,8 @@ __device__ __forceinline__ void cgp4_task(const DevArrays& A, double* part, int6
   T* Pn = Vec<T>::pb(A, k) + c.voff;
   for (int z = c.za; z < c.zb; z += 2) {
     const bool two = z + 1 < c.zb;
-    const int l0 = c.lxy + z * c.nxy, l1 = l0 + c.nxy;
+    const int l0 = HF_IX4(A, c.lxy + z * c.nxy, c.vn);
+    const int l1 = two ? HF_IX4(A, l0 + c.nxy, c.vn) : 0;
     V4<T> r0 = ldv4(R + l0), o0{}, r1{}, o1{};
     if (!first) o0 = ldv4(Po + l0);
     if (two) {
@@ -931,7 +955,8 @@ __device__ __forceinline__ void xupd4_task(const DevArrays& A, double* part, int
   const float sig = (float)s.sigma_prev;
   for (int z = c.za; z < c.zb; z += 2) {
     const bool two = z + 1 < c.zb;
-    const int l0 = c.lxy + z * c.nxy, l1 = l0 + c.nxy;
+    const int l0 = HF_IX4(A, c.lxy + z * c.nxy, c.vn);
+    const int l1 = two ? HF_IX4(A, l0 + c.nxy, c.vn) : 0;
     V4<double> x0 = ldv4(XR + l0), x1{}, s0{}, s1{};
     V4<TY> y0{}, y1{};
     V4<float> f0{}, f1{};
@@ -991,7 +1016,7 @@ __device__ __forceinline__ void res_hx4_task(const DevArrays& A, double* part, i
   float gg = 0.f;
   if (c.act) {
     for (int z = c.za; z < c.zb; ++z) {
-      const int l = c.lxy + z * c.nxy;
+      const int l = HF_IX4(A, c.lxy + z * c.nxy, c.vn);
       const V4<double> bv = ldv4(b + l), cv = ldv4(yc + l), pv = ldv4(yp + l);
       V4<double> rs{}, s64{};
       V4<float> s32{};
@@ -1703,6 +1728,16 @@ cudaError_t launch_solve(Ctx& c, unsigned long long wait_ns, int leaver) {
   if (fp32) return cudaLaunchKernelEx(&cfg, k_solve<float>, c.A, c.d_sctl, limit, wait_ns, leaver);
   return cudaLaunchKernelEx(&cfg, k_solve<double>, c.A, c.d_sctl, limit, wait_ns, leaver);
 }
+
+#ifdef HF_CHECKED
+// One failed check and no memory access (the index is only compared with its range), so a test
+// can see a failed check recorded and reported.
+__global__ void k_check_probe(DevArrays A) { (void)HF_IX(A, -1, 1); }
+cudaError_t launch_check_probe(Ctx& c) {
+  k_check_probe<<<1, 1, 0, c.stream>>>(c.A);
+  return cudaGetLastError();
+}
+#endif
 
 // ---- launchers ---------------------------------------------------------------------------------
 cudaError_t launch_step_begin(Ctx& c, int64_t itime, int) {

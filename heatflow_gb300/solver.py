@@ -61,18 +61,31 @@ def make_opts(precision="fp64", criterion="recursive", tol=None, itmax=50000, in
 
 
 class HeatFlow:
-    def __init__(self, problems: Union[Problem, Sequence[Problem]], **opts):
-        self.lib = abi.load_library()
+    def __init__(self, problems: Union[Problem, Sequence[Problem]], library=None, **opts):
+        """library: the loaded CUDA library to run on (default: abi.load_library(); the tests
+        pass the index-checked build, abi.load_library(checked=True))."""
+        self.lib = library or abi.load_library()
         self.problems = [problems] if isinstance(problems, Problem) else list(problems)
         self.opts = make_opts(**opts)
         arr = (abi.HfProblem * len(self.problems))(*[p.to_c() for p in self.problems])
         self._arr = arr
         h = C.c_void_p()
-        abi.check(self.lib.hf_create_batch(arr, len(self.problems), C.byref(self.opts), C.byref(h)),
+        self._check(self.lib.hf_create_batch(arr, len(self.problems), C.byref(self.opts), C.byref(h)),
                   "hf_create")
         self.h = h
         self.sizes = [p.ncells for p in self.problems]
         self.n = sum(self.sizes)
+
+    def _check(self, code: int, where: str):
+        abi.check(code, where, self.lib)
+
+    def index_checks(self, probe: bool = False):
+        """(enabled, record) of the index checks: enabled is True in the checked build; record =
+        [failed checks, site of the first, its index, the extent]; the record is cleared."""
+        en = C.c_int32()
+        rec = (C.c_int64 * 4)()
+        self._check(self.lib.hf_index_checks(self.h, int(probe), C.byref(en), rec), "hf_index_checks")
+        return bool(en.value), list(rec)
 
     def close(self):
         if getattr(self, "h", None):
@@ -94,12 +107,12 @@ class HeatFlow:
     def set_stream(self, stream_handle: int):
         """Run on an existing CUDA stream (cudaStream_t as an integer, e.g. torch's
         ``stream.cuda_stream``); 0 returns to the context's own stream."""
-        abi.check(self.lib.hf_set_stream(self.h, C.c_void_p(stream_handle or None)), "hf_set_stream")
+        self._check(self.lib.hf_set_stream(self.h, C.c_void_p(stream_handle or None)), "hf_set_stream")
 
     def time_kernel(self, kernel: int, reps: int = 20) -> float:
         """Mean duration (ms) of one launch of a step kernel, CUDA-event timed."""
         ms = C.c_double()
-        abi.check(self.lib.hf_time_kernel(self.h, int(kernel), int(reps), C.byref(ms)), "hf_time_kernel")
+        self._check(self.lib.hf_time_kernel(self.h, int(kernel), int(reps), C.byref(ms)), "hf_time_kernel")
         return ms.value
 
     def solve_profile(self, cap: int = 64):
@@ -108,7 +121,7 @@ class HeatFlow:
         rounds = C.c_int64()
         ph = (C.c_int32 * cap)()
         us = (C.c_double * cap)()
-        abi.check(self.lib.hf_solve_profile(self.h, cap, C.byref(rounds), ph, us), "hf_solve_profile")
+        self._check(self.lib.hf_solve_profile(self.h, cap, C.byref(rounds), ph, us), "hf_solve_profile")
         n = min(rounds.value, cap, 64)
         return [(abi.PHASE_NAMES.get(ph[i], str(ph[i])), us[i]) for i in range(n)], rounds.value
 
@@ -116,7 +129,7 @@ class HeatFlow:
         """Microseconds of the latest step: step begin -> RHS, RHS -> its finalize, finalize ->
         persistent solve, solve (to the end of its last round), -> step end (None where absent)."""
         us = (C.c_double * 5)()
-        abi.check(self.lib.hf_step_timeline(self.h, us), "hf_step_timeline")
+        self._check(self.lib.hf_step_timeline(self.h, us), "hf_step_timeline")
         keys = ("begin_to_rhs", "rhs", "finalize", "solve", "solve_to_end")
         return {k: (us[i] if us[i] >= 0 else None) for i, k in enumerate(keys)}
 
@@ -126,7 +139,7 @@ class HeatFlow:
         order).  After every step each such cell takes its properties at its new T^n and the
         operator is rebuilt on the device.  An empty list returns to fixed properties."""
         if not tables:
-            abi.check(self.lib.hf_set_property_tables(self.h, 0, None, None, None),
+            self._check(self.lib.hf_set_property_tables(self.h, 0, None, None, None),
                       "hf_set_property_tables")
             return
         offsets = np.cumsum([0] + [len(t) for t in tables]).astype(np.int32)
@@ -134,7 +147,7 @@ class HeatFlow:
         ct = np.ascontiguousarray(cell_table, np.int32)
         assert ct.size == self.n
         self._tables = (offsets, rows, ct)      # the library copies them; keep until the call ends
-        abi.check(self.lib.hf_set_property_tables(
+        self._check(self.lib.hf_set_property_tables(
             self.h, len(tables), offsets.ctypes.data_as(C.POINTER(C.c_int32)), _d(rows),
             ct.ctypes.data_as(C.POINTER(C.c_int32))), "hf_set_property_tables")
 
@@ -149,19 +162,19 @@ class HeatFlow:
             out = np.empty(n)
         assert out.dtype == np.float64 and out.flags.c_contiguous and out.size == n
         t = C.c_int64()
-        abi.check(self.lib.hf_subbox_async(self.h, int(instance), lo, hi, int(which), _d(out),
+        self._check(self.lib.hf_subbox_async(self.h, int(instance), lo, hi, int(which), _d(out),
                                            C.byref(t)), "hf_subbox_async")
         return t.value, out
 
     def subbox_wait(self, ticket: int):
-        abi.check(self.lib.hf_subbox_wait(self.h, int(ticket)), "hf_subbox_wait")
+        self._check(self.lib.hf_subbox_wait(self.h, int(ticket)), "hf_subbox_wait")
 
     def autotune(self, itime0: int = 1, steps: int = 3):
         """Choose the task depth (and, mixed, the inner tolerance) by timing `steps` steps of this
         problem per candidate; state and statistics are unchanged.  Returns the candidates."""
         res = (abi.HfTuneResult * 16)()
         n = C.c_int32()
-        abi.check(self.lib.hf_autotune(self.h, int(itime0), int(steps), res, 16, C.byref(n)),
+        self._check(self.lib.hf_autotune(self.h, int(itime0), int(steps), res, 16, C.byref(n)),
                   "hf_autotune")
         out = [dict(task_depth=r.task_depth, inner_tol=r.inner_tol, ms_per_step=r.ms_per_step,
                     chosen=bool(r.chosen)) for r in res[:n.value]]
@@ -173,14 +186,14 @@ class HeatFlow:
     # ---- options
     def set_opts(self, **opts):
         self.opts = make_opts(**opts)
-        abi.check(self.lib.hf_set_opts(self.h, C.byref(self.opts)), "hf_set_opts")
+        self._check(self.lib.hf_set_opts(self.h, C.byref(self.opts)), "hf_set_opts")
 
     # ---- state
     def set_state(self, tp, tpp):
         tp = np.ascontiguousarray(tp, np.float64)
         tpp = np.ascontiguousarray(tpp, np.float64)
         assert tp.size == self.n and tpp.size == self.n
-        abi.check(self.lib.hf_set_state(self.h, _d(tp), _d(tpp)), "hf_set_state")
+        self._check(self.lib.hf_set_state(self.h, _d(tp), _d(tpp)), "hf_set_state")
 
     def initial_evolve(self):
         """Temp_p = Temp_pp = T_System (mod_init_evolve.f90:47-48)."""
@@ -197,7 +210,7 @@ class HeatFlow:
             if a is not None:
                 assert a.dtype == np.float64 and a.flags.c_contiguous and a.size == self.n
         tp, tpp = out
-        abi.check(self.lib.hf_get_state(self.h, _d(tp) if tp is not None else None,
+        self._check(self.lib.hf_get_state(self.h, _d(tp) if tp is not None else None,
                                         _d(tpp) if tpp is not None else None), "hf_get_state")
         return tp, tpp
 
@@ -211,12 +224,12 @@ class HeatFlow:
     # ---- stepping
     def simulate(self, itime: int) -> dict:
         st = abi.HfStats()
-        abi.check(self.lib.hf_step(self.h, int(itime), C.byref(st)), "simulate")
+        self._check(self.lib.hf_step(self.h, int(itime), C.byref(st)), "simulate")
         return st.as_dict()
 
     def run(self, itime0: int, nsteps: int) -> dict:
         st = abi.HfStats()
-        abi.check(self.lib.hf_run(self.h, int(itime0), int(nsteps), C.byref(st)), "run")
+        self._check(self.lib.hf_run(self.h, int(itime0), int(nsteps), C.byref(st)), "run")
         return st.as_dict()
 
     def step_host_async(self, itime: int, tp, tpp, out):
@@ -225,49 +238,49 @@ class HeatFlow:
         for a in (tp, tpp, out):
             assert a.dtype == np.float64 and a.flags.c_contiguous and a.size == self.n
         self._queued = getattr(self, "_queued", []) + [(tp, tpp, out)]
-        abi.check(self.lib.hf_step_host_async(self.h, int(itime), _d(tp), _d(tpp), _d(out)),
+        self._check(self.lib.hf_step_host_async(self.h, int(itime), _d(tp), _d(tpp), _d(out)),
                   "hf_step_host_async")
 
     def host_sync(self) -> dict:
         st = abi.HfStats()
         self._queued = []
-        abi.check(self.lib.hf_host_sync(self.h, C.byref(st)), "hf_host_sync")
+        self._check(self.lib.hf_host_sync(self.h, C.byref(st)), "hf_host_sync")
         return st.as_dict()
 
     # ---- parity probes
     def operator(self):
         out = [np.empty(self.n) for _ in range(4)]
-        abi.check(self.lib.hf_get_operator(self.h, *[_d(a) for a in out]), "hf_get_operator")
+        self._check(self.lib.hf_get_operator(self.h, *[_d(a) for a in out]), "hf_get_operator")
         return dict(zip(("diag", "cx", "cy", "cz"), out))
 
     def rhs(self, itime: int):
         out = [np.empty(self.n) for _ in range(6)]
-        abi.check(self.lib.hf_get_rhs(self.h, int(itime), *[_d(a) for a in out]), "hf_get_rhs")
+        self._check(self.lib.hf_get_rhs(self.h, int(itime), *[_d(a) for a in out]), "hf_get_rhs")
         return dict(zip(("B", "Q", "Qdens", "S_cat", "S", "x0"), out))
 
     def atimes(self, x):
         x = np.ascontiguousarray(x, np.float64)
         y = np.empty(self.n)
-        abi.check(self.lib.hf_apply_operator(self.h, _d(x), _d(y)), "atimes")
+        self._check(self.lib.hf_apply_operator(self.h, _d(x), _d(y)), "atimes")
         return y
 
     def linbcg(self, b, x):
         b = np.ascontiguousarray(b, np.float64)
         x = np.array(x, np.float64, copy=True)
         st = abi.HfStats()
-        abi.check(self.lib.hf_solve(self.h, _d(b), _d(x), C.byref(st)), "linbcg")
+        self._check(self.lib.hf_solve(self.h, _d(b), _d(x), C.byref(st)), "linbcg")
         return x, st.as_dict()
 
     def sparse_hmatrix(self, instance: int = 0):
         ln = C.c_int64()
-        abi.check(self.lib.hf_assemble_coo(self.h, instance, 0, None, None, None, C.byref(ln), None),
+        self._check(self.lib.hf_assemble_coo(self.h, instance, 0, None, None, None, C.byref(ln), None),
                   "hf_assemble_coo")
         cap = ln.value
         irow = np.empty(cap, np.int64)
         jcol = np.empty(cap, np.int64)
         val = np.empty(cap, np.float64)
         cnt = C.c_int64()
-        abi.check(self.lib.hf_assemble_coo(self.h, instance, cap, irow.ctypes.data_as(_ip),
+        self._check(self.lib.hf_assemble_coo(self.h, instance, cap, irow.ctypes.data_as(_ip),
                                            jcol.ctypes.data_as(_ip), _d(val), C.byref(ln),
                                            C.byref(cnt)), "hf_assemble_coo")
         return irow, jcol, val, cnt.value

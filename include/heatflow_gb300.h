@@ -273,6 +273,20 @@ enum {
  * round's length in microseconds (device %globaltimer; round 0 counts from the kernel's start). */
 int hf_solve_profile(hf_ctx* ctx, int64_t cap, int64_t* rounds, int32_t* phases, double* round_us);
 
+/* ---- index checks ------------------------------------------------------------------------------
+ * No counterpart in the reference (the reference has no bounds-checked build; this stands in for a
+ * memory checker, which is not available on the GPUs this library is tested on).  The library can
+ * be built with -DHF_CHECKED (a separate build for tests): every global load and store of the
+ * step kernels then checks its index against the extent of its array in the instance's layout
+ * (4-cell vector accesses also their 16-byte alignment); a failed check is recorded on the device
+ * and the access is moved inside the array, with no trap and no fault, and the next call that
+ * finishes steps returns HF_EDEVICE naming the first failed check's site in hf_last_error.
+ * hf_index_checks sets *enabled = 1 in the checked build (0 otherwise), copies the record
+ * {failed checks, site of the first (100000 * file + line), its index, the extent} to record
+ * (4 values, or NULL) and clears it.  probe != 0 (checked build only) first runs one check on an
+ * index outside its range without any memory access, so a test can see a failure recorded. */
+int hf_index_checks(hf_ctx* ctx, int32_t probe, int32_t* enabled, int64_t* record);
+
 /* ---- temperature-dependent properties -------------------------------------------------------
  * The reference's TempDepProp = 1 rebuilds H after every step from unchanged properties (its
  * table lookup is commented out, mod_tempdep.f90:66-95; the rebuild is called at
