@@ -96,3 +96,79 @@ def test_config_inclusions_512_100_steps(cuda_lib):
           f"max rise {np.max(T64) - 300.0:.4g} K")
     assert err_T <= 1e-8
     assert err_rise <= 1e-5
+
+
+# ---- oracle legs at size: the FP64 GPU field tied to the reference's arithmetic ------------------
+def _cpu_pcg_run(prob, steps, tol=1e-13):
+    """The clean CPU solver (oracle/cpu_pcg.c: the oracle's operator bit for bit, Jacobi-PCG in
+    FP64 to the true relative residual `tol`, all host cores) over `steps` steps."""
+    import os
+    from oracle.oracle import CleanPCG, Oracle
+    o = Oracle(prob)
+    o.set_state(*prob.initial_state())
+    cp = CleanPCG(o, threads=os.cpu_count() or 1)
+    for k in range(steps):
+        rc, _, rel = cp.step(k + 1, tol=tol)
+        assert rc == 0 and rel <= tol, (k, rc, rel)
+    return o.get_state()[0]
+
+
+def _gpu_run(probs, steps, precision):
+    tol = 1e-13 if precision == "fp64" else 1e-10
+    with HeatFlow(probs, precision=precision, criterion="true", tol=tol, use_graph=1) as hf:
+        hf.initial_evolve()
+        st = hf.run(1, steps)
+        T = hf.get_state()[0]
+        parts = hf.split(T) if isinstance(probs, list) else [T]
+    assert st["unconverged"] == 0
+    return parts
+
+
+def test_config_layered_slab_128_vs_oracle(cuda_lib):
+    """128^3 layered slab (Cattaneo), 10 steps: the FP64 GPU field against the oracle's BiCG (the
+    reference's COO Jacobi-BiCG, tol 1e-12) within 1e-10 relative L2; the mixed field within 1e-9."""
+    from oracle.oracle import Oracle, set_threads
+    import os
+    prob = layered_slab(128, icattaneo=1)
+    set_threads(os.cpu_count() or 1)
+    o = Oracle(prob)
+    o.set_state(*prob.initial_state())
+    for k in range(10):
+        rc, _, _ = o.simulate(k + 1, mode=0, tol=1e-12, itmax=50000)
+        assert rc == 0
+    Tref = o.get_state()[0]
+    (T64,) = _gpu_run(prob, 10, "fp64")
+    (T32,) = _gpu_run(prob, 10, "mixed")
+    e64, e32 = _rel(T64, Tref), _rel(T32, Tref)
+    print(f"\nconfig 2 at 128^3, 10 steps vs oracle BiCG: FP64 {e64:.3e}, mixed {e32:.3e}")
+    assert e64 <= 1e-10 and e32 <= 1e-9
+
+
+def test_config_batched_sweep_all_instances_vs_cpu(cuda_lib):
+    """All 256 grids of the batched sweep, 20 steps in one persistent launch per step: every
+    instance's FP64 GPU field within 1e-10 relative L2 of the CPU FP64 solver (true rel-res
+    1e-13) on the same grid, and every mixed field within 1e-9."""
+    probs = batched_sweep(256, seed=0)
+    g64 = _gpu_run(probs, 20, "fp64")
+    g32 = _gpu_run(probs, 20, "mixed")
+    worst64 = worst32 = 0.0
+    for i, p in enumerate(probs):
+        Tref = _cpu_pcg_run(p, 20)
+        e64, e32 = _rel(g64[i], Tref), _rel(g32[i], Tref)
+        worst64, worst32 = max(worst64, e64), max(worst32, e32)
+        assert e64 <= 1e-10, (i, e64)
+        assert e32 <= 1e-9, (i, e32)
+    print(f"\nconfig 3, 256 instances x 20 steps vs CPU FP64 PCG: worst FP64 {worst64:.3e}, "
+          f"worst mixed {worst32:.3e}")
+
+
+def test_config_inclusions_512_vs_cpu(cuda_lib):
+    """512^3 inclusion grid (periodic x/y), 3 steps: the FP64 GPU field within 1e-10 relative L2
+    of the CPU FP64 solver on the same grid, the mixed field within 1e-9."""
+    prob = inclusions(512)
+    (T64,) = _gpu_run(prob, 3, "fp64")
+    (T32,) = _gpu_run(prob, 3, "mixed")
+    Tref = _cpu_pcg_run(prob, 3)
+    e64, e32 = _rel(T64, Tref), _rel(T32, Tref)
+    print(f"\nconfig 5 at 512^3, 3 steps vs CPU FP64 PCG: FP64 {e64:.3e}, mixed {e32:.3e}")
+    assert e64 <= 1e-10 and e32 <= 1e-9
