@@ -46,9 +46,9 @@ BYTES_PER_CELL = {
     "rhs": 6 * 8 + 1 + 2 * 8,
     # mixed: x, diag, cx, cy, cz, S (8 B) + 1/sqrt|H_II| (4 B) read; g (4 B) + H x (8 B) written
     "residual_mixed": 6 * 8 + 4 + 4 + 8,
-    # mixed step start from the stored products: S, H T^n, H T^(n-1), H*1 (8 B) + 1/sqrt|H_II|
-    # (4 B) read; g (4 B) written
-    "residual_init_hx_mixed": 4 * 8 + 4 + 4,
+    # mixed step start from the stored products: S, H T^n, H T^(n-1) (8 B) + 1/sqrt|H_II| (4 B)
+    # read; g (4 B) written (no +TINY under the true-residual criterion, so no H*1)
+    "residual_init_hx_mixed": 3 * 8 + 4 + 4,
     # FP64: x, diag, cx, cy, cz, S, 1/sqrt|H_II| (8 B) read; g, H x (8 B) written
     "residual_fp64": 7 * 8 + 8 + 8,
     # direction update: r, p_old read, p written; SpMV: p, ax, ay, az read, q written
@@ -63,20 +63,20 @@ BYTES_PER_CELL = {
 }
 # FP64 floating-point operations per cell (an FMA counts 2) of the FP64-pipe kernels: the
 # residual does 7 FMA for S - Hx, 1 FMA for ||r||^2 and 1 sub for H x = S - r; the step-start
-# residual from the stored products 1 FMA + 1 add (S - 2 H T^n + H T^(n-1)), 1 FMA (TINY) and 1 FMA
+# residual from the stored products 1 FMA + 1 add (S - 2 H T^n + H T^(n-1)) and 1 FMA
 # (||r||^2); the RHS 2 mul (rho c T/dt), 1 FMA + 1 mul (S_cat), 1 add, 2 add (x0) - its x0 - T <
 # TINY test and ||S||^2 run on the integer/FP32 pipes.
-FP64_FLOPS_PER_CELL = {"residual_mixed": 17, "residual_fp64": 19, "residual_init_hx_mixed": 7,
+FP64_FLOPS_PER_CELL = {"residual_mixed": 17, "residual_fp64": 19, "residual_init_hx_mixed": 5,
                        "rhs": 8}
 
 # Algorithmic bytes per cell of each round of the persistent solve kernel (k_solve), by phase:
-# (bytes, bytes of the first inner iteration / of an update without a correction).  The first
-# residual also reads H*1 (the x0 + TINY rule applies on this workload: far-field cells do not
-# move, so x0 - T < TINY somewhere every step).
+# (bytes, bytes of the first inner iteration / of an update without a correction).  Under the
+# true-residual criterion the reference's +TINY on x0 is not applied (it moves only the starting
+# point), so the first residual does not read H*1.
 PHASE_BYTES = {
-    "mixed": {"res_init": (64, 64), "res_init_hx": (40, 40), "res": (64, 64), "cg_p": (12, 8),
+    "mixed": {"res_init": (56, 56), "res_init_hx": (32, 32), "res": (64, 64), "cg_p": (12, 8),
               "cg_q": (20, 20), "cg_pq": (28, 24), "cg_b": (24, 20), "xupd": (24, 16)},
-    "fp64": {"res_init": (72, 72), "res_init_hx": (48, 48), "res": (72, 72), "cg_p": (24, 16),
+    "fp64": {"res_init": (64, 64), "res_init_hx": (40, 40), "res": (72, 72), "cg_p": (24, 16),
              "cg_q": (40, 40), "cg_b": (48, 40), "xupd": (32, 16)},
 }
 
@@ -114,11 +114,11 @@ def solve_bytes_per_cell(rounds, precision):
 
 # FP64 instructions per cell of each round (the rest of the work is FP32/integer): the mixed
 # path's residual sweep 7 FMA + 1 sub (||r||^2 in FP32), its pointwise first residual 1 FMA + 1 add
-# + 1 FMA (TINY) + 1 FMA (||r||^2), the stencil first residual 7 + 1 + 1 FMA, the x update 1 add.
+# + 1 FMA (||r||^2), the stencil first residual 7 + 1 FMA, the x update 1 add.
 PHASE_FP64_INSTR = {
-    "mixed": {"res_init_hx": 4, "res_init": 9, "res": 8, "xupd": 1},
-    "fp64": {"res_init_hx": 6, "res_init": 11, "res": 10, "xupd": 1, "cg_p": 1, "cg_q": 8,
-             "cg_b": 4},
+    "mixed": {"res_init_hx": 3, "res_init": 8, "res": 8, "xupd": 1},
+    "fp64": {"res_init_hx": 5, "res_init": 10, "res": 10, "xupd": 1, "cg_p": 1, "cg_q": 7,
+             "cg_b": 3},
 }
 
 

@@ -100,6 +100,18 @@ __global__ void k_step_end(DevArrays A) {
   if (i < A.ninst) end_step(A.scal[i]);
 }
 
+// The reference adds TINY to every x0 when any x0 - T < TINY (mod_evolve.f90:140-141) so that its
+// BiCG never starts from a zero residual.  The TINY moves only the starting point: the system and
+// its solution are unchanged.  Under the reference's own stopping rule (HF_STOP_RECURSIVE) the
+// iterates follow linbcg's, so the TINY is applied (in the first residual as -TINY * H1, in x with
+// the first update).  Under HF_STOP_TRUE every step is accepted on the true residual of its final
+// x, whatever the start, and this CG treats a zero residual itself, so the TINY is skipped: one
+// FP64 instruction per cell less in the first residual and in the x update (GB300's FP64 pipe
+// bounds both).
+__device__ __forceinline__ bool tiny_applies(const DevArrays& A, const InstScal& s) {
+  return s.x0flag != 0 && A.opts.criterion == HF_STOP_RECURSIVE;
+}
+
 // ---- neighbour access for the columns of a task ------------------------------------------------
 // x neighbours come from the lanes of the same warp (shuffles); lanes at a task edge, periodic
 // wraps and the y neighbours are loaded; the z neighbours roll through registers as the block
@@ -208,7 +220,7 @@ __device__ __forceinline__ void res_hx_task(const DevArrays& A, double* part, in
   const bool f32 = sizeof(TR) == 4;           // FP32 g goes into the FP32 layout
   TR* R = Vec<TR>::r(A) + (f32 ? c.off4 : off);
   const float isig = (float)(1.0 / s.sigma);
-  const bool tiny = s.x0flag != 0;            // the residual of x0 + TINY: r(x0) - TINY * H1
+  const bool tiny = tiny_applies(A, s);       // the residual of x0 + TINY: r(x0) - TINY * H1
   double rr = 0.0, gg64 = 0.0;
   float gg = 0.f;
   if (c.act(0)) {
@@ -285,7 +297,7 @@ __device__ __forceinline__ void res_task(const DevArrays& A, double* part, int64
   // less per cell on this FP64-bound sweep)
   SqSum rq;
   // INIT: the residual of x0 + TINY (mod_evolve.f90:141) is r(x0) - TINY * H1
-  const bool tiny = INIT && s.x0flag;
+  const bool tiny = INIT && tiny_applies(A, s);
   const bool act = c.act(0);
   const int nz = c.nz, nxy = c.nxy, base = c.base(0);
   const XEdge xe = x_edges(c);
@@ -1011,7 +1023,7 @@ __device__ __forceinline__ void res_hx4_task(const DevArrays& A, double* part, i
   const bool f32 = sizeof(TR) == 4;
   TR* R = Vec<TR>::r(A) + (f32 ? A.inst[A.tasks[task].x].off4 : off);
   const float isig = (float)(1.0 / s.sigma);
-  const bool tiny = s.x0flag != 0;            // the residual of x0 + TINY: r(x0) - TINY * H1
+  const bool tiny = tiny_applies(A, s);       // the residual of x0 + TINY: r(x0) - TINY * H1
   double rr = 0.0, gg64 = 0.0;
   float gg = 0.f;
   if (c.act) {
@@ -1200,7 +1212,7 @@ __device__ void epi_residual_s(InstScal& s, const InstDesc& G, const DevOpts& o,
     const int t = s.role[2]; s.role[2] = s.role[3]; s.role[3] = t;
     s.tiny_pending = 0;
   } else {
-    s.tiny_pending = s.x0flag;
+    s.tiny_pending = (o.criterion == HF_STOP_RECURSIVE) ? s.x0flag : 0;   // tiny_applies
   }
   s.rr_true = tot[0];
   s.relres = s.bb > 0.0 ? sqrt(tot[0] / s.bb) : (tot[0] > 0.0 ? INFINITY : 0.0);

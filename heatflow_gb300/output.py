@@ -111,7 +111,8 @@ class SubboxLog:
             th.start()
             try:
                 k, slot = itime0, 0
-                for m in marks + [itime0 + nsteps - 1]:
+                last = itime0 + nsteps - 1          # steps after the last record run too
+                for m in marks + ([] if copies.get(last) else [last]):
                     if m >= k:
                         st = self.hf.run(k, m - k + 1)
                         stats["steps"] += st["steps"]

@@ -130,13 +130,19 @@ def test_config_layered_slab_128_vs_oracle(cuda_lib):
     from oracle.oracle import Oracle, set_threads
     import os
     prob = layered_slab(128, icattaneo=1)
+    # all host threads for this run only: with more than one, the oracle's SpMV takes the
+    # reference's OpenMP-atomic form, whose summation order varies, and later bit-exact
+    # comparisons with the oracle expect the serial order
     set_threads(os.cpu_count() or 1)
-    o = Oracle(prob)
-    o.set_state(*prob.initial_state())
-    for k in range(10):
-        rc, _, _ = o.simulate(k + 1, mode=0, tol=1e-12, itmax=50000)
-        assert rc == 0
-    Tref = o.get_state()[0]
+    try:
+        o = Oracle(prob)
+        o.set_state(*prob.initial_state())
+        for k in range(10):
+            rc, _, _ = o.simulate(k + 1, mode=0, tol=1e-12, itmax=50000)
+            assert rc == 0
+        Tref = o.get_state()[0]
+    finally:
+        set_threads(1)
     (T64,) = _gpu_run(prob, 10, "fp64")
     (T32,) = _gpu_run(prob, 10, "mixed")
     e64, e32 = _rel(T64, Tref), _rel(T32, Tref)
