@@ -42,7 +42,8 @@ UNIT = "time-steps/s"
 # Algorithmic bytes per cell of each kernel (what the kernel must read + write from HBM),
 # for the layered-slab workload (Cattaneo, per-cell heater power array present).
 BYTES_PER_CELL = {
-    # T^n, T^(n-1), rho*c, tau'*rho*c, B, heater power (8 B each) + heater case (1 B); writes S, x0
+    # T^n, T^(n-1), the T^n coefficient of S, tau'*rho*c, B, heater power (8 B each) + heater case
+    # (1 B); writes S, x0
     "rhs": 6 * 8 + 1 + 2 * 8,
     # mixed: x, diag, cx, cy, cz, S (8 B) + 1/sqrt|H_II| (4 B) read; g (4 B) + H x (8 B) written
     "residual_mixed": 6 * 8 + 4 + 4 + 8,
@@ -64,10 +65,10 @@ BYTES_PER_CELL = {
 # FP64 floating-point operations per cell (an FMA counts 2) of the FP64-pipe kernels: the
 # residual does 7 FMA for S - Hx, 1 FMA for ||r||^2 and 1 sub for H x = S - r; the step-start
 # residual from the stored products 1 FMA + 1 add (S - 2 H T^n + H T^(n-1)) and 1 FMA
-# (||r||^2); the RHS 2 mul (rho c T/dt), 1 FMA + 1 mul (S_cat), 1 add, 2 add (x0) - its x0 - T <
-# TINY test and ||S||^2 run on the integer/FP32 pipes.
+# (||r||^2); the RHS under the true-residual criterion 1 mul + 1 FMA (S = T^n c1 + ccat T^(n-1))
+# and 1 FMA (x0 = 2 T^n - T^(n-1)) per interior cell - its ||S||^2 runs on the integer/FP32 pipes.
 FP64_FLOPS_PER_CELL = {"residual_mixed": 17, "residual_fp64": 19, "residual_init_hx_mixed": 5,
-                       "rhs": 8}
+                       "rhs": 5}
 
 # Algorithmic bytes per cell of each round of the persistent solve kernel (k_solve), by phase:
 # (bytes, bytes of the first inner iteration / of an update without a correction).  Under the

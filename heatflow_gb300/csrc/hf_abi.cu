@@ -837,7 +837,7 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
   ALLOC(A.rsum, N); ALLOC(A.sinv32, N);
   ALLOC(A.a64x, N); ALLOC(A.a64y, N); ALLOC(A.a64z, N);
   ALLOC(A.a32x, N4); ALLOC(A.a32y, N4); ALLOC(A.a32z, N4);
-  ALLOC(A.rhoc, N); ALLOC(A.ccat, N); ALLOC(A.bvec, N); ALLOC(A.tau_s, N);
+  ALLOC(A.rhoc, N); ALLOC(A.ccat, N); ALLOC(A.bvec, N); ALLOC(A.tau_s, N); ALLOC(A.scoef, N);
   ALLOC(c.asm_.kappa, N);
   if (c.any_power) ALLOC(A.power, N);
   if (c.any_em) ALLOC(A.emc, N);
@@ -863,7 +863,7 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
   CK(cudaMemsetAsync(A.stamps, 0, sizeof(unsigned long long) * kStamps, c.stream));
   CK(cudaMemsetAsync(A.check, 0, sizeof(unsigned long long) * 4, c.stream));
   for (void* p : {(void*)A.diag, (void*)A.cx, (void*)A.cy, (void*)A.cz, (void*)c.asm_.kappa,
-                  (void*)d_rho, (void*)d_hc, (void*)d_tau, (void*)A.rhoc, (void*)A.ccat,
+                  (void*)d_rho, (void*)d_hc, (void*)d_tau, (void*)A.rhoc, (void*)A.ccat, (void*)A.scoef,
                   (void*)A.bvec, (void*)A.tau_s, (void*)A.a64x, (void*)A.a64y, (void*)A.a64z,
                   (void*)A.b, (void*)A.y, (void*)A.r, (void*)A.p, (void*)A.q, (void*)A.rsum,
                   (void*)A.p2, (void*)A.hx[0], (void*)A.hx[1]})

@@ -123,6 +123,13 @@ struct HM {
 };
 
 // ---- per-cell properties: set_global_variables, mod_setup.f90:53-68 ------------------------
+// The coefficient of T^n in S (mod_evolve.f90:112-116 with S_cat, mod_cattaneo.f90:35-36):
+// -rho c / dt - 2 tau' rho c, or -rho c / dt in Fourier mode.
+__device__ __forceinline__ double scoef(const InstDesc& d, double rc, double cc) {
+  const double a = -d.inv_dt * rc;
+  return d.icattaneo == 1 ? a - 2.0 * cc : a;
+}
+
 __global__ void k_props(DevArrays A, const double* rho, const double* hc, const double* tau,
                         const double* em) {
   int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -134,6 +141,7 @@ __global__ void k_props(DevArrays A, const double* rho, const double* hc, const 
   A.rhoc[g] = rc;
   A.tau_s[g] = ts;
   A.ccat[g] = ts * rc;                                   // (tau*lin_rhoc), mod_cattaneo.f90:35-36
+  A.scoef[g] = scoef(d, rc, ts * rc);
   if (A.emc) A.emc[g] = em[g] * d.len[0] * d.len[1] * kStefBoltz;   // mod_heating.f90:121-122
 }
 
@@ -482,6 +490,7 @@ __global__ void k_tempdep(DevArrays A, const int32_t* toff, const double* trows,
   const double rc = table_col(at, 2) * table_col(at, 3);
   A.rhoc[g] = rc;
   A.ccat[g] = A.tau_s[g] * rc;
+  A.scoef[g] = scoef(d, rc, A.ccat[g]);
 }
 
 cudaError_t launch_tempdep(Ctx& c) {

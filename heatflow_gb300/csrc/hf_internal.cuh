@@ -174,6 +174,9 @@ struct DevArrays {
   float* sinv32;          // FP32 copy of sinv (scaling of FP32 right-hand sides/corrections)
   float *a32x, *a32y, *a32z;
   double *rhoc, *ccat, *bvec, *power, *emc;
+  // -rho c / dt - 2 tau' rho c per cell (-rho c / dt in Fourier mode): S = T^n scoef + ccat T^(n-1)
+  // - Qdens - B, the RHS's form under the true-residual criterion (fewer FP64 roundings)
+  double* scoef;
   int8_t* icase;
   double* tau_s;          // tau/dt^2 (heater case 5)
   // state: four temperature-sized buffers, roles per instance in InstScal::role
