@@ -3,6 +3,7 @@
 // (cell lengths, volumes, heated volume, Neumann power densities) and is compiled without FMA
 // contraction so it rounds as the reference does.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -120,10 +121,8 @@ void free_all(Ctx& c) {
   if (c.stream) cudaStreamSynchronize(c.stream);   // queued host-buffer steps may still run
   drop_graph(c);
   if (c.out_stream) cudaStreamSynchronize(c.out_stream);
-  for (cudaEvent_t* e : {&c.ev_placed, &c.ev_in_pp, &c.ev_gathered}) {
-    if (*e) cudaEventDestroy(*e);
-    *e = nullptr;
-  }
+  if (c.ev_gathered) cudaEventDestroy(c.ev_gathered);
+  c.ev_gathered = nullptr;
   for (auto& o : c.outs) {
     if (o.done) cudaEventDestroy(o.done);
     o.done = nullptr;
@@ -133,9 +132,15 @@ void free_all(Ctx& c) {
     }
     o.ptr = nullptr;
   }
-  for (auto& e : c.ev_in_chunk) {
-    if (e) cudaEventDestroy(e);
-    e = nullptr;
+  for (auto& st : c.stage) {
+    for (cudaEvent_t* e : {&st.in_pp, &st.free}) {
+      if (*e) cudaEventDestroy(*e);
+      *e = nullptr;
+    }
+    for (auto& e : st.in_chunk) {
+      if (e) cudaEventDestroy(e);
+      e = nullptr;
+    }
   }
   if (c.copy_stream) cudaStreamSynchronize(c.copy_stream);
   for (auto& sl : c.sub) {
@@ -1125,22 +1130,31 @@ int hf_step_host_async(hf_ctx* h, int64_t itime, const double* tp, const double*
     if ((rc = sync_scal(c))) return rc;
     c.async_before.assign(c.h_scal, c.h_scal + c.ninst);
     c.async_steps = 0;
+    c.async_calls.clear();
+    c.async_host_kernels = 0;
     if ((rc = build_post_graph(c))) return rc;
     build_host_chunks(c);
     if (!c.copy_stream) CU(cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking));
     if (!c.out_stream) CU(cudaStreamCreateWithFlags(&c.out_stream, cudaStreamNonBlocking));
-    for (cudaEvent_t* e : {&c.ev_placed, &c.ev_in_pp, &c.ev_gathered})
-      if (!*e) CU(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+    if (!c.ev_gathered) CU(cudaEventCreateWithFlags(&c.ev_gathered, cudaEventDisableTiming));
     for (auto& o : c.outs) {
       if (!o.done) CU(cudaEventCreateWithFlags(&o.done, cudaEventDisableTiming));
       for (auto& e : o.chunk)
         if (!e) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     }
-    for (auto& e : c.ev_in_chunk)
-      if (!e) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-    for (double** b : {&c.d_stage_p, &c.d_stage_pp, &c.d_stage_out})
-      if (!*b && (rc = dalloc(c, b, (size_t)total))) return rc;
-    CU(cudaEventRecord(c.ev_placed, c.stream));
+    for (auto& st : c.stage) {
+      for (cudaEvent_t* e : {&st.in_pp, &st.free})
+        if (!*e) CU(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+      for (auto& e : st.in_chunk)
+        if (!e) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      for (double** b : {&st.p, &st.pp})
+        if (!*b && (rc = dalloc(c, b, (size_t)total))) return rc;
+      CU(cudaEventRecord(st.free, c.stream));
+    }
+    if (!c.d_stage_out && (rc = dalloc(c, &c.d_stage_out, (size_t)total))) return rc;
+    if (!c.d_check_call && (rc = dalloc(c, &c.d_check_call, (size_t)1))) return rc;
+    const int64_t none = INT64_MAX;
+    CU(cudaMemcpyAsync(c.d_check_call, &none, sizeof(none), cudaMemcpyHostToDevice, c.stream));
     for (auto& o : c.outs) {
       CU(cudaEventRecord(o.done, c.stream));
       o.ptr = nullptr;
@@ -1148,50 +1162,78 @@ int hf_step_host_async(hf_ctx* h, int64_t itime, const double* tp, const double*
   }
   const std::vector<Ctx::HostChunk>& ch = c.host_chunks;
   const int nch = (int)ch.size();
-  // Copy stream.  The staging buffers are free once the previous step placed its inputs; by then
-  // every download older than the last two queued ones is done too (the previous step's main
-  // stream waited for the download before it).  An input that is the destination of one of the
-  // last two downloads waits for it: T^(n-1), normally the result of two steps back, as a whole
-  // (its upload then overlaps the previous step's solve); T^n, normally the previous step's
-  // result, chunk by chunk behind that chunk's download, so both directions of the link run at
-  // once.
-  CU(cudaStreamWaitEvent(c.copy_stream, c.ev_placed, 0));
+  const int64_t call = c.async_steps;
+  Ctx::Stage& st = c.stage[call & 1];
+  // Early start: the inputs are the previous call's result and the previous call's T^n -- the
+  // rotation simulate() performs -- so, unless the caller broke the rule that queued arrays stay
+  // untouched, their bits are those the device holds as T^n and T^(n-1) now.  The step then starts
+  // from the device's copy while the uploads travel, and the next call (or hf_host_sync) compares
+  // the uploaded bits with that copy before the copy can be overwritten; a difference makes
+  // hf_host_sync run the queue again from that call's uploaded inputs.
+  const bool early = call >= 1 && tp == c.outs[c.out_last].ptr && tpp == c.async_calls.back().tp;
+  // Copy stream.  A staging set is free once the consumer of its previous inputs (two calls back)
+  // has run; by then every download older than the last kHostOuts queued ones is done (the main
+  // stream had passed a gather that waited for it).  An input that is the destination of one of
+  // those downloads waits for it: T^(n-1), normally the result of two steps back, as a whole (its
+  // upload then overlaps the previous step's solve); T^n, normally the previous step's result,
+  // chunk by chunk behind that chunk's download, so both directions of the link run at once.
+  CU(cudaStreamWaitEvent(c.copy_stream, st.free, 0));
   for (const auto& o : c.outs)
     if (o.ptr && tpp == o.ptr) CU(cudaStreamWaitEvent(c.copy_stream, o.done, 0));
-  CU(cudaMemcpyAsync(c.d_stage_pp, tpp, sizeof(double) * (size_t)total, cudaMemcpyHostToDevice,
+  CU(cudaMemcpyAsync(st.pp, tpp, sizeof(double) * (size_t)total, cudaMemcpyHostToDevice,
                      c.copy_stream));
-  CU(cudaEventRecord(c.ev_in_pp, c.copy_stream));
+  CU(cudaEventRecord(st.in_pp, c.copy_stream));
   for (int k = 0; k < nch; ++k) {
     for (const auto& o : c.outs)
       if (o.ptr && tp == o.ptr) CU(cudaStreamWaitEvent(c.copy_stream, o.chunk[k], 0));
-    CU(cudaMemcpyAsync(c.d_stage_p + ch[k].clo, tp + ch[k].clo,
+    CU(cudaMemcpyAsync(st.p + ch[k].clo, tp + ch[k].clo,
                        sizeof(double) * (size_t)(ch[k].chi - ch[k].clo), cudaMemcpyHostToDevice,
                        c.copy_stream));
-    CU(cudaEventRecord(c.ev_in_chunk[k], c.copy_stream));
+    CU(cudaEventRecord(st.in_chunk[k], c.copy_stream));
   }
-  // Main stream: place T^(n-1), begin the step, then place each chunk of T^n as it lands and run
-  // the RHS of its tasks (the later chunks are still on the link); then the rest of the step as
-  // one graph and the gather of its result.  The download runs on a stream of its own, chunk by
-  // chunk, so the next step's placements and RHS chunks do not queue behind it.
-  CU(cudaStreamWaitEvent(c.stream, c.ev_in_pp, 0));
-  CU(launch_host_in(c, c.d_stage_pp, 1, c.stream));
+  // Main stream.  First the check of the previous call's inputs if it started early: its step
+  // has ended, so its T^n and T^(n-1) are roles 1 and 2 now, and this step's RHS is about to
+  // overwrite role 2.
+  if (call >= 1 && c.async_calls.back().early) {
+    Ctx::Stage& ps = c.stage[(call - 1) & 1];
+    CU(cudaStreamWaitEvent(c.stream, ps.in_pp, 0));
+    for (int k = 0; k < nch; ++k) CU(cudaStreamWaitEvent(c.stream, ps.in_chunk[k], 0));
+    CU(launch_host_check(c, ps.p, ps.pp, call - 1, c.d_check_call, c.stream));
+    CU(cudaEventRecord(ps.free, c.stream));
+    c.async_host_kernels += 1;
+  }
   const int64_t per = c.opts.precision == HF_PREC_MIXED ? c.opts.inner_itmax : c.opts.itmax;
-  CU(launch_ctrl_init(c, itime, 2 * (int64_t)(c.opts.max_refine + 3) * (per + 3)));
-  // kernels of the step outside the host copies: begin, RHS per chunk, finalize, solve, end
-  CU(launch_graph_step_begin(c, c.d_ctrl, nch + 4 + (c.tempdep ? 4 : 0)));
-  for (int k = 0; k < nch; ++k) {
-    CU(cudaStreamWaitEvent(c.stream, c.ev_in_chunk[k], 0));
-    CU(launch_host_in_range(c, c.d_stage_p, 0, ch[k].glo, ch[k].ghi, c.stream));
-    CU(launch_rhs_range(c, ch[k].tlo, ch[k].thi));
+  if (early) {
+    // begin the step from the device's copy of the inputs; the whole RHS as one launch
+    CU(launch_ctrl_init(c, itime, 2 * (int64_t)(c.opts.max_refine + 3) * (per + 3)));
+    CU(launch_graph_step_begin(c, c.d_ctrl, 1 + 4 + (c.tempdep ? 4 : 0)));
+    CU(launch_rhs(c));
+    c.async_host_kernels += 2;                    // control reset, gather
+  } else {
+    // place T^(n-1), begin the step, then place each chunk of T^n as it lands and run the RHS of
+    // its tasks (the later chunks are still on the link)
+    CU(cudaStreamWaitEvent(c.stream, st.in_pp, 0));
+    CU(launch_host_in(c, st.pp, 1, c.stream));
+    CU(launch_ctrl_init(c, itime, 2 * (int64_t)(c.opts.max_refine + 3) * (per + 3)));
+    // kernels of the step outside the host copies: begin, RHS per chunk, finalize, solve, end
+    CU(launch_graph_step_begin(c, c.d_ctrl, nch + 4 + (c.tempdep ? 4 : 0)));
+    for (int k = 0; k < nch; ++k) {
+      CU(cudaStreamWaitEvent(c.stream, st.in_chunk[k], 0));
+      CU(launch_host_in_range(c, st.p, 0, ch[k].glo, ch[k].ghi, c.stream));
+      CU(launch_rhs_range(c, ch[k].tlo, ch[k].thi));
+    }
+    CU(cudaEventRecord(st.free, c.stream));
+    c.async_host_kernels += 3 + nch;              // placements, control reset, gather
   }
-  CU(cudaEventRecord(c.ev_placed, c.stream));
+  // the rest of the step as one graph and the gather of its result; the download runs on a
+  // stream of its own, chunk by chunk, so the next step's work does not queue behind it
   CU(cudaGraphLaunch(c.post_exec, c.stream));
-  // the previous download has left d_stage_out
-  CU(cudaStreamWaitEvent(c.stream, c.outs[c.out_last].done, 0));
+  CU(cudaStreamWaitEvent(c.stream, c.outs[c.out_last].done, 0));   // d_stage_out is free
   CU(launch_host_out(c, c.d_stage_out, c.stream));
   CU(cudaEventRecord(c.ev_gathered, c.stream));
   CU(cudaStreamWaitEvent(c.out_stream, c.ev_gathered, 0));
-  Ctx::HostOut& o = c.outs[c.out_last ^ 1];   // replaces the download of two steps back
+  const int next = (c.out_last + 1) % Ctx::kHostOuts;   // replaces the oldest tracked download
+  Ctx::HostOut& o = c.outs[next];
   for (int k = 0; k < nch; ++k) {
     CU(cudaMemcpyAsync(out + ch[k].clo, c.d_stage_out + ch[k].clo,
                        sizeof(double) * (size_t)(ch[k].chi - ch[k].clo), cudaMemcpyDeviceToHost,
@@ -1200,7 +1242,8 @@ int hf_step_host_async(hf_ctx* h, int64_t itime, const double* tp, const double*
   }
   CU(cudaEventRecord(o.done, c.out_stream));
   o.ptr = out;
-  c.out_last ^= 1;
+  c.out_last = next;
+  c.async_calls.push_back(Ctx::HostCall{itime, tp, tpp, out, early});
   c.async_pending = true;
   c.async_steps += 1;
   c.state_set = true;
@@ -1214,25 +1257,49 @@ int hf_host_sync(hf_ctx* h, hf_stats* stats) {
     if (stats) std::memset(stats, 0, sizeof(*stats));
     return HF_OK;
   }
+  const int nch = (int)c.host_chunks.size();
+  if (c.async_calls.back().early) {          // the check of the last call's inputs
+    Ctx::Stage& ps = c.stage[(c.async_steps - 1) & 1];
+    CU(cudaStreamWaitEvent(c.stream, ps.in_pp, 0));
+    for (int k = 0; k < nch; ++k) CU(cudaStreamWaitEvent(c.stream, ps.in_chunk[k], 0));
+    CU(launch_host_check(c, ps.p, ps.pp, c.async_steps - 1, c.d_check_call, c.stream));
+    CU(cudaEventRecord(ps.free, c.stream));
+    c.async_host_kernels += 1;
+  }
   c.async_pending = false;
   CtrlState cs{};
+  int64_t first_bad = INT64_MAX;
   CU(cudaMemcpyAsync(&cs, c.d_ctrl, sizeof(cs), cudaMemcpyDeviceToHost, c.stream));
+  CU(cudaMemcpyAsync(&first_bad, c.d_check_call, sizeof(first_bad), cudaMemcpyDeviceToHost, c.stream));
   CU(cudaStreamSynchronize(c.stream));
   CU(cudaStreamSynchronize(c.copy_stream));
   CU(cudaStreamSynchronize(c.out_stream));
   const int64_t steps = c.async_steps;
   c.async_steps = 0;
-  // host copies per step: T^(n-1) placed, T^n placed per chunk, the control reset, the gather
-  const int64_t host_kernels = 3 + (int64_t)c.host_chunks.size();
-  c.launches += cs.launches + host_kernels * steps;
+  c.launches += cs.launches + c.async_host_kernels;
   if (cs.guard_hit & 2)
     return set_err(HF_EDEVICE, "persistent solve: a grid barrier wait reached its time limit");
   if (cs.guard_hit) return set_err(HF_EDEVICE, "captured solve loop reached its iteration bound");
-  int rc = sync_scal(c);
-  if (rc) return rc;
+  int rc;
+  if (first_bad != INT64_MAX) {
+    // An early-started call's uploaded inputs differed from the device copy it started from (a
+    // queued array was changed): from that call on, every step runs again from its own uploaded
+    // inputs (hf_set_state, one step, the result into its array), as a call without an early
+    // start would have.  The queued arrays are still valid: they stay untouched until now.
+    for (size_t j = (size_t)first_bad; j < c.async_calls.size(); ++j) {
+      const Ctx::HostCall& hc = c.async_calls[j];
+      if ((rc = hf_set_state(h, hc.tp, hc.tpp))) return rc;
+      hf_stats one;
+      if ((rc = run_steps(c, hc.itime, 1, &one))) return rc;
+      if ((rc = hf_get_state(h, hc.out, nullptr))) return rc;
+    }
+    const int64_t none = INT64_MAX;
+    CU(cudaMemcpy(c.d_check_call, &none, sizeof(none), cudaMemcpyHostToDevice));
+  }
+  if ((rc = sync_scal(c))) return rc;
   if ((rc = diagnose(c))) return rc;
   fill_stats(c, stats, steps, c.async_before);
-  if (stats) stats->kernel_launches = cs.launches + host_kernels * steps;
+  if (stats) stats->kernel_launches = cs.launches + c.async_host_kernels;
   return first_error(c);
 }
 

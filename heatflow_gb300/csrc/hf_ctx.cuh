@@ -66,20 +66,42 @@ struct Ctx {
   // host-buffer steps queued without host round trips (hf_step_host_async): copy engines move
   // compact staging buffers; kernels place them into (and gather from) the role buffers
   static constexpr int kHostChunks = 8;
-  cudaEvent_t ev_placed = nullptr;     // the last queued step's inputs are in their role buffers
-  // Downloads of the last two queued steps (older ones are covered by ev_placed): the host array
-  // each writes, with events for the whole download and chunk by chunk.  An upload from one of
-  // these arrays waits for its download, whatever order the caller passes the arrays in.
+  static constexpr int kHostOuts = 4;
+  // Downloads of the last kHostOuts queued steps (older ones are complete once a staging set's
+  // free event has passed): the host array each writes, with events for the whole download and
+  // chunk by chunk.  An upload from one of these arrays waits for its download, whatever order
+  // the caller passes the arrays in.
   struct HostOut {
     const double* ptr = nullptr;
     cudaEvent_t done = nullptr;
     cudaEvent_t chunk[kHostChunks] = {};
   };
-  HostOut outs[2];
+  HostOut outs[kHostOuts];
   int out_last = 0;                    // outs[out_last]: the last queued download
-  double* d_stage_p = nullptr;         // T^n of the next step (compact layout)
-  double* d_stage_pp = nullptr;        // T^(n-1) of the next step
+  // Two staging sets for the uploaded inputs, used by alternate calls, so a call's uploads need
+  // not wait for the previous call's inputs to be consumed.
+  struct Stage {
+    double* p = nullptr;               // T^n of the call (compact layout)
+    double* pp = nullptr;              // T^(n-1)
+    cudaEvent_t in_pp = nullptr;       // T^(n-1) has landed
+    cudaEvent_t in_chunk[kHostChunks] = {};   // ... T^n, chunk by chunk
+    cudaEvent_t free = nullptr;        // the set's consumer (placement or check) has run
+  };
+  Stage stage[2];
   double* d_stage_out = nullptr;       // the last step's result
+  // The queued calls.  A call whose inputs are the previous call's result and inputs (the
+  // rotation simulate() performs) starts from the device's own copy of them ("early"), while its
+  // uploads travel; the next call (or hf_host_sync) checks the uploaded bits against that copy.
+  struct HostCall {
+    int64_t itime;
+    const double* tp;
+    const double* tpp;
+    double* out;
+    bool early;
+  };
+  std::vector<HostCall> async_calls;
+  int64_t* d_check_call = nullptr;     // first call whose uploads differed from the device copy
+  int64_t async_host_kernels = 0;      // host-copy kernels of the queued calls
   // T^n moves in chunks of whole task z-slabs: each chunk's RHS tasks run as soon as its cells
   // are placed, while later chunks are still on the link.  Cells [clo, chi) of the compact host
   // layout, [glo, ghi) of the device layout, tasks [tlo, thi).
@@ -88,14 +110,12 @@ struct Ctx {
   int host_chunks_depth = -1;           // task depth the chunks were cut for
   cudaStream_t out_stream = nullptr;    // downloads, so the next step's work need not queue behind them
   cudaEvent_t ev_gathered = nullptr;    // the last queued step's result is in d_stage_out
-  cudaEvent_t ev_in_pp = nullptr;       // T^(n-1) of the next step is in its staging buffer
-  cudaEvent_t ev_in_chunk[kHostChunks] = {};   // ... T^n, chunk by chunk
   // the step after its RHS (finalize, persistent solve, step end, property rebuild) as one graph
   cudaGraphExec_t post_exec = nullptr;
   cudaGraph_t post_graph = nullptr;
   int post_precision = -1, post_criterion = -1;
   bool async_pending = false;          // steps queued since the last hf_host_sync
-  int64_t async_steps = 0;
+  int64_t async_steps = 0;             // = async_calls.size()
   std::vector<InstScal> async_before;  // scalars before the first queued step
   // tabulated properties re-evaluated after every step (hf_set_property_tables)
   bool tempdep = false;

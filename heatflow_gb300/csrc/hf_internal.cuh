@@ -467,6 +467,11 @@ cudaError_t launch_host_in(Ctx& c, const double* src, int which, cudaStream_t st
 cudaError_t launch_host_in_range(Ctx& c, const double* src, int which, int64_t glo, int64_t ghi,
                                  cudaStream_t stream);
 cudaError_t launch_host_out(Ctx& c, double* dst, cudaStream_t stream);
+// Bit-for-bit check of uploaded inputs (compact layout) against the device's T^n and T^(n-1) of
+// the step that just ended (roles 1 and 2 after its rotation): a difference sets *first to
+// min(*first, call).  Instances whose step failed are skipped.
+cudaError_t launch_host_check(Ctx& c, const double* sp, const double* spp, int64_t call,
+                              int64_t* first, cudaStream_t stream);
 // Control block of a one-step graph launch queued without the host (async host-buffer steps).
 cudaError_t launch_ctrl_init(Ctx& c, int64_t itime, int64_t limit);
 cudaError_t launch_rhs_parts(Ctx& c, double* B, double* Q, double* Qd, double* Sc);

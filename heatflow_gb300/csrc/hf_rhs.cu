@@ -504,6 +504,23 @@ __global__ void k_host_in(DevArrays A, const double* __restrict__ src, int which
   }
 }
 
+__global__ void k_host_check(DevArrays A, const double* __restrict__ sp,
+                             const double* __restrict__ spp, int64_t call, int64_t* first) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  bool diff = false;
+  for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < A.ncells; g += stride) {
+    const int inst = A.tile_inst[g / kTile];
+    const InstDesc& d = A.inst[inst];
+    const int64_t l = g - d.off;
+    if (l >= d.n) continue;
+    const InstScal& s = A.scal[inst];
+    if (s.status != 0) continue;                 // the step failed: its error is reported instead
+    diff |= dbits(sp[d.hoff + l]) != dbits(A.tbuf[s.role[1]][g]);
+    diff |= dbits(spp[d.hoff + l]) != dbits(A.tbuf[s.role[2]][g]);
+  }
+  if (diff) atomicMin(reinterpret_cast<long long*>(first), (long long)call);
+}
+
 __global__ void k_host_out(DevArrays A, double* __restrict__ dst) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < A.ncells; g += stride) {
@@ -542,6 +559,12 @@ cudaError_t launch_host_in_range(Ctx& c, const double* src, int which, int64_t g
   if (ghi <= glo) return cudaSuccess;
   const unsigned nb = (unsigned)std::max<int64_t>(1, std::min<int64_t>((ghi - glo + 255) / 256, 152 * 8));
   k_host_in<<<nb, 256, 0, stream>>>(c.A, src, which, glo, ghi);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_host_check(Ctx& c, const double* sp, const double* spp, int64_t call,
+                              int64_t* first, cudaStream_t stream) {
+  k_host_check<<<host_copy_blocks(c), 256, 0, stream>>>(c.A, sp, spp, call, first);
   return cudaGetLastError();
 }
 

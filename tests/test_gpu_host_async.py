@@ -1,8 +1,10 @@
 """Host-buffer steps queued without host round trips (hf_step_host_async / hf_host_sync): a caller
 that feeds back the results it downloads gets the bits of an uninterrupted hf_run (the stored
-products H T^n, H T^(n-1) survive an input equal to the device's state), on one grid and on a
-batch, with torch-pinned and with registered host arrays; a changed input drops the products as
-hf_set_state does; pageable arrays and calls while steps are queued are refused."""
+products H T^n, H T^(n-1) survive an input equal to the device's state; such calls start early,
+from the device's copy, while their uploads travel), on one grid and on a batch, with torch-pinned
+and with registered host arrays; a changed input drops the products as hf_set_state does; an
+input changed while queued under an early start is caught by the check of the uploaded bits and
+the queue runs again from there; pageable arrays and calls while steps are queued are refused."""
 import ctypes as C
 
 import numpy as np
@@ -214,3 +216,33 @@ def test_async_inputs_in_any_order(cuda_lib):
     assert st["steps"] == K and st["unconverged"] == 0
     for k in range(K):
         assert np.array_equal(outs[k], ref[k]), k
+
+
+def test_early_start_checked_against_uploads(cuda_lib):
+    """The second call's T^(n-1) is the first call's T^n array, which the caller changes after the
+    first call (breaking the rule that queued arrays stay untouched): the second and third calls
+    start early from the device's copy, the check of the uploaded bits finds the difference, and
+    hf_host_sync runs both again from their uploaded inputs.  The results equal steps run from
+    those inputs with hf_set_state."""
+    torch = pytest.importorskip("torch")
+    prob = layered_slab(16, nz=20, layer=5)
+    tp, tpp = _initial(prob)
+    a, b, c, d, e = (_pinned(prob.ncells, 0.0) for _ in range(5))
+    a[:] = tp
+    b[:] = tpp
+    with HeatFlow(prob, **KW) as hf:
+        hf.step_host_async(3, a, b, c)          # T^n = a, T^(n-1) = b -> c
+        torch.cuda.synchronize()                # every copy of the first call has landed
+        a[5] += 0.25                            # the caller changes a queued array
+        hf.step_host_async(4, c, a, d)          # the rotation: starts early from the device copy
+        hf.step_host_async(5, d, c, e)
+        st = hf.host_sync()
+    assert st["steps"] == 3
+    with HeatFlow(prob, **KW) as ref:
+        ref.set_state(c, a)                     # the second call's uploaded inputs
+        ref.run(4, 1)
+        d_ref, _ = ref.get_state()
+        ref.set_state(d_ref, c)
+        ref.run(5, 1)
+        e_ref, _ = ref.get_state()
+    assert np.array_equal(d, d_ref) and np.array_equal(e, e_ref)
