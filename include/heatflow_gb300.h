@@ -211,7 +211,12 @@ int hf_adjoint_accumulate(hf_ctx* ctx, const double* lam, const double* x, int64
  * result of two calls back - is uploaded on a second stream while the previous step is still
  * solving; T^n - normally the previous call's temp_out - is uploaded chunk by chunk right behind
  * that download, so both directions of the host link run at once, and the right-hand side of
- * each chunk's cells is computed as soon as the chunk is placed.  Any arrays may be passed:
+ * each chunk's cells is computed as soon as the chunk is placed.  A call whose temp_p is the
+ * previous call's temp_out and whose temp_pp is the previous call's temp_p (the rotation simulate
+ * performs) starts at once from the device's copy of those fields while its uploads travel; the
+ * uploaded bits are compared with that copy before it can be overwritten, and if they differ
+ * (an array was changed while queued) hf_host_sync runs the queue again from that call, each
+ * step from its uploaded inputs as hf_set_state would place them.  Any arrays may be passed:
  * an input that is the temp_out of one of the queued calls waits for that download, in
  * whatever order the arrays rotate.  Every array
  * holds total_cells doubles (instances back to back) and must stay valid and untouched until
