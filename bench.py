@@ -42,9 +42,9 @@ UNIT = "time-steps/s"
 # Algorithmic bytes per cell of each kernel (what the kernel must read + write from HBM),
 # for the layered-slab workload (Cattaneo, per-cell heater power array present).
 BYTES_PER_CELL = {
-    # T^n, T^(n-1), the T^n coefficient of S, tau'*rho*c, B, heater power (8 B each) + heater case
-    # (1 B); writes S, x0
-    "rhs": 6 * 8 + 1 + 2 * 8,
+    # every cell: T^n, T^(n-1), the T^n coefficient of S, tau'*rho*c read, S and x0 written (8 B
+    # each); B, heater case and power only where they exist (rhs_bytes)
+    "rhs": 6 * 8,
     # mixed: x, diag, cx, cy, cz, S (8 B) + 1/sqrt|H_II| (4 B) read; g (4 B) + H x (8 B) written
     "residual_mixed": 6 * 8 + 4 + 4 + 8,
     # mixed step start from the stored products: S, H T^n, H T^(n-1) (8 B) + 1/sqrt|H_II| (4 B)
@@ -73,37 +73,62 @@ FP64_FLOPS_PER_CELL = {"residual_mixed": 17, "residual_fp64": 19, "residual_init
 # Algorithmic bytes per cell of each round of the persistent solve kernel (k_solve), by phase:
 # (bytes, bytes of the first inner iteration / of an update without a correction).  Under the
 # true-residual criterion the reference's +TINY on x0 is not applied (it moves only the starting
-# point), so the first residual does not read H*1.
+# point), so the first residual does not read H*1.  A CG update that also forms x ("cg_bx", the
+# iteration predicted to end the inner solve) counts the CG update's bytes plus, if its x is the
+# one the next residual sweep reads, the x update's (x, S^-1 in, x out: XB); when the solve went
+# on after it, the x it formed was not used and is not counted.
 PHASE_BYTES = {
     "mixed": {"res_init": (56, 56), "res_init_hx": (32, 32), "res": (64, 64), "cg_p": (12, 8),
-              "cg_q": (20, 20), "cg_pq": (28, 24), "cg_b": (24, 20), "xupd": (24, 16)},
+              "cg_q": (20, 20), "cg_pq": (28, 24), "cg_b": (24, 20), "cg_bx": (24, 20),
+              "xupd": (24, 16)},
     "fp64": {"res_init": (64, 64), "res_init_hx": (40, 40), "res": (72, 72), "cg_p": (24, 16),
-             "cg_q": (40, 40), "cg_b": (48, 40), "xupd": (32, 16)},
+             "cg_q": (40, 40), "cg_b": (48, 40), "cg_bx": (48, 40), "xupd": (32, 16)},
 }
+XB = {"mixed": 8 + 4 + 8, "fp64": 3 * 8}
+
+
+def rhs_bytes(prob):
+    """Algorithmic bytes of one RHS launch: 48 B per cell (BYTES_PER_CELL["rhs"]), the boundary
+    vector B at the cells on non-periodic outer faces (boundary() leaves every other cell at 0),
+    and the heater case (1 B) and power (8 B) of the heated cells."""
+    import numpy as np
+    dims = (prob.nx, prob.ny, prob.nz)
+    per = tuple(getattr(prob, "periodic", (0, 0, 0)) or (0, 0, 0))
+    inner = 1
+    for n, p in zip(dims, per):
+        inner *= n if p else max(n - 2, 0)
+    N = prob.nx * prob.ny * prob.nz
+    heated = int(np.count_nonzero(np.asarray(prob.iheater) > 0)) if prob.iheater is not None else 0
+    return BYTES_PER_CELL["rhs"] * N + 8 * (N - inner) + 9 * heated
 
 
 def round_bytes_per_cell(rounds, precision):
     """Algorithmic bytes per cell of each round of one persistent-solve launch (its round log)."""
     table = PHASE_BYTES[precision]
-    out, first_cg, first_b, have_y = [], True, True, False
+    out, first_cg, first_b, have_y, bx = [], True, True, False, None
     for ph, _ in rounds:
         full, alt = table.get(ph, (0, 0))
         b = 0
         if ph in ("res_init", "res_init_hx", "res"):
+            if ph == "res" and bx is not None:      # this sweep reads the x that update formed
+                out[bx] += XB[precision]
             b = full
             first_cg = first_b = True
             have_y = False
+            bx = None
         elif ph in ("cg_pq", "cg_p"):
             b = alt if first_cg else full
             first_cg = False
         elif ph == "cg_q":
             b = full
-        elif ph == "cg_b":
+        elif ph in ("cg_b", "cg_bx"):
             b = alt if first_b else full
             first_b = False
             have_y = True
+            bx = len(out) if ph == "cg_bx" else None
         elif ph == "xupd":
             b = full if have_y else alt
+            bx = None
         out.append(b)
     return out
 
@@ -115,11 +140,12 @@ def solve_bytes_per_cell(rounds, precision):
 
 # FP64 instructions per cell of each round (the rest of the work is FP32/integer): the mixed
 # path's residual sweep 7 FMA + 1 sub (||r||^2 in FP32), its pointwise first residual 1 FMA + 1 add
-# + 1 FMA (||r||^2), the stencil first residual 7 + 1 FMA, the x update 1 add.
+# + 1 FMA (||r||^2), the stencil first residual 7 + 1 FMA, the x update 1 add (also when a CG
+# update forms x).
 PHASE_FP64_INSTR = {
-    "mixed": {"res_init_hx": 3, "res_init": 8, "res": 8, "xupd": 1},
+    "mixed": {"res_init_hx": 3, "res_init": 8, "res": 8, "xupd": 1, "cg_bx": 1},
     "fp64": {"res_init_hx": 5, "res_init": 10, "res": 10, "xupd": 1, "cg_p": 1, "cg_q": 7,
-             "cg_b": 3},
+             "cg_b": 3, "cg_bx": 4},
 }
 
 
@@ -157,16 +183,20 @@ def phase_table(rounds, precision, N):
         e["us"] += us
     for ph, e in out.items():
         full, _ = PHASE_BYTES[precision].get(ph, (0, 0))
+        if ph == "cg_bx":
+            full += XB[precision]
         e["us_per_round"] = e["us"] / e["rounds"]
         e["GB/s_upper"] = full * N / (e["us_per_round"] * 1e-6) / 1e9 if full else None
     return out
 
 
-def kernel_table(kms, N, peak, fp_rates):
-    """Standalone kernel times -> GB/s, fraction of HBM and, for the FP64-pipe kernels, TFLOP/s."""
+def kernel_table(kms, N, peak, fp_rates, total_bytes=None):
+    """Standalone kernel times -> GB/s, fraction of HBM and, for the FP64-pipe kernels, TFLOP/s.
+    total_bytes: {kernel: algorithmic bytes per launch} where it is not BYTES_PER_CELL x N."""
     out = {}
     for k, v in kms.items():
-        gbs = BYTES_PER_CELL[k] * N / (v / 1000.0) / 1e9
+        b = (total_bytes or {}).get(k, BYTES_PER_CELL[k] * N)
+        gbs = b / (v / 1000.0) / 1e9
         e = {"ms": v, "GB/s": gbs, "frac": gbs / peak}
         if fp_rates and k in FP64_FLOPS_PER_CELL:
             tf = FP64_FLOPS_PER_CELL[k] * N / (v / 1000.0) / 1e12
@@ -549,7 +579,8 @@ def main():
                 "algorithmic_bytes_per_launch": solve_bpc * N, "ms_per_launch": solve_ms,
                 "rounds_per_launch": nrounds, "share_of_step": solve_ms / (ms / K)}
     rhs_ms = hf.time_kernel(abi.HF_KERNEL_RHS, reps=10)
-    roofline["k_rhs"] = {"ms": rhs_ms, "GB/s": BYTES_PER_CELL["rhs"] * N / (rhs_ms / 1000.0) / 1e9,
+    rhs_gbs = rhs_bytes(prob) / (rhs_ms / 1000.0) / 1e9
+    roofline["k_rhs"] = {"ms": rhs_ms, "GB/s": rhs_gbs, "frac": rhs_gbs / peak,
                          "share_of_step": rhs_ms / (ms / K)}
     detail = {"phases": phase_table(rounds, prec, N)}
     if fp_rates:
@@ -568,7 +599,7 @@ def main():
                    "residual_mixed": abi.HF_KERNEL_RESIDUAL}                # that rewrites H x
         kms = {name: hf.time_kernel(k, reps=10) for name, k in kernels.items()}
         kms["rhs"] = rhs_ms
-        detail["kernels"] = kernel_table(kms, N, peak, fp_rates)
+        detail["kernels"] = kernel_table(kms, N, peak, fp_rates, {"rhs": rhs_bytes(prob)})
     hf.close()
 
     # ---- plain FP64 GPU path at the same residual

@@ -144,11 +144,11 @@ _SIGNATURES = {
 HF_KERNEL_RHS, HF_KERNEL_RESIDUAL, HF_KERNEL_CG_P, HF_KERNEL_CG_SPMV, HF_KERNEL_CG_UPDATE = 0, 1, 2, 3, 4
 HF_KERNEL_XUPDATE, HF_KERNEL_SOLVE, HF_KERNEL_CG_PQ, HF_KERNEL_RESIDUAL_INIT = 5, 6, 7, 8
 (HF_PHASE_IDLE, HF_PHASE_START, HF_PHASE_RES_INIT, HF_PHASE_CG_P, HF_PHASE_CG_Q, HF_PHASE_CG_PQ,
- HF_PHASE_CG_B, HF_PHASE_XUPD, HF_PHASE_RES, HF_PHASE_RES_INIT_HX) = range(10)
+ HF_PHASE_CG_B, HF_PHASE_XUPD, HF_PHASE_RES, HF_PHASE_RES_INIT_HX, HF_PHASE_CG_BX) = range(11)
 PHASE_NAMES = {HF_PHASE_IDLE: "idle", HF_PHASE_START: "start", HF_PHASE_RES_INIT: "res_init",
                HF_PHASE_CG_P: "cg_p", HF_PHASE_CG_Q: "cg_q", HF_PHASE_CG_PQ: "cg_pq",
                HF_PHASE_CG_B: "cg_b", HF_PHASE_XUPD: "xupd", HF_PHASE_RES: "res",
-               HF_PHASE_RES_INIT_HX: "res_init_hx"}
+               HF_PHASE_RES_INIT_HX: "res_init_hx", HF_PHASE_CG_BX: "cg_bx"}
 
 # the index-checked build of the same library (tests only; built by build_library(checked=True))
 CHECKED_LIB_PATH = os.path.join(HERE, "_build", "checked", "libheatflow_gb300_checked.so")

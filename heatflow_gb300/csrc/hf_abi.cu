@@ -1760,6 +1760,7 @@ int hf_time_kernel(hf_ctx* h, int which, int reps, double* ms) {
     s.status = 0;
     s.rho = 1.0; s.gg0 = 1.0; s.beta = 0.5; s.alpha = 0.5; s.eta = 0.0;
     s.sigma = 1.0; s.sigma_prev = 1.0;
+    s.xw = 0;                     // the plain CG update and x update
     if (s.bb <= 0.0) s.bb = 1.0;
   }
   cudaEvent_t e0, e1;
@@ -1900,6 +1901,7 @@ int hf_solve(hf_ctx* h, const double* b, double* x, hf_stats* stats) {
   double rms = std::sqrt(bb / (double)d.n) * d.mean_sinv * 1e-6;
   s.sigma = (c.opts.precision == HF_PREC_MIXED && rms > 0.0 && std::isfinite(rms))
                 ? std::exp2(std::rint(std::log2(rms))) : 1.0;
+  s.xw = 0;
   s.phase = PH_RES_INIT;
   if ((rc = push_scal(c))) return rc;
   if ((rc = device_solve(c))) return rc;
@@ -1956,6 +1958,7 @@ int hf_solve_device(hf_ctx* h, const double* b, double* x, hf_stats* stats) {
   s.x0flag = 0;
   s.tiny_pending = 0;
   s.status = 0;
+  s.xw = 0;
   s.phase = PH_RES_INIT;
   if ((rc = push_scal(c))) return rc;
   CU(cudaMemcpyAsync(c.A.b + d.off, b, 8 * d.n, cudaMemcpyDeviceToDevice, c.stream));

@@ -105,11 +105,17 @@ struct InstScal {
   int32_t hx_role;      // hx[hx_role] = H T^n, hx[1 - hx_role] = H T^(n-1) (when hx_ok says so)
   int32_t hx_ok;        // how many of those two products are valid (trailing steps, 0..2)
   int32_t hx_fresh;     // this step's last sweep stored H x of its final x in hx[1 - hx_role]
-  int32_t pad3;
+  int32_t xw;           // fused x update: kXwAllowed | kXwThis | kXwDone bits
   double sigma_prev;    // scale used by the previous residual sweep
   double last_err, last_relres;   // of the last finished step
   int64_t last_iter;
 };
+
+// InstScal::xw.  kXwAllowed: the inner CG update may form x itself (true-residual criterion;
+// FP32 vectors only on rows of 4k cells, where they index like x).  kXwThis: the next CG update
+// is predicted to be the inner solve's last and also forms x_new into role[3].  kXwDone: the last
+// CG update did so and y has not changed since, so the separate x update is skipped.
+constexpr int32_t kXwThis = 1, kXwDone = 2, kXwAllowed = 4;
 
 // Device-side control of a captured step (CUDA graph with conditional nodes).
 struct CtrlState {
@@ -136,7 +142,7 @@ enum : int32_t {
 };
 
 // Control block of one launch of the persistent solve kernel (zeroed before every launch).
-constexpr int kRoundLog = 64;                      // rounds whose end time is recorded
+constexpr int kRoundLog = 512;                     // rounds whose end time is recorded
 struct SolveCtl {
   unsigned count;          // blocks arrived at the current grid barrier
   unsigned gen;            // barrier generation (release/acquire)

@@ -127,12 +127,15 @@ __device__ __forceinline__ double rhs_cell(const DevArrays& A, const InstDesc& d
   return S;
 }
 
-// Vector form for rows of 4k cells: each thread owns 4 consecutive x cells of a quarter of the
-// task's planes (the layout of the solver's vector passes), so every thread has 4 independent
-// cells of FP64 work in flight: the pass is bound by the FP64 pipe, and one cell per thread left
-// it partly idle.  ||S||^2 is summed per thread plane by plane, cells in x order.
-__device__ __forceinline__ void rhs4_task(const DevArrays& A, int64_t task, const InstDesc& d,
-                                          const InstScal& s, const RhsCtx& r) {
+// The common task of a step under the true-residual criterion, on rows of 4k cells: no heated
+// cell, S = T^n scoef + ccat T^(n-1) - B and x0 = 2 T^n - T^(n-1) (3 FP64 instructions per cell),
+// the arithmetic and summation order of rhs4_task's fast form.  Kept apart from the general forms
+// (out of line) so that its operands stay in registers: with them in one body the kernel's 64
+// registers spilled, and the pass ran on local-memory traffic as large as its HBM traffic (ncu).
+// B is read only on the outer faces: boundary() (k_assemble, k_tempdep) gives it to no other
+// cell, where it is +0.0.
+__device__ __forceinline__ void rhs4_fast_task(const DevArrays& A, int64_t task, const InstDesc& d,
+                                               const InstScal& s) {
   const int4 tk = A.tasks[task];
   const int tid = threadIdx.x, grp = tid >> 6, w = tid & 63;
   const int x = tk.y + 4 * (w & 7), y = tk.z + (w >> 3);
@@ -140,6 +143,69 @@ __device__ __forceinline__ void rhs4_task(const DevArrays& A, int64_t task, cons
   const int per = (z1 - tk.w + 3) >> 2;
   const int za = min(tk.w + grp * per, z1), zb = min(za + per, z1);
   const bool act = x < d.nx && y < d.ny;
+  const bool face_col = x == 0 || x + 4 >= d.nx || y == 0 || y == d.ny - 1;
+  const bool cat = d.icattaneo == 1;
+  const int64_t off = d.off;
+  const int nxy = d.nx * d.ny, lxy = y * d.nx + x;
+  const double* Tp = A.tbuf[s.role[0]] + off;
+  const double* Tpp = A.tbuf[s.role[1]] + off;
+  double* X = A.tbuf[s.role[2]] + off;
+  const double* __restrict__ sc = A.scoef + off;
+  const double* __restrict__ ccat = A.ccat + off;
+  const double* __restrict__ bvec = A.bvec + off;
+  double* bout = A.b + off;
+  SqSum sq;
+  if (act) {
+    for (int z = za; z < zb; ++z) {
+      const int l = HF_IX4(A, lxy + z * nxy, d.n);
+      const double2* tp2 = reinterpret_cast<const double2*>(Tp + l);
+      const double2* tq2 = reinterpret_cast<const double2*>(Tpp + l);
+      const double2* sc2 = reinterpret_cast<const double2*>(sc + l);
+      const double2* cc2 = reinterpret_cast<const double2*>(ccat + l);
+      const double2* bv2 = reinterpret_cast<const double2*>(bvec + l);
+      const double2 t0 = tp2[0], t1 = tp2[1], u0 = tq2[0], u1 = tq2[1], h0 = sc2[0], h1 = sc2[1];
+      double2 c0 = make_double2(0.0, 0.0), c1 = c0, b0 = c0, b1 = c0;
+      if (cat) { c0 = cc2[0]; c1 = cc2[1]; }
+      if (face_col || z == 0 || z == d.nz - 1) { b0 = bv2[0]; b1 = bv2[1]; }
+      const double tp[4] = {t0.x, t0.y, t1.x, t1.y}, tpp[4] = {u0.x, u0.y, u1.x, u1.y};
+      const double rh[4] = {h0.x, h0.y, h1.x, h1.y}, cc[4] = {c0.x, c0.y, c1.x, c1.y};
+      const double bv[4] = {b0.x, b0.y, b1.x, b1.y};
+      double S[4], x0[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        S[i] = cat ? fma(tp[i], rh[i], cc[i] * tpp[i]) : tp[i] * rh[i];
+        if (!dbl_is_zero(bv[i])) S[i] = S[i] - bv[i];
+        x0[i] = fma(2.0, tp[i], -tpp[i]);
+        sq.add(S[i]);
+      }
+      reinterpret_cast<double2*>(bout + l)[0] = make_double2(S[0], S[1]);
+      reinterpret_cast<double2*>(bout + l)[1] = make_double2(S[2], S[3]);
+      reinterpret_cast<double2*>(X + l)[0] = make_double2(x0[0], x0[1]);
+      reinterpret_cast<double2*>(X + l)[1] = make_double2(x0[2], x0[3]);
+    }
+  }
+  const double bb = sq.value();
+  if (threadIdx.x == 0) A.partials[task * kNR + 1] = 0.0;   // no x0 - T < TINY test here
+  const double v[1] = {bb};
+  tile_store<1>(A, task, v);
+}
+
+// Vector form for rows of 4k cells: each thread owns 4 consecutive x cells of a quarter of the
+// task's planes (the layout of the solver's vector passes), so every thread has 4 independent
+// cells of FP64 work in flight: the pass is bound by the FP64 pipe, and one cell per thread left
+// it partly idle.  ||S||^2 is summed per thread plane by plane, cells in x order.
+__device__ __noinline__ void rhs4_task(const DevArrays& A, int64_t task, const InstDesc& d,
+                                       const InstScal& s, const RhsCtx& r) {
+  const int4 tk = A.tasks[task];
+  const int tid = threadIdx.x, grp = tid >> 6, w = tid & 63;
+  const int x = tk.y + 4 * (w & 7), y = tk.z + (w >> 3);
+  const int z1 = min(tk.w + d.zc, d.nz);
+  const int per = (z1 - tk.w + 3) >> 2;
+  const int za = min(tk.w + grp * per, z1), zb = min(za + per, z1);
+  const bool act = x < d.nx && y < d.ny;
+  // boundary() gives B only to cells on the outer faces (k_assemble, k_tempdep): elsewhere it is
+  // +0.0, so a quad off the x/y faces reads B only in the first and last plane
+  const bool face_col = x == 0 || x + 4 >= d.nx || y == 0 || y == d.ny - 1;
   const int64_t off = d.off;
   const int nxy = d.nx * d.ny, lxy = y * d.nx + x;
   const double* Tp = A.tbuf[s.role[0]] + off;
@@ -161,12 +227,15 @@ __device__ __forceinline__ void rhs4_task(const DevArrays& A, int64_t task, cons
       const double2* cc2 = reinterpret_cast<const double2*>(ccat + l);
       const double2* bv2 = reinterpret_cast<const double2*>(bvec + l);
       const double2 t0 = tp2[0], t1 = tp2[1], u0 = tq2[0], u1 = tq2[1];
-      const double2 h0 = rc2[0], h1 = rc2[1], c0 = cc2[0], c1 = cc2[1], b0 = bv2[0], b1 = bv2[1];
+      const double2 h0 = rc2[0], h1 = rc2[1], c0 = cc2[0], c1 = cc2[1];
+      double2 b0 = make_double2(0.0, 0.0), b1 = b0;
+      if (face_col || z == 0 || z == d.nz - 1) { b0 = bv2[0]; b1 = bv2[1]; }
       const double tp[4] = {t0.x, t0.y, t1.x, t1.y}, tpp[4] = {u0.x, u0.y, u1.x, u1.y};
       const double rh[4] = {h0.x, h0.y, h1.x, h1.y}, cc[4] = {c0.x, c0.y, c1.x, c1.y};
       const double bv[4] = {b0.x, b0.y, b1.x, b1.y};
       double S[4], x0[4];
-      if (r.heater) {
+      if (r.heater) {               // unrolled too: a dynamic index would put the arrays in
+#pragma unroll                      // local memory for both branches
         for (int i = 0; i < 4; ++i)
           S[i] = rhs_cell<true>(A, d, r, off, l + i, tp[i], tpp[i], rh[i], cc[i], bv[i], x0[i], flag);
       } else {
@@ -202,8 +271,13 @@ __global__ void __launch_bounds__(kBlock, 4) k_rhs(DevArrays A, double* oB, doub
     const InstScal& s = A.scal[inst];
     if ((d.nx & 3) == 0) {
       if (!s.outer_active) return;
+      const bool heater = d.heater && (d.has_em || A.task_heat[task]);
+      if (!heater && A.opts.criterion == HF_STOP_TRUE && d.isteady == 0) {
+        rhs4_fast_task(A, task, d, s);
+        return;
+      }
       RhsCtx r;
-      r.heater = d.heater && (d.has_em || A.task_heat[task]);
+      r.heater = heater;
       r.has_power = d.has_power; r.has_em = d.has_em; r.case5 = d.has_case5;
       r.cat = d.icattaneo == 1; r.steady = d.isteady != 0;
       r.qmode = d.qdens_mode;

@@ -63,6 +63,7 @@ __device__ __forceinline__ void begin_step(InstScal& s, int64_t itime) {
   s.tiny_pending = 0;
   s.err = 0.0;
   s.hx_fresh = 0;
+  s.xw = 0;
   s.phase = s.outer_active ? PH_RES_INIT : PH_IDLE;   // the persistent solve's first round
 }
 
@@ -578,29 +579,39 @@ __device__ __forceinline__ void upd_task(const DevArrays& A, double* part, int64
   const double* __restrict__ diag = A.diag + off;
   const bool act = c.act(0);
   const int nxy = c.nxy, base = c.base(0);
+  // FP64 vectors share the compact layout with x: the predicted last iteration also forms
+  // x_new = x + S^-1 y_new (the x update's arithmetic)
+  const bool wx = sizeof(T) == 8 && (s.xw & kXwThis) != 0;
+  const double* XR = A.tbuf[s.role[2]] + off;
+  double* XW = A.tbuf[s.role[3]] + off;
+  const double* __restrict__ sinv = A.sinv + off;
   T rr = T(0);
   double rw = 0.0;
   if (act) {
     for (int z0 = c.z0; z0 < c.z1; z0 += 4) {
       T pv[4], qv[4], rv[4], yv[4];
+      double xv[4], sv[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        pv[u] = T(0); qv[u] = T(0); rv[u] = T(0); yv[u] = T(0);
+        pv[u] = T(0); qv[u] = T(0); rv[u] = T(0); yv[u] = T(0); xv[u] = 0.0; sv[u] = 0.0;
         if (z0 + u < c.z1) {
           const int l = HF_IX(A, base + (z0 + u) * nxy, c.n());
           pv[u] = P[l]; qv[u] = Q[l]; rv[u] = R[l];
           if (!first) yv[u] = Y[l];
+          if (wx) { xv[u] = XR[l]; sv[u] = sinv[l]; }
         }
       }
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         if (z0 + u >= c.z1) continue;
         const int l = HF_IX(A, base + (z0 + u) * nxy, c.n());
-        Y[l] = first ? alpha * pv[u] : fma(alpha, pv[u], yv[u]);
+        const T y = first ? alpha * pv[u] : fma(alpha, pv[u], yv[u]);
+        Y[l] = y;
         const T r = fma(-alpha, qv[u], rv[u]);
         R[l] = r;
         rr = fma(r, r, rr);
         if (weighted) rw = fma(-diag[l] * (double)r, (double)r, rw);
+        if (wx) XW[l] = fma(sv[u], (double)y, xv[u]);
       }
     }
   }
@@ -877,7 +888,37 @@ __device__ __forceinline__ void upd4_task(const DevArrays& A, double* part, int6
   const double* __restrict__ diag = A.diag + c.off;
   T rr = T(0);
   double rw = 0.0;
-  if (c.act) {
+  if (c.act && (s.xw & kXwThis)) {
+    // The iteration predicted to end the inner solve also forms x_new = x + sigma S^-1 y_new, the
+    // x update's arithmetic on the y it stores (rows of 4k cells: both layouts index alike).
+    const double* XR = A.tbuf[s.role[2]] + c.off;
+    double* XW = A.tbuf[s.role[3]] + c.off;
+    const double* __restrict__ sinv = A.sinv + c.off;
+    const float* __restrict__ sinv32 = A.sinv32 + c.off;
+    const float sig = (float)s.sigma_prev;
+    for (int z = c.za; z < c.zb; ++z) {
+      const int l = HF_IX4(A, c.lxy + z * c.nxy, c.vn);
+      const V4<T> pv = ldv4(P + l), qv = ldv4(Q + l), rv = ldv4(R + l);
+      V4<T> yv{};
+      if (!first) yv = ldv4(Y + l);
+      V4<double> xv = ldv4(XR + l), sv{};
+      V4<float> fv{};
+      if (sizeof(T) == 8) sv = ldv4(sinv + l); else fv = ldv4(sinv32 + l);
+      V4<T> yo, ro;
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        yo.v[i] = first ? alpha * pv.v[i] : fma(alpha, pv.v[i], yv.v[i]);
+        const T r = fma(-alpha, qv.v[i], rv.v[i]);
+        ro.v[i] = r;
+        rr = fma(r, r, rr);
+        if (sizeof(T) == 8) xv.v[i] = fma(sv.v[i], (double)yo.v[i], xv.v[i]);
+        else xv.v[i] = xv.v[i] + f32_to_f64(sig * fv.v[i] * (float)yo.v[i]);
+      }
+      stv4(Y + l, yo);
+      stv4(R + l, ro);
+      stv4(XW + l, xv);
+    }
+  } else if (c.act) {
     for (int z = c.za; z < c.zb; z += 2) {
       const bool two = z + 1 < c.zb;
       const int l0 = HF_IX4(A, c.lxy + z * c.nxy, c.vn);
@@ -1104,7 +1145,7 @@ __global__ void __launch_bounds__(kBlock) k_residual(DevArrays A) {
 template <typename TY>
 __global__ void __launch_bounds__(kBlock) k_xupdate(DevArrays A) {
   const InstScal& s = A.scal[A.tasks[blockIdx.x].x];
-  if (!s.outer_active || s.inner_active || s.refine == 0) return;
+  if (!s.outer_active || s.inner_active || s.refine == 0 || (s.xw & kXwDone)) return;
   xupd_any<TY>(A, A.partials, blockIdx.x, s);
 }
 
@@ -1208,6 +1249,7 @@ __device__ void epi_rhs_diag(const DevArrays& A, int inst, const double* tot) {
 // Epilogue of a residual sweep: convergence test and set-up of the next inner solve.
 template <bool INIT>
 __device__ void epi_residual_s(InstScal& s, const InstDesc& G, const DevOpts& o, const double* tot) {
+  s.xw = 0;                              // this sweep consumed any x formed by a CG update
   if (!INIT) {
     const int t = s.role[2]; s.role[2] = s.role[3]; s.role[3] = t;
     s.tiny_pending = 0;
@@ -1261,6 +1303,11 @@ __device__ void epi_residual_s(InstScal& s, const InstDesc& G, const DevOpts& o,
     s.sigma = 1.0;
   }
   if (!(tot[1] > 0.0)) s.inner_active = 0;  // exact already: go straight to the update
+  if (s.inner_active && o.criterion == HF_STOP_TRUE &&
+      (o.precision != HF_PREC_MIXED || (G.nx & 3) == 0)) {
+    const int64_t cap = (o.precision == HF_PREC_MIXED) ? (int64_t)o.inner_itmax : o.itmax;
+    s.xw = kXwAllowed | (cap <= 1 ? kXwThis : 0);
+  }
 }
 
 
@@ -1278,7 +1325,7 @@ __device__ void epi_spmv_s(InstScal& s, const double* tot) {
 template <typename T>
 __device__ void epi_upd_s(InstScal& s, const DevOpts& o, const double* tot) {
   const bool weighted = (o.criterion == HF_STOP_RECURSIVE);
-  const double rho_new = tot[0];
+  const double rho_new = tot[0], rho_old = s.rho;
   s.beta = rho_new / s.rho;
   s.rho = rho_new;
   s.iter += 1;
@@ -1301,6 +1348,15 @@ __device__ void epi_upd_s(InstScal& s, const DevOpts& o, const double* tot) {
   }
   if (!(rho_new > 0.0)) stop = true;
   if (stop) s.inner_active = 0;
+  // Fused x update: whether the update that just ran formed x, and whether the next one should.
+  // The next iteration is predicted to end the solve when it reaches the iteration cap, or when
+  // the criterion shrinks once more by this iteration's factor: err_k^2 (rho_k / rho_(k-1)) <= eta^2.
+  const int32_t wrote = (s.xw & kXwThis) ? kXwDone : 0;
+  s.xw = (s.xw & kXwAllowed) | wrote;
+  if (!stop && (s.xw & kXwAllowed)) {
+    const double next = (rho_new / s.gg0) * (rho_new / rho_old);
+    if (s.iter + 1 >= cap || next <= s.eta * s.eta) s.xw |= kXwThis;
+  }
 }
 
 
@@ -1449,7 +1505,7 @@ template <typename T>
 __device__ __forceinline__ int32_t phase_after(const InstScal& s) {
   if (!s.outer_active) return PH_IDLE;
   if (s.inner_active) return PH_CG_P;   // the fused FP32 pass (PH_CG_PQ) measured slower
-  return PH_XUPD;
+  return (s.xw & kXwDone) ? PH_RES : PH_XUPD;   // the last CG update may have formed x already
 }
 __device__ __forceinline__ int phase_partials(int32_t ph) {
   return (ph == PH_RES_INIT || ph == PH_RES || ph == PH_CG_B) ? 2
@@ -1579,6 +1635,7 @@ __device__ bool grid_barrier_epilogue(const DevArrays& A, SolveCtl* ctl, unsigne
     if (threadIdx.x == 0 && round < kRoundLog) {
       int32_t ph = __ldcg(&A.scal[0].phase);
       if (ph == PH_RES_INIT && __ldcg(&A.scal[0].hx_ok) >= 2) ph = HF_PHASE_RES_INIT_HX;
+      if (ph == PH_CG_B && (__ldcg(&A.scal[0].xw) & kXwThis)) ph = HF_PHASE_CG_BX;
       ctl->phase_log[round] = ph;
     }
     const int act = all_epilogues<T>(A, red);

@@ -115,14 +115,14 @@ class HeatFlow:
         self._check(self.lib.hf_time_kernel(self.h, int(kernel), int(reps), C.byref(ms)), "hf_time_kernel")
         return ms.value
 
-    def solve_profile(self, cap: int = 64):
+    def solve_profile(self, cap: int = 512):
         """Rounds of the last persistent solve: [(phase name, microseconds), ...] and the total
-        number of rounds (the per-round list stops at 64)."""
+        number of rounds (the per-round list stops at 512)."""
         rounds = C.c_int64()
         ph = (C.c_int32 * cap)()
         us = (C.c_double * cap)()
         self._check(self.lib.hf_solve_profile(self.h, cap, C.byref(rounds), ph, us), "hf_solve_profile")
-        n = min(rounds.value, cap, 64)
+        n = min(rounds.value, cap, 512)
         return [(abi.PHASE_NAMES.get(ph[i], str(ph[i])), us[i]) for i in range(n)], rounds.value
 
     def step_timeline(self):

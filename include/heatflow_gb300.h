@@ -270,11 +270,13 @@ enum {
   HF_PHASE_CG_B = 6,      /* inner CG: y += alpha p, r -= alpha q, r.r */
   HF_PHASE_XUPD = 7,      /* x += sigma S^-1 y */
   HF_PHASE_RES = 8,       /* true residual of the updated x */
-  HF_PHASE_RES_INIT_HX = 9 /* first true residual from the stored H T^n and H T^(n-1) (pointwise) */
+  HF_PHASE_RES_INIT_HX = 9, /* first true residual from the stored H T^n and H T^(n-1) (pointwise) */
+  HF_PHASE_CG_BX = 10     /* inner CG update that also forms x += sigma S^-1 y: the iteration
+                             predicted to end the inner solve (true-residual criterion) */
 };
 /* Round profile of the context's last persistent solve (use_graph = 1, or hf_time_kernel with
  * HF_KERNEL_SOLVE).  No counterpart in the reference.  *rounds = grid-wide rounds run; for the
- * first min(rounds, cap, 64) rounds, phases[r] = the phase instance 0 ran and round_us[r] = the
+ * first min(rounds, cap, 512) rounds, phases[r] = the phase instance 0 ran and round_us[r] = the
  * round's length in microseconds (device %globaltimer; round 0 counts from the kernel's start). */
 int hf_solve_profile(hf_ctx* ctx, int64_t cap, int64_t* rounds, int32_t* phases, double* round_us);
 
