@@ -62,12 +62,13 @@ BYTES_PER_CELL = {
     "xupdate_fp64": 4 * 8,
     "cg_p_fp64": 3 * 8, "cg_spmv_fp64": 5 * 8, "cg_update_fp64": 6 * 8,
 }
-# FP64 floating-point operations per cell (an FMA counts 2) of the FP64-pipe kernels: the
-# residual does 7 FMA for S - Hx, 1 FMA for ||r||^2 and 1 sub for H x = S - r; the step-start
-# residual from the stored products 1 FMA + 1 add (S - 2 H T^n + H T^(n-1)) and 1 FMA
-# (||r||^2); the RHS under the true-residual criterion 1 mul + 1 FMA (S = T^n c1 + ccat T^(n-1))
-# and 1 FMA (x0 = 2 T^n - T^(n-1)) per interior cell - its ||S||^2 runs on the integer/FP32 pipes.
-FP64_FLOPS_PER_CELL = {"residual_mixed": 17, "residual_fp64": 19, "residual_init_hx_mixed": 5,
+# FP64 floating-point operations per cell (an FMA counts 2) of the FP64-pipe kernels: the mixed
+# residual does 7 FMA for S - Hx and 1 sub for H x = S - r (||r||^2 in FP32), the FP64 one also
+# 1 FMA for ||r||^2 and a multiply and an FMA for g and ||g||^2; the mixed step-start residual
+# from the stored products 1 FMA + 1 add (S - 2 H T^n + H T^(n-1), ||r||^2 in FP32); the RHS
+# under the true-residual criterion 1 mul + 1 FMA (S = T^n c1 + ccat T^(n-1)) and 1 FMA
+# (x0 = 2 T^n - T^(n-1)) per interior cell - its ||S||^2 runs on the integer/FP32 pipes.
+FP64_FLOPS_PER_CELL = {"residual_mixed": 15, "residual_fp64": 20, "residual_init_hx_mixed": 3,
                        "rhs": 5}
 
 # Algorithmic bytes per cell of each round of the persistent solve kernel (k_solve), by phase:
@@ -139,12 +140,12 @@ def solve_bytes_per_cell(rounds, precision):
 
 
 # FP64 instructions per cell of each round (the rest of the work is FP32/integer): the mixed
-# path's residual sweep 7 FMA + 1 sub (||r||^2 in FP32), its pointwise first residual 1 FMA + 1 add
-# + 1 FMA (||r||^2), the stencil first residual 7 + 1 FMA, the x update 1 add (also when a CG
-# update forms x).
+# path's residual sweep 7 FMA + 1 sub, its pointwise first residual 1 FMA + 1 add, the stencil
+# first residual 7 FMA (||r||^2 in FP32 in all three), the x update 1 add (also when a CG update
+# forms x).
 PHASE_FP64_INSTR = {
-    "mixed": {"res_init_hx": 3, "res_init": 8, "res": 8, "xupd": 1, "cg_bx": 1},
-    "fp64": {"res_init_hx": 5, "res_init": 10, "res": 10, "xupd": 1, "cg_p": 1, "cg_q": 7,
+    "mixed": {"res_init_hx": 2, "res_init": 7, "res": 8, "xupd": 1, "cg_bx": 1},
+    "fp64": {"res_init_hx": 5, "res_init": 10, "res": 11, "xupd": 1, "cg_p": 1, "cg_q": 7,
              "cg_b": 3, "cg_bx": 4},
 }
 

@@ -657,7 +657,22 @@ int download_padded(Ctx& c, T* dst, const T* src) {
   return HF_OK;
 }
 
-int effective_depth(const hf_solver_opts& o) { return o.task_depth > 0 ? o.task_depth : kZC; }
+// Task depth of the option 0 (default): kZC planes, or fewer (halving down to kMinTaskDepth) while
+// the grids would give fewer tasks than a persistent solve has blocks (3 per SM on GB300's 152).
+// A round lasts as long as its slowest task, so on a small grid deep tasks leave most SMs idle:
+// a 64^3 grid has 32 tasks of 8192 cells at depth 32, 256 at depth 4.  A fixed count keeps the
+// task table, and so the bits, independent of the device.
+constexpr int64_t kDefaultMinTasks = 3 * 152;
+int effective_depth(const Ctx& c, const hf_solver_opts& o) {
+  if (o.task_depth > 0) return o.task_depth;
+  for (int depth = kZC; depth > kMinTaskDepth; depth /= 2) {
+    int64_t n = 0;
+    for (const InstDesc& d : c.h_inst)
+      n += (int64_t)((d.nx + kTX - 1) / kTX) * ((d.ny + kTY - 1) / kTY) * ((d.nz + depth - 1) / depth);
+    if (n >= kDefaultMinTasks) return depth;
+  }
+  return kMinTaskDepth;
+}
 
 // (Re)build the task table for a task depth: per instance, kTX x kTY column tiles x `depth`
 // planes, ordered (z, y, x); uploads the table and the instance descriptors, recomputes the
@@ -915,7 +930,7 @@ int create_impl(const hf_problem* probs, int64_t count, const hf_solver_opts* op
     }
   }
   {
-    const int r = build_tasks(c, effective_depth(o));
+    const int r = build_tasks(c, effective_depth(c, o));
     if (r) return fail(r);
   }
   CK(launch_props(c, d_rho, d_hc, d_tau, d_em));
@@ -995,7 +1010,7 @@ int hf_set_opts(hf_ctx* h, const hf_solver_opts* opts) {
   h->c.opts = *opts;
   h->c.A.opts = dev_opts(*opts);
   drop_graph(h->c);   // captured kernels hold the options by value
-  if (effective_depth(*opts) != h->c.depth) return build_tasks(h->c, effective_depth(*opts));
+  if (effective_depth(h->c, *opts) != h->c.depth) return build_tasks(h->c, effective_depth(h->c, *opts));
   return HF_OK;
 }
 

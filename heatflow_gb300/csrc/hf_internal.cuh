@@ -111,8 +111,9 @@ struct InstScal {
   int64_t last_iter;
 };
 
-// InstScal::xw.  kXwAllowed: the inner CG update may form x itself (true-residual criterion;
-// FP32 vectors only on rows of 4k cells, where they index like x).  kXwThis: the next CG update
+// InstScal::xw.  kXwAllowed: the inner CG update may form x itself (true-residual criterion, rows
+// of 4k cells: the vector form of the update, whose FP32 vectors index like x there).  kXwThis:
+// the next CG update
 // is predicted to be the inner solve's last and also forms x_new into role[3].  kXwDone: the last
 // CG update did so and y has not changed since, so the separate x update is skipped.
 constexpr int32_t kXwThis = 1, kXwDone = 2, kXwAllowed = 4;

@@ -224,6 +224,7 @@ __device__ __forceinline__ void res_hx_task(const DevArrays& A, double* part, in
   const bool tiny = tiny_applies(A, s);       // the residual of x0 + TINY: r(x0) - TINY * H1
   double rr = 0.0, gg64 = 0.0;
   float gg = 0.f;
+  SqSum rq;                                    // mixed: ||r||^2 off the FP64 pipe
   if (c.act(0)) {
     const int nxy = c.nxy, base = c.base(0);
     const int rxy = f32 ? c.nxy4 : nxy, rbase = f32 ? c.base4(0) : base;
@@ -239,7 +240,7 @@ __device__ __forceinline__ void res_hx_task(const DevArrays& A, double* part, in
       double a = fma(-2.0, yc[lc], b[lc]);
       a = a + yp[lc];
       if (tiny) a = fma(-kTiny, rsum[lc], a);
-      rr = fma(a, a, rr);
+      if (sizeof(TR) == 4) rq.add(a); else rr = fma(a, a, rr);
       if (sizeof(TR) == 4) {
         const float g = -sinv32[lc] * f64_to_f32_trunc(a) * isig;
         R[HF_IX(A, lr, c.n4())] = (TR)g;
@@ -251,6 +252,7 @@ __device__ __forceinline__ void res_hx_task(const DevArrays& A, double* part, in
       }
     }
   }
+  if (sizeof(TR) == 4) rr = rq.value();
   if (sizeof(TR) == 4) {
     task_store_f(part + task * kNR, 1, gg);
     const double v[1] = {rr};
@@ -269,7 +271,8 @@ __device__ __forceinline__ void res_hx4_task(const DevArrays& A, double* part, i
 // FP64 true residual of one task: r = S - H x with x in the x-read buffer (INIT: x0 from the RHS
 // kernel) or, after an update, in the x-write buffer (the epilogue then swaps the roles).  Writes
 // g = -S^-1 r / sigma into the inner residual (type TR).  FP64 work per cell: 7 FMA for S - Hx,
-// 1 FMA for ||r||^2; after an update also H x = S - r into hx[1 - hx_role] (1 subtraction).
+// 1 FMA for ||r||^2 on the FP64 path (the mixed path sums it in FP32, SqSum); after an update
+// also H x = S - r into hx[1 - hx_role] (1 subtraction).
 template <bool INIT, typename TR>
 __device__ __forceinline__ void res_task(const DevArrays& A, double* part, int64_t task,
                                           const InstScal& s) {
@@ -294,8 +297,8 @@ __device__ __forceinline__ void res_task(const DevArrays& A, double* part, int64
   const int rxy = f32 ? c.nxy4 : c.nxy, rbase = f32 ? c.base4(0) : c.base(0);
   double* HX = A.hx[1 - s.hx_role] + off;
   const float isig = (float)(1.0 / s.sigma);
-  // mixed, after an update: ||r||^2 summed in FP32 over per-thread scaled r (one FP64 instruction
-  // less per cell on this FP64-bound sweep)
+  // mixed: ||r||^2 summed in FP32 over per-thread scaled r (one FP64 instruction less per cell on
+  // this FP64-bound sweep)
   SqSum rq;
   // INIT: the residual of x0 + TINY (mod_evolve.f90:141) is r(x0) - TINY * H1
   const bool tiny = INIT && tiny_applies(A, s);
@@ -349,7 +352,7 @@ __device__ __forceinline__ void res_task(const DevArrays& A, double* part, int64
         a = fma(-czc, xn, a);
         a = fma(-czm, xm, a);
       }
-      if (INIT || sizeof(TR) == 8) rr = fma(a, a, rr);
+      if (sizeof(TR) == 8) rr = fma(a, a, rr);
       else rq.add(a);
       const int lc = HF_IX(A, l, n);
       if (!INIT) HX[lc] = bl - a;
@@ -367,7 +370,7 @@ __device__ __forceinline__ void res_task(const DevArrays& A, double* part, int64
     xm = xc;
     xc = xn;
   }
-  if (!INIT && sizeof(TR) == 4) rr = rq.value();
+  if (sizeof(TR) == 4) rr = rq.value();
   if (sizeof(TR) == 4) {
     task_store_f(part + task * kNR, 1, gg);
     const double v[1] = {rr};
@@ -579,39 +582,29 @@ __device__ __forceinline__ void upd_task(const DevArrays& A, double* part, int64
   const double* __restrict__ diag = A.diag + off;
   const bool act = c.act(0);
   const int nxy = c.nxy, base = c.base(0);
-  // FP64 vectors share the compact layout with x: the predicted last iteration also forms
-  // x_new = x + S^-1 y_new (the x update's arithmetic)
-  const bool wx = sizeof(T) == 8 && (s.xw & kXwThis) != 0;
-  const double* XR = A.tbuf[s.role[2]] + off;
-  double* XW = A.tbuf[s.role[3]] + off;
-  const double* __restrict__ sinv = A.sinv + off;
   T rr = T(0);
   double rw = 0.0;
   if (act) {
     for (int z0 = c.z0; z0 < c.z1; z0 += 4) {
       T pv[4], qv[4], rv[4], yv[4];
-      double xv[4], sv[4];
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
-        pv[u] = T(0); qv[u] = T(0); rv[u] = T(0); yv[u] = T(0); xv[u] = 0.0; sv[u] = 0.0;
+        pv[u] = T(0); qv[u] = T(0); rv[u] = T(0); yv[u] = T(0);
         if (z0 + u < c.z1) {
           const int l = HF_IX(A, base + (z0 + u) * nxy, c.n());
           pv[u] = P[l]; qv[u] = Q[l]; rv[u] = R[l];
           if (!first) yv[u] = Y[l];
-          if (wx) { xv[u] = XR[l]; sv[u] = sinv[l]; }
         }
       }
 #pragma unroll
       for (int u = 0; u < 4; ++u) {
         if (z0 + u >= c.z1) continue;
         const int l = HF_IX(A, base + (z0 + u) * nxy, c.n());
-        const T y = first ? alpha * pv[u] : fma(alpha, pv[u], yv[u]);
-        Y[l] = y;
+        Y[l] = first ? alpha * pv[u] : fma(alpha, pv[u], yv[u]);
         const T r = fma(-alpha, qv[u], rv[u]);
         R[l] = r;
         rr = fma(r, r, rr);
         if (weighted) rw = fma(-diag[l] * (double)r, (double)r, rw);
-        if (wx) XW[l] = fma(sv[u], (double)y, xv[u]);
       }
     }
   }
@@ -1067,6 +1060,7 @@ __device__ __forceinline__ void res_hx4_task(const DevArrays& A, double* part, i
   const bool tiny = tiny_applies(A, s);       // the residual of x0 + TINY: r(x0) - TINY * H1
   double rr = 0.0, gg64 = 0.0;
   float gg = 0.f;
+  SqSum rq;                                    // mixed: ||r||^2 off the FP64 pipe
   if (c.act) {
     for (int z = c.za; z < c.zb; ++z) {
       const int l = HF_IX4(A, c.lxy + z * c.nxy, c.vn);
@@ -1082,7 +1076,7 @@ __device__ __forceinline__ void res_hx4_task(const DevArrays& A, double* part, i
         double a = fma(-2.0, cv.v[i], bv.v[i]);
         a = a + pv.v[i];
         if (tiny) a = fma(-kTiny, rs.v[i], a);
-        rr = fma(a, a, rr);
+        if (f32) rq.add(a); else rr = fma(a, a, rr);
         if (f32) {
           const float g = -s32.v[i] * f64_to_f32_trunc(a) * isig;
           g4.v[i] = (TR)g;
@@ -1096,6 +1090,7 @@ __device__ __forceinline__ void res_hx4_task(const DevArrays& A, double* part, i
       stv4(R + l, g4);
     }
   }
+  if (f32) rr = rq.value();
   if (sizeof(TR) == 4) {
     task_store_f(part + task * kNR, 1, gg);
     const double v[1] = {rr};
@@ -1303,8 +1298,7 @@ __device__ void epi_residual_s(InstScal& s, const InstDesc& G, const DevOpts& o,
     s.sigma = 1.0;
   }
   if (!(tot[1] > 0.0)) s.inner_active = 0;  // exact already: go straight to the update
-  if (s.inner_active && o.criterion == HF_STOP_TRUE &&
-      (o.precision != HF_PREC_MIXED || (G.nx & 3) == 0)) {
+  if (s.inner_active && o.criterion == HF_STOP_TRUE && (G.nx & 3) == 0) {
     const int64_t cap = (o.precision == HF_PREC_MIXED) ? (int64_t)o.inner_itmax : o.itmax;
     s.xw = kXwAllowed | (cap <= 1 ? kXwThis : 0);
   }

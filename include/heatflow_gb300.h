@@ -102,7 +102,8 @@ typedef struct hf_solver_opts {
                            2 = a CUDA graph per step with conditional WHILE/SWITCH nodes;
                            3 = as 1, but one graph launch per step (kernels visible to profilers,
                            which do not see kernels inside conditional nodes) */
-  int32_t task_depth;   /* z-planes per task of the step kernels (0: 32; otherwise 4..1024) */
+  int32_t task_depth;   /* z-planes per task of the step kernels (0: 32, or 16/8/4 when the
+                           grids would give fewer than 456 tasks; otherwise 4..1024) */
 } hf_solver_opts;
 
 typedef struct hf_stats {
