@@ -111,10 +111,12 @@ void drop_graph(Ctx& c) {
   if (c.loop_graph) cudaGraphDestroy(c.loop_graph);
   c.loop_exec = nullptr;
   c.loop_graph = nullptr;
-  if (c.post_exec) cudaGraphExecDestroy(c.post_exec);
-  if (c.post_graph) cudaGraphDestroy(c.post_graph);
-  c.post_exec = nullptr;
-  c.post_graph = nullptr;
+  for (int j = 0; j < 2; ++j) {
+    if (c.post_exec[j]) cudaGraphExecDestroy(c.post_exec[j]);
+    if (c.post_graph[j]) cudaGraphDestroy(c.post_graph[j]);
+    c.post_exec[j] = nullptr;
+    c.post_graph[j] = nullptr;
+  }
 }
 
 void free_all(Ctx& c) {
@@ -131,6 +133,10 @@ void free_all(Ctx& c) {
       e = nullptr;
     }
     o.ptr = nullptr;
+  }
+  for (auto& e : c.stage_x_free) {
+    if (e) cudaEventDestroy(e);
+    e = nullptr;
   }
   for (auto& st : c.stage) {
     for (cudaEvent_t* e : {&st.in_pp, &st.free}) {
@@ -495,12 +501,15 @@ int build_graph(Ctx& c) {
 // The step after its RHS (RHS finalize, persistent solve, step end, property rebuild) as one
 // graph, for steps whose RHS runs chunk by chunk behind the host upload (hf_step_host_async).
 int build_post_graph(Ctx& c) {
-  if (c.post_exec && c.post_precision == c.opts.precision && c.post_criterion == c.opts.criterion)
+  if (c.post_exec[0] && c.post_exec[1] && c.post_precision == c.opts.precision &&
+      c.post_criterion == c.opts.criterion)
     return HF_OK;
-  if (c.post_exec) cudaGraphExecDestroy(c.post_exec);
-  if (c.post_graph) cudaGraphDestroy(c.post_graph);
-  c.post_exec = nullptr;
-  c.post_graph = nullptr;
+  for (int j = 0; j < 2; ++j) {
+    if (c.post_exec[j]) cudaGraphExecDestroy(c.post_exec[j]);
+    if (c.post_graph[j]) cudaGraphDestroy(c.post_graph[j]);
+    c.post_exec[j] = nullptr;
+    c.post_graph[j] = nullptr;
+  }
   if (!c.d_ctrl) {
     int r = dalloc(c, &c.d_ctrl, 1);
     if (r) return r;
@@ -511,31 +520,41 @@ int build_post_graph(Ctx& c) {
   cudaStream_t cs = nullptr;
   CU(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
   cudaStream_t saved = c.stream;
-  cudaGraph_t g = nullptr;
   std::string err;
   auto chk = [&](cudaError_t e, const char* what) {
     if (e != cudaSuccess && err.empty()) err = std::string(what) + ": " + cudaGetErrorString(e);
     return e == cudaSuccess;
   };
-  if (chk(cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed), "capture")) {
-    c.stream = cs;
-    chk(launch_finalize(c, FIN_RHS, nullptr, 0, 0), "rhs finalize");
-    chk(launch_solve(c), "persistent solve");
-    chk(launch_graph_step_end(c, c.d_ctrl, c.d_sctl), "step end");
-    if (c.tempdep) chk(launch_tempdep(c), "properties");
-    chk(cudaStreamEndCapture(cs, &g), "end capture");
-    if (err.empty()) chk(cudaGraphInstantiate(&c.post_exec, g, 0), "instantiate");
+  // one graph per result buffer: the kernels' DevArrays carry it as xout (only these graphs do)
+  for (int j = 0; j < 2 && err.empty(); ++j) {
+    cudaGraph_t g = nullptr;
+    if (chk(cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed), "capture")) {
+      c.stream = cs;
+      c.A.xout = c.d_stage_x[j];
+      chk(launch_finalize(c, FIN_RHS, nullptr, 0, 0), "rhs finalize");
+      chk(launch_solve(c), "persistent solve");
+      chk(launch_stage_fallback(c), "result fallback");
+      chk(launch_graph_step_end(c, c.d_ctrl, c.d_sctl), "step end");
+      if (c.tempdep) chk(launch_tempdep(c), "properties");
+      c.A.xout = nullptr;
+      chk(cudaStreamEndCapture(cs, &g), "end capture");
+      if (err.empty()) chk(cudaGraphInstantiate(&c.post_exec[j], g, 0), "instantiate");
+    }
+    c.post_graph[j] = g;
   }
+  c.A.xout = nullptr;
   c.stream = saved;
   cudaStreamDestroy(cs);
   if (!err.empty()) {
-    if (c.post_exec) cudaGraphExecDestroy(c.post_exec);
-    c.post_exec = nullptr;
-    if (g) cudaGraphDestroy(g);
+    for (int j = 0; j < 2; ++j) {
+      if (c.post_exec[j]) cudaGraphExecDestroy(c.post_exec[j]);
+      if (c.post_graph[j]) cudaGraphDestroy(c.post_graph[j]);
+      c.post_exec[j] = nullptr;
+      c.post_graph[j] = nullptr;
+    }
     cudaGetLastError();
     return set_err(HF_ECUDA, "graph capture: " + err);
   }
-  c.post_graph = g;
   c.post_precision = c.opts.precision;
   c.post_criterion = c.opts.criterion;
   return HF_OK;
@@ -1147,6 +1166,11 @@ int hf_step_host_async(hf_ctx* h, int64_t itime, const double* tp, const double*
     c.async_steps = 0;
     c.async_calls.clear();
     c.async_host_kernels = 0;
+    for (int j = 0; j < 2; ++j) {   // the result buffers are part of the post-RHS graphs
+      if (!c.d_stage_x[j] && (rc = dalloc(c, &c.d_stage_x[j], (size_t)total))) return rc;
+      if (!c.stage_x_free[j]) CU(cudaEventCreateWithFlags(&c.stage_x_free[j], cudaEventDisableTiming));
+      CU(cudaEventRecord(c.stage_x_free[j], c.stream));
+    }
     if ((rc = build_post_graph(c))) return rc;
     build_host_chunks(c);
     if (!c.copy_stream) CU(cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking));
@@ -1166,7 +1190,6 @@ int hf_step_host_async(hf_ctx* h, int64_t itime, const double* tp, const double*
         if (!*b && (rc = dalloc(c, b, (size_t)total))) return rc;
       CU(cudaEventRecord(st.free, c.stream));
     }
-    if (!c.d_stage_out && (rc = dalloc(c, &c.d_stage_out, (size_t)total))) return rc;
     if (!c.d_check_call && (rc = dalloc(c, &c.d_check_call, (size_t)1))) return rc;
     const int64_t none = INT64_MAX;
     CU(cudaMemcpyAsync(c.d_check_call, &none, sizeof(none), cudaMemcpyHostToDevice, c.stream));
@@ -1188,7 +1211,8 @@ int hf_step_host_async(hf_ctx* h, int64_t itime, const double* tp, const double*
   const bool early = call >= 1 && tp == c.outs[c.out_last].ptr && tpp == c.async_calls.back().tp;
   // Copy stream.  A staging set is free once the consumer of its previous inputs (two calls back)
   // has run; by then every download older than the last kHostOuts queued ones is done (the main
-  // stream had passed a gather that waited for it).  An input that is the destination of one of
+  // stream had waited, before that call's post-RHS graph, for the download of two calls before
+  // it, whose result buffer the graph rewrites).  An input that is the destination of one of
   // those downloads waits for it: T^(n-1), normally the result of two steps back, as a whole (its
   // upload then overlaps the previous step's solve); T^n, normally the previous step's result,
   // chunk by chunk behind that chunk's download, so both directions of the link run at once.
@@ -1221,41 +1245,44 @@ int hf_step_host_async(hf_ctx* h, int64_t itime, const double* tp, const double*
   if (early) {
     // begin the step from the device's copy of the inputs; the whole RHS as one launch
     CU(launch_ctrl_init(c, itime, 2 * (int64_t)(c.opts.max_refine + 3) * (per + 3)));
-    CU(launch_graph_step_begin(c, c.d_ctrl, 1 + 4 + (c.tempdep ? 4 : 0)));
+    CU(launch_graph_step_begin(c, c.d_ctrl, 1 + 5 + (c.tempdep ? 4 : 0)));
     CU(launch_rhs(c));
-    c.async_host_kernels += 2;                    // control reset, gather
+    c.async_host_kernels += 1;                    // control reset
   } else {
     // place T^(n-1), begin the step, then place each chunk of T^n as it lands and run the RHS of
     // its tasks (the later chunks are still on the link)
     CU(cudaStreamWaitEvent(c.stream, st.in_pp, 0));
     CU(launch_host_in(c, st.pp, 1, c.stream));
     CU(launch_ctrl_init(c, itime, 2 * (int64_t)(c.opts.max_refine + 3) * (per + 3)));
-    // kernels of the step outside the host copies: begin, RHS per chunk, finalize, solve, end
-    CU(launch_graph_step_begin(c, c.d_ctrl, nch + 4 + (c.tempdep ? 4 : 0)));
+    // kernels of the step outside the host copies: begin, RHS per chunk, finalize, solve, result
+    // fallback, end
+    CU(launch_graph_step_begin(c, c.d_ctrl, nch + 5 + (c.tempdep ? 4 : 0)));
     for (int k = 0; k < nch; ++k) {
       CU(cudaStreamWaitEvent(c.stream, st.in_chunk[k], 0));
       CU(launch_host_in_range(c, st.p, 0, ch[k].glo, ch[k].ghi, c.stream));
       CU(launch_rhs_range(c, ch[k].tlo, ch[k].thi));
     }
     CU(cudaEventRecord(st.free, c.stream));
-    c.async_host_kernels += 3 + nch;              // placements, control reset, gather
+    c.async_host_kernels += 2 + nch;              // placements, control reset
   }
-  // the rest of the step as one graph and the gather of its result; the download runs on a
-  // stream of its own, chunk by chunk, so the next step's work does not queue behind it
-  CU(cudaGraphLaunch(c.post_exec, c.stream));
-  CU(cudaStreamWaitEvent(c.stream, c.outs[c.out_last].done, 0));   // d_stage_out is free
-  CU(launch_host_out(c, c.d_stage_out, c.stream));
+  // the rest of the step as one graph, whose last residual sweep also stores the result into
+  // d_stage_x[call & 1] (free once the download of two calls back has read it); the download
+  // runs on a stream of its own, chunk by chunk, so the next step's work does not queue behind it
+  const int xj = (int)(call & 1);
+  CU(cudaStreamWaitEvent(c.stream, c.stage_x_free[xj], 0));
+  CU(cudaGraphLaunch(c.post_exec[xj], c.stream));
   CU(cudaEventRecord(c.ev_gathered, c.stream));
   CU(cudaStreamWaitEvent(c.out_stream, c.ev_gathered, 0));
   const int next = (c.out_last + 1) % Ctx::kHostOuts;   // replaces the oldest tracked download
   Ctx::HostOut& o = c.outs[next];
   for (int k = 0; k < nch; ++k) {
-    CU(cudaMemcpyAsync(out + ch[k].clo, c.d_stage_out + ch[k].clo,
+    CU(cudaMemcpyAsync(out + ch[k].clo, c.d_stage_x[xj] + ch[k].clo,
                        sizeof(double) * (size_t)(ch[k].chi - ch[k].clo), cudaMemcpyDeviceToHost,
                        c.out_stream));
     CU(cudaEventRecord(o.chunk[k], c.out_stream));
   }
   CU(cudaEventRecord(o.done, c.out_stream));
+  CU(cudaEventRecord(c.stage_x_free[xj], c.out_stream));
   o.ptr = out;
   c.out_last = next;
   c.async_calls.push_back(Ctx::HostCall{itime, tp, tpp, out, early});

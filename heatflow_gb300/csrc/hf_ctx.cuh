@@ -88,7 +88,11 @@ struct Ctx {
     cudaEvent_t free = nullptr;        // the set's consumer (placement or check) has run
   };
   Stage stage[2];
-  double* d_stage_out = nullptr;       // the last step's result
+  // The queued steps' results in the compact layout, written by each step's last residual sweep
+  // (or, for a step accepted at its first residual, by the fallback copy after it), for alternate
+  // calls; free again once the download that read it has run.
+  double* d_stage_x[2] = {nullptr, nullptr};
+  cudaEvent_t stage_x_free[2] = {nullptr, nullptr};
   // The queued calls.  A call whose inputs are the previous call's result and inputs (the
   // rotation simulate() performs) starts from the device's own copy of them ("early"), while its
   // uploads travel; the next call (or hf_host_sync) checks the uploaded bits against that copy.
@@ -109,10 +113,11 @@ struct Ctx {
   std::vector<HostChunk> host_chunks;
   int host_chunks_depth = -1;           // task depth the chunks were cut for
   cudaStream_t out_stream = nullptr;    // downloads, so the next step's work need not queue behind them
-  cudaEvent_t ev_gathered = nullptr;    // the last queued step's result is in d_stage_out
-  // the step after its RHS (finalize, persistent solve, step end, property rebuild) as one graph
-  cudaGraphExec_t post_exec = nullptr;
-  cudaGraph_t post_graph = nullptr;
+  cudaEvent_t ev_gathered = nullptr;    // the last queued step's result is in its d_stage_x
+  // the step after its RHS (finalize, persistent solve, step end, result fallback, property
+  // rebuild) as one graph per result buffer d_stage_x[j]
+  cudaGraphExec_t post_exec[2] = {nullptr, nullptr};
+  cudaGraph_t post_graph[2] = {nullptr, nullptr};
   int post_precision = -1, post_criterion = -1;
   bool async_pending = false;          // steps queued since the last hf_host_sync
   int64_t async_steps = 0;             // = async_calls.size()

@@ -205,6 +205,10 @@ struct DevArrays {
   // index-check record of the checked build (HF_CHECKED): [0] failed checks, [1] site of the
   // first, [2] its index, [3] the extent it was checked against
   unsigned long long* check;
+  // host-buffer steps (the graphs of hf_step_host_async only, null elsewhere): the residual
+  // sweeps after an update also store x here, in the compact layout (InstDesc::hoff), so the
+  // step's result needs no gather for its download
+  double* xout;
 };
 
 // ---- index checks of the checked build ----------------------------------------------------------
@@ -473,7 +477,7 @@ cudaError_t launch_host_in(Ctx& c, const double* src, int which, cudaStream_t st
 // The same for the device cells [glo, ghi) (whole z-slabs of instances, padding skipped).
 cudaError_t launch_host_in_range(Ctx& c, const double* src, int which, int64_t glo, int64_t ghi,
                                  cudaStream_t stream);
-cudaError_t launch_host_out(Ctx& c, double* dst, cudaStream_t stream);
+cudaError_t launch_stage_fallback(Ctx& c);
 // Bit-for-bit check of uploaded inputs (compact layout) against the device's T^n and T^(n-1) of
 // the step that just ended (roles 1 and 2 after its rotation): a difference sets *first to
 // min(*first, call).  Instances whose step failed are skipped.

@@ -559,7 +559,7 @@ cudaError_t launch_subbox_gather(Ctx& c, int64_t inst, const int64_t* lo, const 
 
 // ---- host-buffer steps: staging arrays <-> role buffers -----------------------------------------
 // The copy engines move compact arrays (instance i's cells from InstDesc::hoff, no padding); these
-// kernels place them into, or gather them from, the temperature role buffers, whose indices live
+// kernels place them into, or compare them with, the temperature role buffers, whose indices live
 // on the device, so they can be queued behind the step that rotates the roles.  Placing compares
 // bit patterns first: an input that is exactly the state already there (a caller feeding back the
 // results it downloaded) keeps the stored products H T^n, H T^(n-1); any other drops them.
@@ -595,14 +595,27 @@ __global__ void k_host_check(DevArrays A, const double* __restrict__ sp,
   if (diff) atomicMin(reinterpret_cast<long long*>(first), (long long)call);
 }
 
-__global__ void k_host_out(DevArrays A, double* __restrict__ dst) {
+// The result of a host-buffer step for the instances whose last residual sweep did not store it
+// in A.xout; runs after the solve, before the step end rotates the roles.  A step accepted at its
+// first residual (no sweep after an update: hx_fresh = 0) has x = x0 in role 2; a failed step
+// keeps T^n (role 0), which is what it returns.  The blocks first look whether any instance needs
+// it, so the common step costs one short pass over the instances' scalars.
+__global__ void k_stage_fallback(DevArrays A) {
+  int need = 0;
+  for (int64_t i = threadIdx.x; i < A.ninst; i += blockDim.x) {
+    const InstScal& s = A.scal[i];
+    need |= (s.status != 0 || s.hx_fresh == 0) ? 1 : 0;
+  }
+  if (!__syncthreads_or(need)) return;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < A.ncells; g += stride) {
     const int inst = A.tile_inst[g / kTile];
     const InstDesc& d = A.inst[inst];
     const int64_t l = g - d.off;
     if (l >= d.n) continue;
-    dst[d.hoff + l] = A.tbuf[A.scal[inst].role[0]][g];
+    const InstScal& s = A.scal[inst];
+    if (s.status == 0 && s.hx_fresh != 0) continue;
+    A.xout[d.hoff + l] = A.tbuf[s.role[s.status != 0 ? 0 : 2]][g];
   }
 }
 
@@ -642,8 +655,8 @@ cudaError_t launch_host_check(Ctx& c, const double* sp, const double* spp, int64
   return cudaGetLastError();
 }
 
-cudaError_t launch_host_out(Ctx& c, double* dst, cudaStream_t stream) {
-  k_host_out<<<host_copy_blocks(c), 256, 0, stream>>>(c.A, dst);
+cudaError_t launch_stage_fallback(Ctx& c) {
+  k_stage_fallback<<<152, 256, 0, c.stream>>>(c.A);
   return cudaGetLastError();
 }
 

@@ -273,7 +273,7 @@ __device__ __forceinline__ void res_hx4_task(const DevArrays& A, double* part, i
 // g = -S^-1 r / sigma into the inner residual (type TR).  FP64 work per cell: 7 FMA for S - Hx,
 // 1 FMA for ||r||^2 on the FP64 path (the mixed path sums it in FP32, SqSum); after an update
 // also H x = S - r into hx[1 - hx_role] (1 subtraction).
-template <bool INIT, typename TR>
+template <bool INIT, typename TR, bool XOUT = false>
 __device__ __forceinline__ void res_task(const DevArrays& A, double* part, int64_t task,
                                           const InstScal& s) {
   if (INIT && s.hx_ok >= 2) {
@@ -296,6 +296,8 @@ __device__ __forceinline__ void res_task(const DevArrays& A, double* part, int64
   TR* R = Vec<TR>::r(A) + (f32 ? c.off4 : off);
   const int rxy = f32 ? c.nxy4 : c.nxy, rbase = f32 ? c.base4(0) : c.base(0);
   double* HX = A.hx[1 - s.hx_role] + off;
+  // host-buffer steps (the persistent solve of their graphs): x into the result buffer too
+  double* XO = (XOUT && !INIT) ? A.xout + A.inst[c.inst].hoff : nullptr;
   const float isig = (float)(1.0 / s.sigma);
   // mixed: ||r||^2 summed in FP32 over per-thread scaled r (one FP64 instruction less per cell on
   // this FP64-bound sweep)
@@ -356,6 +358,7 @@ __device__ __forceinline__ void res_task(const DevArrays& A, double* part, int64
       else rq.add(a);
       const int lc = HF_IX(A, l, n);
       if (!INIT) HX[lc] = bl - a;
+      if (XOUT && !INIT) XO[lc] = xc;
       if (sizeof(TR) == 4) {             // mixed: g in FP32, scaled by 1/sigma
         const float g = -sinv32[lc] * f64_to_f32_trunc(a) * isig;
         R[HF_IX(A, rbase + z * rxy, c.n4())] = (TR)g;
@@ -1669,7 +1672,7 @@ __device__ bool grid_barrier_epilogue(const DevArrays& A, SolveCtl* ctl, unsigne
   return s_ok != 0;
 }
 
-template <typename T>
+template <typename T, bool XOUT>
 __device__ __forceinline__ void round_task(const DevArrays& A, double* part, int64_t task,
                                            const InstScal& s) {
   if constexpr (sizeof(T) == 4) {
@@ -1684,7 +1687,7 @@ __device__ __forceinline__ void round_task(const DevArrays& A, double* part, int
   }
   switch (s.phase) {
     case PH_RES_INIT: res_task<true, T>(A, part, task, s); break;
-    case PH_RES: res_task<false, T>(A, part, task, s); break;
+    case PH_RES: res_task<false, T, XOUT>(A, part, task, s); break;
     case PH_CG_P: cgp_any<T>(A, part, task, s); break;
     case PH_CG_B: upd_any<T>(A, part, task, s); break;
     case PH_XUPD: xupd_any<T>(A, part, task, s); break;
@@ -1693,7 +1696,9 @@ __device__ __forceinline__ void round_task(const DevArrays& A, double* part, int
 }
 
 // Blocks per SM: 3 (85 registers: the FP64 stencil and the FP32 vector pass need about that).
-template <typename T>
+// XOUT: the instance used by the graphs of host-buffer steps, whose residual sweeps also store x
+// into A.xout (a variant of its own, so the other solves carry none of it).
+template <typename T, bool XOUT>
 __global__ void __launch_bounds__(kBlock, 3)
     k_solve(DevArrays A, SolveCtl* ctl, int64_t limit, unsigned long long wait_ns, int leaver) {
   __shared__ InstScal sh;
@@ -1737,7 +1742,7 @@ __global__ void __launch_bounds__(kBlock, 3)
           __syncthreads();
           cur = inst;
         }
-        if (sh.phase != PH_IDLE) round_task<T>(A, A.partials, t, sh);
+        if (sh.phase != PH_IDLE) round_task<T, XOUT>(A, A.partials, t, sh);
       }
       __syncthreads();                       // s_next holds the block's next task
       k = s_next;
@@ -1755,10 +1760,14 @@ __global__ void __launch_bounds__(kBlock, 3)
 int solve_grid_blocks(Ctx& c, int fp32) {
   int& cached = c.solve_blocks[fp32 ? 1 : 0];
   if (cached > 0) return cached;
-  int per_sm = 0, nsm = 0;
-  cudaError_t e = fp32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve<float>, kBlock, 0)
-                       : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve<double>, kBlock, 0);
+  int per_sm = 0, per_sm_x = 0, nsm = 0;
+  cudaError_t e = fp32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve<float, false>, kBlock, 0)
+                       : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve<double, false>, kBlock, 0);
   if (e != cudaSuccess) return -1;
+  e = fp32 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_x, k_solve<float, true>, kBlock, 0)
+           : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_x, k_solve<double, true>, kBlock, 0);
+  if (e != cudaSuccess) return -1;
+  if (per_sm_x < per_sm) per_sm = per_sm_x;    // one grid size for both variants
   if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, c.device) != cudaSuccess) return -1;
   // every SM holds the same number of blocks; tasks are handed out one at a time, so the blocks
   // of busier SMs take fewer of them
@@ -1788,8 +1797,12 @@ cudaError_t launch_solve(Ctx& c, unsigned long long wait_ns, int leaver) {
   at[0].val.cooperative = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  if (fp32) return cudaLaunchKernelEx(&cfg, k_solve<float>, c.A, c.d_sctl, limit, wait_ns, leaver);
-  return cudaLaunchKernelEx(&cfg, k_solve<double>, c.A, c.d_sctl, limit, wait_ns, leaver);
+  if (c.A.xout) {
+    if (fp32) return cudaLaunchKernelEx(&cfg, k_solve<float, true>, c.A, c.d_sctl, limit, wait_ns, leaver);
+    return cudaLaunchKernelEx(&cfg, k_solve<double, true>, c.A, c.d_sctl, limit, wait_ns, leaver);
+  }
+  if (fp32) return cudaLaunchKernelEx(&cfg, k_solve<float, false>, c.A, c.d_sctl, limit, wait_ns, leaver);
+  return cudaLaunchKernelEx(&cfg, k_solve<double, false>, c.A, c.d_sctl, limit, wait_ns, leaver);
 }
 
 #ifdef HF_CHECKED

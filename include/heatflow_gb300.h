@@ -208,7 +208,8 @@ int hf_adjoint_accumulate(hf_ctx* ctx, const double* lam, const double* x, int64
  * For callers that keep the state in host arrays, as simulate() does (Temp_p/Temp_pp): each call
  * queues one step whose inputs come from and whose result goes to pinned host memory, and returns
  * at once.  Copy engines move compact staging buffers (kernels place them into the state's role
- * buffers, whose indices live on the device, and gather the result).  T^(n-1) - normally the
+ * buffers, whose indices live on the device; the step's last residual sweep also writes its
+ * result into one, so the download needs no gather).  T^(n-1) - normally the
  * result of two calls back - is uploaded on a second stream while the previous step is still
  * solving; T^n - normally the previous call's temp_out - is uploaded chunk by chunk right behind
  * that download, so both directions of the host link run at once, and the right-hand side of

@@ -61,6 +61,27 @@ def test_async_equals_uninterrupted_run(cuda_lib):
     assert st["steps"] == 7 and st["inner_iterations"] == iters and st["unconverged"] == 0
 
 
+def test_async_step_accepted_at_first_residual(cuda_lib):
+    """The result of a host-buffer step is stored by the step's last residual sweep; a step
+    accepted at its first residual (x = x0, no sweep of an updated x) gets it from the fallback
+    copy after the solve: the bits of an uninterrupted run either way."""
+    prob = layered_slab(16, nz=20, layer=5)
+    kw = dict(KW, tol=1e-1)
+    tp, tpp = _initial(prob)
+    with HeatFlow(prob, **kw) as hf:
+        hf.set_state(tp, tpp)
+        st = hf.run(3, 5)
+        T_ref, Tp_ref = hf.get_state()
+    assert st["inner_iterations"] == 0 and st["refinements"] == 5
+    bufs = [_pinned(prob.ncells, 0.0) for _ in range(3)]
+    bufs[0][:] = tp
+    bufs[1][:] = tpp
+    with HeatFlow(prob, **kw) as hf:
+        st2, (cur, prev, _) = _run_async(hf, bufs, 3, 5)
+    assert st2["inner_iterations"] == 0 and st2["refinements"] == 5
+    assert np.array_equal(bufs[cur], T_ref) and np.array_equal(bufs[prev], Tp_ref)
+
+
 def test_async_products_used_and_dropped(cuda_lib):
     """Fed-back inputs keep the products (the first residual is pointwise from the third step on);
     a changed input makes the next two steps use the stencil, like a fresh context."""
