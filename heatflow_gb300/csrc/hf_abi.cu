@@ -677,11 +677,12 @@ int download_padded(Ctx& c, T* dst, const T* src) {
 }
 
 // Task depth of the option 0 (default): kZC planes, or fewer (halving down to kMinTaskDepth) while
-// the grids would give fewer tasks than a persistent solve has blocks (3 per SM on GB300's 152).
-// A round lasts as long as its slowest task, so on a small grid deep tasks leave most SMs idle:
-// a 64^3 grid has 32 tasks of 8192 cells at depth 32, 256 at depth 4.  A fixed count keeps the
-// task table, and so the bits, independent of the device.
-constexpr int64_t kDefaultMinTasks = 3 * 152;
+// the grids would give fewer than two tasks per block of a persistent solve (3 blocks per SM on
+// GB300's 152).  A round lasts as long as its slowest task, so on a small grid deep tasks leave
+// most SMs idle: a 64^3 grid has 32 tasks of 8192 cells at depth 32, 256 at depth 4; at 128^3
+// depth 8 (1024 tasks) solved faster than 16 (512) and 32.  A fixed count keeps the task table,
+// and so the bits, independent of the device.
+constexpr int64_t kDefaultMinTasks = 2 * 3 * 152;
 int effective_depth(const Ctx& c, const hf_solver_opts& o) {
   if (o.task_depth > 0) return o.task_depth;
   for (int depth = kZC; depth > kMinTaskDepth; depth /= 2) {

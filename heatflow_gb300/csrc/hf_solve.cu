@@ -1182,15 +1182,37 @@ __global__ void __launch_bounds__(kBlock) k_cg_upd(DevArrays A) {
 // kWarpSumMax tasks the whole block sums (thread-strided, then block_sum), otherwise warp 0 sums
 // (lane-strided, then a shuffle tree).  The result is valid in thread 0.  Partials are read
 // through L2 (written by other blocks of the same persistent launch).
+// acc += the partials of tasks first, first + step, ... (< ntask) of an instance, in that order.
+// The loads of kSumBatch tasks are issued before their adds (the same adds in the same order, so
+// the same bits): a grid barrier's epilogue waits on this sum, and one L2 round trip per task
+// made it several microseconds per round.
+constexpr int kSumBatch = 8;
+template <int NRV>
+__device__ __forceinline__ void strided_sum(const double* part, int64_t task0, int64_t ntask,
+                                            int64_t first, int step, double (&acc)[NRV]) {
+  for (int64_t t0 = first; t0 < ntask; t0 += (int64_t)kSumBatch * step) {
+    double v[kSumBatch][NRV];
+#pragma unroll
+    for (int u = 0; u < kSumBatch; ++u) {
+      const int64_t t = t0 + (int64_t)u * step;
+#pragma unroll
+      for (int k = 0; k < NRV; ++k) v[u][k] = t < ntask ? __ldcg(&part[(task0 + t) * kNR + k]) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < kSumBatch; ++u) {
+      if (t0 + (int64_t)u * step >= ntask) break;
+#pragma unroll
+      for (int k = 0; k < NRV; ++k) acc[k] += v[u][k];
+    }
+  }
+}
+
 template <int NRV>
 __device__ __forceinline__ void warp_instance_sum(const double* part, const InstDesc& d, int lane,
                                                   double (&acc)[NRV]) {
 #pragma unroll
   for (int k = 0; k < NRV; ++k) acc[k] = 0.0;
-  for (int64_t t = lane; t < d.ntask; t += 32) {
-#pragma unroll
-    for (int k = 0; k < NRV; ++k) acc[k] += __ldcg(&part[(d.task0 + t) * kNR + k]);
-  }
+  strided_sum<NRV>(part, d.task0, d.ntask, lane, 32, acc);
 #pragma unroll
   for (int k = 0; k < NRV; ++k) acc[k] = warp_sum(acc[k]);
 }
@@ -1201,10 +1223,7 @@ __device__ __forceinline__ void instance_sum(const double* part, const InstDesc&
   if (d.ntask > kWarpSumMax) {
 #pragma unroll
     for (int k = 0; k < NRV; ++k) acc[k] = 0.0;
-    for (int64_t t = threadIdx.x; t < d.ntask; t += blockDim.x) {
-#pragma unroll
-      for (int k = 0; k < NRV; ++k) acc[k] += __ldcg(&part[(d.task0 + t) * kNR + k]);
-    }
+    strided_sum<NRV>(part, d.task0, d.ntask, threadIdx.x, (int)blockDim.x, acc);
     block_sum<NRV>(acc, red);
   } else if (threadIdx.x < 32) {
     warp_instance_sum<NRV>(part, d, (int)threadIdx.x, acc);
@@ -1585,10 +1604,7 @@ __device__ int all_epilogues(const DevArrays& A, double* red) {
         if (j >= nb) continue;
         const InstDesc& d = A.inst[base + j];
         if (d.ntask > kWarpSumMax || phase_partials(s_ph[j]) == 0) continue;
-        for (int64_t t = lane; t < d.ntask; t += 32) {
-          acc[u][0] += __ldcg(&A.partials[(d.task0 + t) * kNR + 0]);
-          acc[u][1] += __ldcg(&A.partials[(d.task0 + t) * kNR + 1]);
-        }
+        strided_sum<2>(A.partials, d.task0, d.ntask, lane, 32, acc[u]);
       }
 #pragma unroll
       for (int u = 0; u < kEpiUnroll; ++u) {

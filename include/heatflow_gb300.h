@@ -103,7 +103,7 @@ typedef struct hf_solver_opts {
                            3 = as 1, but one graph launch per step (kernels visible to profilers,
                            which do not see kernels inside conditional nodes) */
   int32_t task_depth;   /* z-planes per task of the step kernels (0: 32, or 16/8/4 when the
-                           grids would give fewer than 456 tasks; otherwise 4..1024) */
+                           grids would give fewer than 912 tasks; otherwise 4..1024) */
 } hf_solver_opts;
 
 typedef struct hf_stats {
