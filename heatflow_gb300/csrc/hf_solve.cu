@@ -1529,7 +1529,7 @@ __device__ __forceinline__ int phase_partials(int32_t ph) {
 }
 
 constexpr int kScalWords = (int)(sizeof(InstScal) / 8);
-static_assert(sizeof(InstScal) % 8 == 0 && kScalWords <= kBlock, "scalar copy");
+static_assert(sizeof(InstScal) % 8 == 0 && kScalWords < kBlock, "scalar copy");
 
 // Epilogue of one instance after a round (one thread): scalars read through L2, updated, stored.
 // Returns whether the instance has work in the next round.
@@ -1726,6 +1726,7 @@ __global__ void __launch_bounds__(kBlock, 3)
   // several instances: every round starts with all their phases in shared memory, so tasks of
   // instances without work this round are passed over without reading their scalars
   const bool cache = A.ninst > 1 && A.ninst <= kPhaseCache;
+  const bool single = A.ninst == 1;
   if (blockIdx.x == 0 && threadIdx.x == 0) A.stamps[kStampSolve] = ctl->t_start = gtimer();
   for (int64_t r = 0;; ++r) {
     if (r >= limit) {
@@ -1734,14 +1735,18 @@ __global__ void __launch_bounds__(kBlock, 3)
     }
     // odd rounds walk the tasks backwards, so a round starts on the data the previous round wrote
     // last, which is still in L2 (the partial sums have fixed slots: the order changes no bits)
-    int cur = -1;
+    int cur = single ? 0 : -1;
     if (cache) {
       for (int i = threadIdx.x; i < (int)A.ninst; i += kBlock) s_phase[i] = __ldcg(&A.scal[i].phase);
     }
     // tasks are handed out one at a time from a counter, so a block on a busier SM takes fewer
     // (every SM holds the same number of blocks, but a round lasts as long as its slowest SM);
-    // each block asks for its next task while it runs the current one
+    // each block asks for its next task while it runs the current one.  With one instance its
+    // scalars are loaded beside the first request (threads 1..kScalWords), not after it.
     if (threadIdx.x == 0) s_next = atomicAdd(&ctl->next_task[r & 1], 1u);
+    if (single && threadIdx.x >= 1 && (int)threadIdx.x <= kScalWords)
+      reinterpret_cast<unsigned long long*>(&sh)[threadIdx.x - 1] =
+          __ldcg(reinterpret_cast<const unsigned long long*>(A.scal) + threadIdx.x - 1);
     __syncthreads();
     for (unsigned k = s_next; k < nt;) {
       __syncthreads();                       // every thread has read s_next
