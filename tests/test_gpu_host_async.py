@@ -239,14 +239,16 @@ def test_async_inputs_in_any_order(cuda_lib):
         assert np.array_equal(outs[k], ref[k]), k
 
 
-def test_early_start_checked_against_uploads(cuda_lib):
+@pytest.mark.parametrize("n,cell", [(16, 5), (16, 16 * 16 * 19 + 40), (15, 7)])
+def test_early_start_checked_against_uploads(cuda_lib, n, cell):
     """The second call's T^(n-1) is the first call's T^n array, which the caller changes after the
     first call (breaking the rule that queued arrays stay untouched): the second and third calls
     start early from the device's copy, the check of the uploaded bits finds the difference, and
     hf_host_sync runs both again from their uploaded inputs.  The results equal steps run from
-    those inputs with hf_set_state."""
+    those inputs with hf_set_state.  The changed cell lies in the bottom slab, in the heated top
+    slab, and on a grid whose rows are not 4k cells."""
     torch = pytest.importorskip("torch")
-    prob = layered_slab(16, nz=20, layer=5)
+    prob = layered_slab(n, nz=20, layer=5)
     tp, tpp = _initial(prob)
     a, b, c, d, e = (_pinned(prob.ncells, 0.0) for _ in range(5))
     a[:] = tp
@@ -254,7 +256,7 @@ def test_early_start_checked_against_uploads(cuda_lib):
     with HeatFlow(prob, **KW) as hf:
         hf.step_host_async(3, a, b, c)          # T^n = a, T^(n-1) = b -> c
         torch.cuda.synchronize()                # every copy of the first call has landed
-        a[5] += 0.25                            # the caller changes a queued array
+        a[cell] += 0.25                         # the caller changes a queued array
         hf.step_host_async(4, c, a, d)          # the rotation: starts early from the device copy
         hf.step_host_async(5, d, c, e)
         st = hf.host_sync()
