@@ -79,10 +79,10 @@ FP64_FLOPS_PER_CELL = {"residual_mixed": 15, "residual_fp64": 20, "residual_init
 # one the next residual sweep reads, the x update's (x, S^-1 in, x out: XB); when the solve went
 # on after it, the x it formed was not used and is not counted.
 PHASE_BYTES = {
-    "mixed": {"res_init": (56, 56), "res_init_hx": (32, 32), "res": (64, 64), "cg_p": (12, 8),
+    "mixed": {"res_init": (56, 56), "res_init_hx": (32, 32), "res": (64, 64), "cg_p": (12, 12),
               "cg_q": (20, 20), "cg_pq": (28, 24), "cg_b": (24, 20), "cg_bx": (24, 20),
               "xupd": (24, 16)},
-    "fp64": {"res_init": (64, 64), "res_init_hx": (40, 40), "res": (72, 72), "cg_p": (24, 16),
+    "fp64": {"res_init": (64, 64), "res_init_hx": (40, 40), "res": (72, 72), "cg_p": (24, 24),
              "cg_q": (40, 40), "cg_b": (48, 40), "cg_bx": (48, 40), "xupd": (32, 16)},
 }
 XB = {"mixed": 8 + 4 + 8, "fp64": 3 * 8}
@@ -117,7 +117,10 @@ def round_bytes_per_cell(rounds, precision):
             first_cg = first_b = True
             have_y = False
             bx = None
-        elif ph in ("cg_pq", "cg_p"):
+        elif ph == "cg_p":                        # iteration 0 has no direction round (p_0 = r)
+            b = full
+            first_cg = False
+        elif ph == "cg_pq":
             b = alt if first_cg else full
             first_cg = False
         elif ph == "cg_q":

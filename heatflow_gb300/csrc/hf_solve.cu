@@ -480,7 +480,8 @@ __device__ __forceinline__ void spmv_task(const DevArrays& A, double* part, int6
   const int64_t k = s.iter;
   const bool first = !FUSED || (k == 0);
   const T beta = (T)s.beta;
-  const T* Src = FUSED ? Vec<T>::r(A) + off : Vec<T>::pb(A, k) + off;   // r, or p itself
+  // r, or p itself (p_0 = r: the first iteration reads r, its direction update has no round)
+  const T* Src = (FUSED || k == 0) ? Vec<T>::r(A) + off : Vec<T>::pb(A, k) + off;
   const T* Po = Vec<T>::pb(A, k + 1) + off;
   T* Pn = Vec<T>::pb(A, k) + off;
   T* Q = Vec<T>::q(A) + off;
@@ -581,6 +582,7 @@ __device__ __forceinline__ void upd_task(const DevArrays& A, double* part, int64
   T* Y = Vec<T>::y(A) + off;
   T* R = Vec<T>::r(A) + off;
   const T* P = Vec<T>::pb(A, s.iter) + off;
+  T* P0 = Vec<T>::pb(A, 0) + off;            // p_0 = r, left for p_1 (as in upd4_task)
   const T* Q = Vec<T>::q(A) + off;
   const double* __restrict__ diag = A.diag + off;
   const bool act = c.act(0);
@@ -595,7 +597,8 @@ __device__ __forceinline__ void upd_task(const DevArrays& A, double* part, int64
         pv[u] = T(0); qv[u] = T(0); rv[u] = T(0); yv[u] = T(0);
         if (z0 + u < c.z1) {
           const int l = HF_IX(A, base + (z0 + u) * nxy, c.n());
-          pv[u] = P[l]; qv[u] = Q[l]; rv[u] = R[l];
+          qv[u] = Q[l]; rv[u] = R[l];
+          pv[u] = first ? rv[u] : P[l];
           if (!first) yv[u] = Y[l];
         }
       }
@@ -606,6 +609,7 @@ __device__ __forceinline__ void upd_task(const DevArrays& A, double* part, int64
         Y[l] = first ? alpha * pv[u] : fma(alpha, pv[u], yv[u]);
         const T r = fma(-alpha, qv[u], rv[u]);
         R[l] = r;
+        if (first) P0[l] = rv[u];
         rr = fma(r, r, rr);
         if (weighted) rw = fma(-diag[l] * (double)r, (double)r, rw);
       }
@@ -677,7 +681,7 @@ __device__ __forceinline__ void spmv4_task(const DevArrays& A, double* part, int
   const int64_t k = s.iter;
   const bool first = !FUSED || k == 0;
   const float beta = (float)s.beta;
-  const float* Src = FUSED ? A.r32 + off : ((k & 1) ? A.p232 : A.p32) + off;
+  const float* Src = (FUSED || k == 0) ? A.r32 + off : ((k & 1) ? A.p232 : A.p32) + off;
   const float* Po = (((k + 1) & 1) ? A.p232 : A.p32) + off;
   float* Pn = ((k & 1) ? A.p232 : A.p32) + off;
   float* Q = A.q32 + off;
@@ -879,7 +883,10 @@ __device__ __forceinline__ void upd4_task(const DevArrays& A, double* part, int6
   const bool first = (s.iter == 0);
   T* Y = Vec<T>::y(A) + c.voff;
   T* R = Vec<T>::r(A) + c.voff;
+  // p_0 = r has no round of its own: the first update takes p from r and leaves it in the
+  // direction buffer of iteration 0 (p_1 = r_1 + beta p_0 reads it there)
   const T* P = Vec<T>::pb(A, s.iter) + c.voff;
+  T* P0 = Vec<T>::pb(A, 0) + c.voff;
   const T* Q = Vec<T>::q(A) + c.voff;
   const double* __restrict__ diag = A.diag + c.off;
   T rr = T(0);
@@ -894,7 +901,8 @@ __device__ __forceinline__ void upd4_task(const DevArrays& A, double* part, int6
     const float sig = (float)s.sigma_prev;
     for (int z = c.za; z < c.zb; ++z) {
       const int l = HF_IX4(A, c.lxy + z * c.nxy, c.vn);
-      const V4<T> pv = ldv4(P + l), qv = ldv4(Q + l), rv = ldv4(R + l);
+      const V4<T> qv = ldv4(Q + l), rv = ldv4(R + l);
+      const V4<T> pv = first ? rv : ldv4(P + l);
       V4<T> yv{};
       if (!first) yv = ldv4(Y + l);
       V4<double> xv = ldv4(XR + l), sv{};
@@ -913,16 +921,19 @@ __device__ __forceinline__ void upd4_task(const DevArrays& A, double* part, int6
       stv4(Y + l, yo);
       stv4(R + l, ro);
       stv4(XW + l, xv);
+      if (first) stv4(P0 + l, rv);
     }
   } else if (c.act) {
     for (int z = c.za; z < c.zb; z += 2) {
       const bool two = z + 1 < c.zb;
       const int l0 = HF_IX4(A, c.lxy + z * c.nxy, c.vn);
       const int l1 = two ? HF_IX4(A, l0 + c.nxy, c.vn) : 0;
-      V4<T> p0 = ldv4(P + l0), q0 = ldv4(Q + l0), r0 = ldv4(R + l0), y0{}, p1{}, q1{}, r1{}, y1{};
+      V4<T> q0 = ldv4(Q + l0), r0 = ldv4(R + l0), p0{}, y0{}, p1{}, q1{}, r1{}, y1{};
+      p0 = first ? r0 : ldv4(P + l0);
       if (!first) y0 = ldv4(Y + l0);
       if (two) {
-        p1 = ldv4(P + l1); q1 = ldv4(Q + l1); r1 = ldv4(R + l1);
+        q1 = ldv4(Q + l1); r1 = ldv4(R + l1);
+        p1 = first ? r1 : ldv4(P + l1);
         if (!first) y1 = ldv4(Y + l1);
       }
 #pragma unroll
@@ -946,6 +957,7 @@ __device__ __forceinline__ void upd4_task(const DevArrays& A, double* part, int6
         }
         stv4(Y + l, yo);
         stv4(R + l, ro);
+        if (first) stv4(P0 + l, rv);
       }
     }
   }
@@ -1150,7 +1162,7 @@ __global__ void __launch_bounds__(kBlock) k_xupdate(DevArrays A) {
 template <typename T>
 __global__ void __launch_bounds__(kBlock) k_cg_p(DevArrays A) {
   const InstScal& s = A.scal[A.tasks[blockIdx.x].x];
-  if (!s.inner_active) return;
+  if (!s.inner_active || s.iter == 0) return;   // p_0 = r: the SpMV and the update read r
   cgp_any<T>(A, A.partials, blockIdx.x, s);
 }
 
@@ -1520,7 +1532,8 @@ __device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
 template <typename T>
 __device__ __forceinline__ int32_t phase_after(const InstScal& s) {
   if (!s.outer_active) return PH_IDLE;
-  if (s.inner_active) return PH_CG_P;   // the fused FP32 pass (PH_CG_PQ) measured slower
+  // the fused FP32 pass (PH_CG_PQ) measured slower; iteration 0 needs no direction update (p_0 = r)
+  if (s.inner_active) return s.iter == 0 ? PH_CG_Q : PH_CG_P;
   return (s.xw & kXwDone) ? PH_RES : PH_XUPD;   // the last CG update may have formed x already
 }
 __device__ __forceinline__ int phase_partials(int32_t ph) {
